@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark of the light-probe bake on GB300.
+
+Workload (one "step"): bake the 16x16x16 probe grid of the 64-box scene (778
+triangles, open unit room, seeded sun + 128^2 cubemap sky) with 256 shared
+Fibonacci directions per probe, L2 SH -- 1,048,576 primary rays plus the sun
+shadow rays.  The chosen path (fused trace + projection, FP32) is timed with
+inputs resident in HBM; the plain FP32 path (radiance tile + projection, the
+drop-in) is timed beside it; `e2e` times the public C-ABI call with pinned host
+probe positions in and host SH out.  L2 is flushed (256 MiB write) before every
+timed step; each step is bracketed by CUDA events on the context's stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  Under torchrun each rank bakes its own replica of the
+workload (probes are independent: weak scaling, no data-path collective); the
+max step time over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "vulkan-light-bakery_gb300"
+sys.path.insert(0, str(PKG))
+
+SEED = 1
+NBOXES = 64
+GRID = (16, 16, 16)
+NDIRS = 256
+LMAX = 2
+SKY_N = 128
+WORKLOAD = "probe bake 16^3 probes x 256 Fibonacci dirs, 64-box scene (778 tris), sun + 128^2 cubemap sky, L2 SH"
+METRIC_FULL = "probes/s, Grays/s, p99 bake latency: chosen vs plain FP32, <=1e-4 SH rel err"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
+    return ap.parse_args()
+
+
+def workload_inputs():
+    import vlb
+
+    pos, idx, alb = vlb.synth_box_scene(SEED, NBOXES)
+    sky = vlb.synth_cubemap(SEED, SKY_N)
+    sun = vlb.synth_sun(SEED)
+    bounds = np.concatenate([np.minimum(pos.min(0), 0), np.maximum(pos.max(0), 0)]).astype(np.float32)
+    probes, _ = vlb.probe_grid_ref_order(bounds, GRID)
+    return pos, idx, alb, sky, sun, probes
+
+
+def cpu_time_oracle(pos, idx, alb, sky, sun, probes, nthreads):
+    """Times the FP64 CPU restatement (the oracle) on all host threads."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    d32, w = O.dirs_fibonacci(NDIRS)
+    B = O.basis_matrix(d32.astype(np.float64), w, LMAX)
+    sc = O.Scene(pos, idx, alb)
+    t0 = time.perf_counter()
+    out = sc.bake(probes, d32, B, sun, sky=sky, sky_n=SKY_N, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return out, dt
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for ln in f.read_text().splitlines():
+            if ln.startswith(f"traffic_bytes_per_launch[{kernel}]:"):
+                try:
+                    return float(ln.split(":", 1)[1].split()[0])
+                except ValueError:
+                    pass
+    return None
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return None
+    pos, idx, alb, sky, sun, probes = workload_inputs()
+    nthreads = os.cpu_count() or 1
+    sample = probes[: args.cpu_probes]
+    for _ in range(args.warmup):
+        cpu_time_oracle(pos, idx, alb, sky, sun, sample[:64], nthreads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_time_oracle(pos, idx, alb, sky, sun, sample, nthreads)
+        times.append(dt)
+    pps = len(sample) * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": "probes/s", "metric_full": METRIC_FULL, "value": pps, "unit": "probes/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "probes_per_step": len(sample), "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": pps, "unit": "probes/s", "cores": nthreads, "kind": "port",
+                         "sample": f"first {len(sample)} of {len(probes)} probes, {NDIRS} dirs each, per step"},
+        "e2e": {"value": pps, "unit": "probes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference bake needs Vulkan ray tracing (unavailable on this box); its math runs here as "
+                "the FP64 multithreaded CPU restatement",
+    }
+    return line
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return 0
+    assert args.warmup >= 3, "at least 3 warm-up steps"
+    import torch
+
+    import vlb
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    # a dedicated stream: the library runs on it and the torch events record on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = vlb.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    pos, idx, alb, sky, sun, probes = workload_inputs()
+    scene = ctx.scene(pos, idx, alb)
+    dirs = ctx.fibonacci(NDIRS)
+    skyh = ctx.sky(sky, SKY_N)
+    P = probes.shape[0]
+    K = vlb.k_of(LMAX)
+    d_probes = torch.from_numpy(probes).cuda()
+    d_out = torch.empty((P, K, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    params = {
+        "fused": vlb.bake_params(dirs, LMAX, vlb.PREC_FUSED, sun, sky=skyh),
+        "fp32": vlb.bake_params(dirs, LMAX, vlb.PREC_FP32, sun, sky=skyh),
+    }
+    chosen = "fused"
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(pname: str, steps: int, profile: bool = False):
+        p = params[pname]
+        ctx.set_profiling(profile)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        barrier()
+        torch.cuda.synchronize()
+        l0 = ctx.launch_count
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            ctx.bake(scene, d_probes, p, out=d_out)
+            b.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ctx.set_profiling(False)
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return ms, ctx.launch_count - l0
+
+    for name in params:
+        timed(name, args.warmup)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_chosen, launches = timed(chosen, args.steps)
+    ms_plain, _ = timed("fp32", args.steps)
+    clk = clocks.stop()
+    res_chosen = d_out.cpu().numpy().copy()
+    # per-kernel device time of the chosen path (library events on the same stream)
+    ctx.profile_reset()
+    timed(chosen, min(args.steps, 20), profile=True)
+    prof = ctx.profile()
+    # per-ray work counts for the algorithmic bytes (one debug bake, untimed)
+    _, hit, vis, _ = ctx.bake(scene, probes, params["fp32"], debug=True)
+    shadow_rays = int((vis != 2).sum())
+
+    def agg(ms):
+        t = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    tot_chosen = agg(ms_chosen)
+    tot_plain = agg(ms_plain)
+    value = world * P * args.steps / (tot_chosen / 1e3)
+    plain = world * P * args.steps / (tot_plain / 1e3)
+
+    # e2e: public call with pinned host buffers (H2D probes, D2H SH) inside the timed region
+    h_probes = torch.from_numpy(probes).pin_memory()
+    h_out = torch.empty((P, K, 3), dtype=torch.float32).pin_memory()
+    for _ in range(3):
+        ctx.bake(scene, h_probes, params[chosen], out=h_out)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.bake(scene, h_probes, params[chosen], out=h_out)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_value = world * P * args.steps / (agg(e2e_ms) / 1e3)
+
+    if rank != 0:
+        return 0
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # roofline of the dominant kernel: algorithmic bytes = per-ray node + triangle fetches
+    kname = "trace_fused"
+    klaunch, kms = prof.get(kname, (0, 0.0))
+    k_avg_ms = kms / max(klaunch, 1)
+    rays_primary = P * NDIRS
+    stats = ctx_trace_stats(ctx, scene, probes, params["fp32"])
+    bytes_per_launch = stats["bytes"]
+    achieved = bytes_per_launch / (k_avg_ms * 1e-3) / 1e9 if k_avg_ms > 0 else None
+    traffic = load_traffic(kname)
+    step_ms = sorted(ms_chosen)
+    p50 = step_ms[len(step_ms) // 2]
+    p99 = step_ms[min(len(step_ms) - 1, int(round(0.99 * (len(step_ms) - 1))))]
+    # CPU baseline: the FP64 restatement on a bounded probe sample, all host threads
+    sample = probes[: args.cpu_probes]
+    ref_sh, cpu_dt = cpu_time_oracle(pos, idx, alb, sky, sun, sample, os.cpu_count() or 1)
+    got = res_chosen[: len(sample)].astype(np.float64)
+    err = np.linalg.norm((got - ref_sh).reshape(len(sample), -1), axis=1) / np.maximum(
+        np.linalg.norm(ref_sh.reshape(len(sample), -1), axis=1), 1e-30)
+    line = {
+        "metric": "probes/s", "metric_full": METRIC_FULL, "value": value, "unit": "probes/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_chosen / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 scene, sky and sun)",
+        "config": {"workload": WORKLOAD, "probes": P, "dirs_per_probe": NDIRS, "triangles": int(idx.shape[0]),
+                   "lmax": LMAX, "path": "fused trace+projection FP32",
+                   "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
+        "grays_per_s": value * NDIRS / 1e9, "grays_incl_shadow_per_s": value * (NDIRS + shadow_rays / P) / 1e9,
+        "latency_ms": {"p50": p50, "p99": p99},
+        "plain_fp32": {"value": plain, "unit": "probes/s", "p99_ms": sorted(ms_plain)[-1]},
+        "sh_rel_err_vs_fp64": {"max": float(err.max()), "mean": float(err.mean()), "probes": len(sample)},
+        "e2e": {"value": e2e_value, "unit": "probes/s", "h2d_bytes_per_step": int(P * 12),
+                "d2h_bytes_per_step": int(P * K * 12)},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": k_avg_ms,
+                     "nodes_per_ray": stats["nodes_per_ray"], "tris_per_ray": stats["tris_per_ray"],
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
+        "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)} for k, v in prof.items()},
+        "cpu_baseline": {"value": len(sample) / cpu_dt, "unit": "probes/s", "cores": os.cpu_count() or 1,
+                         "kind": "port", "sample": f"first {len(sample)} of {P} probes, {NDIRS} dirs each"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def ctx_trace_stats(ctx, scene, probes, params):
+    """Nodes visited and triangles tested per ray (instrumented bake)."""
+    import vlb
+
+    st = vlb.trace_stats(ctx, scene, probes, params)
+    rays = st["rays"]
+    return {"bytes": st["nodes"] * 64 + st["tris"] * 48, "nodes_per_ray": st["nodes"] / rays,
+            "tris_per_ray": st["tris"] / rays}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,242 @@
+/* vlb.h -- C ABI of the GB300 light-probe baker (libvlb.so).
+ *
+ * This is the drop-in boundary for the bake path of vulkan-light-bakery.
+ * Plain pointers and sizes only; no C++ or torch types cross it.  Every
+ * function returns a vlb_status; no exception leaves the library.  Each
+ * declaration names the reference interface it replaces (paths inside the
+ * reference project).
+ *
+ * Memory: every array argument may be host memory (pageable or pinned) or
+ * device memory of the context's GPU; the library inspects each pointer.
+ * A call whose outputs are all device pointers is asynchronous on the
+ * context's stream; a call with a host output returns after the result is in
+ * host memory.  Input and output arrays are never retained after a call.
+ * A context is externally synchronised: one thread at a time, and calls on
+ * one context run in stream order.
+ */
+#ifndef VLB_H
+#define VLB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VLB_VERSION 1u
+
+/* Replaces the reference's C++ exceptions (std::runtime_error, vk::SystemError,
+ * caught in src/baker/main.cpp:26-40) and the printed-only fence failure of
+ * src/application.cpp:266-273. */
+typedef enum vlb_status {
+  VLB_OK = 0,
+  VLB_ERR_INVALID = 1,     /* bad argument (message in vlb_last_error) */
+  VLB_ERR_OOM = 2,         /* device or host allocation failed */
+  VLB_ERR_TIMEOUT = 3,     /* a bounded device wait gave up */
+  VLB_ERR_CUDA = 4,        /* CUDA runtime error */
+  VLB_ERR_UNSUPPORTED = 5, /* valid request this build does not implement */
+  VLB_ERR_INTERNAL = 6     /* a device-side check fired (e.g. BVH stack overflow) */
+} vlb_status;
+
+typedef struct vlb_ctx vlb_ctx;
+typedef struct vlb_scene vlb_scene;
+typedef struct vlb_dirset vlb_dirset;
+typedef struct vlb_sky vlb_sky;
+
+/* ---- context ------------------------------------------------------------
+ * Replaces Application::Application (src/application.cpp:540-560): device,
+ * queues and command pools become one CUDA device + one stream. */
+uint32_t vlb_version(void);
+const char* vlb_status_string(vlb_status s);
+vlb_status vlb_ctx_create(int device, vlb_ctx** out);
+void vlb_ctx_destroy(vlb_ctx* ctx);
+/* Run the context's work on a caller-owned cudaStream_t (NULL restores the
+ * context's own stream). */
+vlb_status vlb_ctx_set_stream(vlb_ctx* ctx, void* cuda_stream);
+void* vlb_ctx_get_stream(vlb_ctx* ctx);
+vlb_status vlb_ctx_synchronize(vlb_ctx* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* vlb_last_error(const vlb_ctx* ctx);
+
+/* Per-kernel timing: when enabled, every kernel the library launches is
+ * bracketed by CUDA events on the context's stream. */
+typedef struct vlb_kernel_time {
+  char name[48];
+  uint32_t launches;
+  double total_ms;
+} vlb_kernel_time;
+vlb_status vlb_ctx_set_profiling(vlb_ctx* ctx, int enable);
+/* Synchronises, fills up to cap entries, returns the count in *n. */
+vlb_status vlb_ctx_profile_read(vlb_ctx* ctx, vlb_kernel_time* out, uint32_t cap, uint32_t* n);
+vlb_status vlb_ctx_profile_reset(vlb_ctx* ctx);
+/* Kernels launched by the library on this context since creation. */
+uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx);
+
+/* ---- probe grid -----------------------------------------------------------
+ * Replaces LightBaker::probePositionsFromBoudingBox
+ * (src/baker/light_baker.cpp:138-159): same FP32 arithmetic, same order (the
+ * grid is grown one axis at a time: x runs first, then each existing probe is
+ * repeated along y, then along z).  bounds = {min xyz, max xyz}; out_xyz
+ * holds counts[0]*counts[1]*counts[2]*3 floats; grid_step may be NULL. */
+vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts[3], float* out_xyz,
+                                    float grid_step[3]);
+
+/* ---- scene ------------------------------------------------------------------
+ * Replaces SceneManager::pushScene + Scene_t::buildAccelerationStructures
+ * (src/scene_manager.cpp:1013-1034, :339-443): the hardware BLAS/TLAS becomes
+ * a Morton LBVH built on the device (bit-exact with a CPU build).
+ * positions: nverts vertices, position_stride_bytes apart (12 for packed xyz,
+ * 48 for the reference's shader::Vertex, shaders/structures.h:20-26).
+ * indices: ntris*3 u32.  tri_albedo: ntris*3 linear RGB, or NULL for 1. */
+vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t position_stride_bytes, uint32_t nverts,
+                            const uint32_t* indices, uint32_t ntris, const float* tri_albedo, vlb_scene** out);
+void vlb_scene_destroy(vlb_scene* scene);
+uint32_t vlb_scene_triangle_count(const vlb_scene* scene);
+/* Replaces Scene_t::getBounds (src/scene_manager.hpp:214, cpp:497-507).  The
+ * reference starts its bounds at the origin, so include_origin=1 reproduces
+ * it; 0 gives the plain vertex bounds. */
+vlb_status vlb_scene_bounds(const vlb_scene* scene, int include_origin, float out[6]);
+/* Copies the device LBVH to host arrays (any may be NULL): sorted Morton
+ * codes [n], sorted triangle order [n], children [2(n-1)] (c >= 0 internal
+ * node, c < 0 leaf ~c), boxes [(2n-1)*6] (internal nodes then leaves). */
+vlb_status vlb_scene_bvh_export(const vlb_scene* scene, uint32_t* codes, uint32_t* order, int32_t* children,
+                                float* boxes);
+uint64_t vlb_scene_device_bytes(const vlb_scene* scene);
+
+/* ---- sample direction sets -------------------------------------------------
+ * A direction set is the rays every probe casts and the projection basis
+ * that goes with them: trace direction d_s, basis direction b_s, weight w_s.
+ * The projection is c_k = sum_s w_s Y_k(b_s) L(d_s). */
+typedef enum vlb_frame {
+  VLB_FRAME_WORLD = 0, /* basis evaluated at the traced direction */
+  VLB_FRAME_XZY = 1    /* basis evaluated at the traced direction's .xzy */
+} vlb_frame;
+/* Spherical Fibonacci set of n directions, weight 4*pi/n. */
+vlb_status vlb_dirset_create_fibonacci(vlb_ctx* ctx, uint32_t n, vlb_frame frame, vlb_dirset** out);
+/* The reference's own sample set: one ray per w x h equirect pixel traced
+ * along toVector(x2phi, y2theta).xzy (shaders/env_map.rgen:18-28) and
+ * projected with the un-swizzled direction and weight (2pi/w)(pi/h)sin(theta)
+ * (shaders/sh.comp:27-41).  Sample index s = y*w + x. */
+vlb_status vlb_dirset_create_equirect(vlb_ctx* ctx, uint32_t w, uint32_t h, vlb_dirset** out);
+/* Caller-defined set: n trace directions (xyz, unit length), optional basis
+ * directions (NULL: the trace directions) and weights (FP64). */
+vlb_status vlb_dirset_create(vlb_ctx* ctx, const float* trace_dirs, const float* basis_dirs, const double* weights,
+                             uint32_t n, vlb_dirset** out);
+void vlb_dirset_destroy(vlb_dirset* dirs);
+uint32_t vlb_dirset_count(const vlb_dirset* dirs);
+/* trace_dirs: n*3 FP32 as traced on the device; basis: n*16 FP32 weighted
+ * basis values w_s*Y_k(b_s) (k = l(l+1)+m, l <= 3). Either may be NULL. */
+vlb_status vlb_dirset_export(const vlb_dirset* dirs, float* trace_dirs, float* basis);
+
+/* ---- skybox SH --------------------------------------------------------------
+ * Replaces SkyboxManager::pushSkybox -> Skybox_t::computeSH
+ * (src/skybox_manager.cpp:284-298, :107-130) and its shader
+ * shaders/skybox_sh.comp.  Output: K x 3 FP32, K = (lmax+1)^2, coefficient
+ * k = l(l+1)+m, RGB innermost (the reference's vec3 coeffs[16], scalar
+ * layout).  lmax = 3 gives the reference's 16 coefficients. */
+typedef enum vlb_sky_layout {
+  VLB_SKY_CUBEMAP = 0,  /* 6 faces (+X,-X,+Y,-Y,+Z,-Z) of w x w texels, exact texel solid angles */
+  VLB_SKY_PANORAMA = 1, /* w x h panorama, shaders/skybox_sh.comp:27-39 (phi - pi/2, basis at .xzy) */
+  VLB_SKY_ENVMAP = 2    /* w x h equirect env map, shaders/sh.comp:27-39 */
+} vlb_sky_layout;
+typedef enum vlb_texel_format {
+  VLB_TEXEL_RGB32F = 0, /* 3 floats per texel */
+  VLB_TEXEL_RGBA8 = 1   /* 4 bytes per texel, UNORM (value/255), alpha ignored */
+} vlb_texel_format;
+/* flags: swap R and B, as the reference does by uploading RGBA bytes into a
+ * B8G8R8A8 image (src/skybox_manager.cpp:18, src/application.cpp:690). */
+#define VLB_SKY_REF_BGRA_SWAP 1u
+vlb_status vlb_skybox_sh(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt, vlb_sky_layout layout, uint32_t w,
+                         uint32_t h, uint32_t lmax, uint32_t flags, float* out);
+/* count maps stored back to back; out holds count*K*3 floats. */
+vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt, vlb_sky_layout layout,
+                                 uint32_t w, uint32_t h, uint32_t count, uint32_t lmax, uint32_t flags, float* out);
+
+/* Resident cubemap sky used on ray misses during a bake (the reference's
+ * miss shader shaders/main.rmiss:37-41 reads an unbound set; this defines
+ * it): nearest-texel lookup of a 6 x n x n RGB FP32 cubemap. */
+vlb_status vlb_sky_create(vlb_ctx* ctx, const float* cubemap_rgb, uint32_t n, vlb_sky** out);
+void vlb_sky_destroy(vlb_sky* sky);
+
+/* ---- bake ---------------------------------------------------------------------
+ * Replaces LightBaker::bake (src/baker/light_baker.cpp:345-386) with its
+ * per-probe EnvMapGenerator::getMap (src/baker/env_map_generator.cpp:325-359:
+ * env_map.rgen -> traversal -> env_map.rchit / shadow.rmiss / main.rmiss)
+ * and dispatchBakingKernel (sh.comp).  probe_xyz: nprobes*3.  out: nprobes x
+ * K x 3 FP32, probe-major, coefficient k = l(l+1)+m, RGB innermost; with
+ * lmax = 3 this is byte-for-byte the reference's 192-byte-per-probe layout
+ * (light_baker.cpp:352-379), each probe's own sum (the reference never clears
+ * its accumulator between probes; that carry-over is not reproduced). */
+typedef enum vlb_precision {
+  VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 projection */
+  VLB_PREC_FUSED = 1, /* trace + projection in one kernel, FP32 */
+  VLB_PREC_MIXED = 2  /* BF16 radiance tile, tcgen05 projection with split BF16 basis */
+} vlb_precision;
+
+typedef struct vlb_bake_params {
+  uint32_t lmax;          /* 2: 9 coefficients, 3: 16 (the reference) */
+  uint32_t precision;     /* vlb_precision */
+  uint32_t flags;         /* reserved, 0 */
+  float sun_dir[3];       /* direction toward the sun (normalised by the library) */
+  float sun_intensity;    /* hit radiance = albedo * intensity/pi * max(0, n.l) * visibility */
+  float tmin, tmax;       /* primary ray interval; shaders/env_map.rgen:22-23 use .001, 10000 */
+  float shadow_bias;      /* shadow origin offset along the normal; shaders/env_map.rchit:81 uses .005 */
+  const vlb_dirset* dirs; /* required */
+  const vlb_sky* sky;     /* NULL: black sky */
+} vlb_bake_params;
+void vlb_bake_params_default(vlb_bake_params* p);
+
+/* Per-ray outputs for parity checks (any may be NULL; host or device):
+ * ray r = probe*S + s.  hit_tri: original triangle index or -1.  shadow: 0
+ * occluded, 1 lit, 2 no shadow ray (miss or n.l <= 0).  radiance: r*3 RGB. */
+typedef struct vlb_bake_debug {
+  int32_t* hit_tri;
+  uint8_t* shadow;
+  float* radiance;
+} vlb_bake_debug;
+
+vlb_status vlb_bake(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                    const vlb_bake_params* params, float* out);
+vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                       const vlb_bake_params* params, float* out, const vlb_bake_debug* debug);
+/* Measurement aid (no reference counterpart; the reference's traversal is
+ * inside the driver): one instrumented bake of the same rays, counting
+ * out[0] primary rays, out[1] shadow rays, out[2] BVH nodes fetched (64 B
+ * each), out[3] triangles tested (48 B each).  Host output. */
+vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                                const vlb_bake_params* params, uint64_t out[4]);
+
+/* ---- projection and reconstruction ----------------------------------------
+ * Replaces dispatchBakingKernel / shaders/sh.comp:23-42 for a radiance tile
+ * laid out [nprobes][3][S] (S = the direction set's count): out nprobes x K x
+ * 3.  dtype selects FP32 or BF16 radiance. */
+typedef enum vlb_dtype { VLB_DTYPE_F32 = 0, VLB_DTYPE_BF16 = 1 } vlb_dtype;
+vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint32_t nprobes, const vlb_dirset* dirs,
+                       uint32_t lmax, float* out);
+/* Replaces shaders/sh_sum.comp:35-52: out[y][x] = scale * sum_k c_k
+ * Y_k(toVector(x2phi(x), y2theta(y))) as w*h*3 FP32 (the reference uses
+ * scale 1250). coeffs: K x 3. */
+vlb_status vlb_sh_eval_envmap(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, uint32_t w, uint32_t h, float scale,
+                              float* out);
+
+/* ---- synthetic inputs (bench and tests) -------------------------------------
+ * Seeded SplitMix64 generators for the benchmark workloads.  The room is the
+ * unit box [0,1]^3 open at +Y (10 triangles, albedo 0.5); each box has its
+ * centre uniform in [0.1,0.9]^3, edges uniform in [0.05,0.2] per axis and
+ * albedo uniform in [0.2,0.8] per channel (12 triangles).  Outputs: positions
+ * (nverts*3), indices (ntris*3), per-triangle albedo (ntris*3); call with
+ * NULL arrays to get the counts. */
+vlb_status vlb_synth_box_scene(uint64_t seed, uint32_t nboxes, float* positions, uint32_t* indices, float* albedo,
+                               uint32_t* nverts, uint32_t* ntris);
+/* 6 x n x n RGB FP32 cubemap: 0.3 + three spherical Gaussian lobes, lobe
+ * direction uniform on the sphere, sharpness uniform in [20,200], RGB
+ * intensity uniform in [1,50]. */
+vlb_status vlb_synth_cubemap(uint64_t seed, uint32_t n, float* out);
+/* Unit direction uniform on the upper (+Y) hemisphere. */
+vlb_status vlb_synth_sun(uint64_t seed, float out_dir[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VLB_H */

@@ -1,0 +1,768 @@
+// vlb_oracle.cpp -- FP64 CPU restatement of the light-probe bake path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle for the CUDA
+// library and the timed CPU baseline of bench.py.  Only tests/, the smoke check
+// in __graft_entry__.py and the cpu_baseline / reference legs of bench.py load
+// it.  The product library never links, calls or falls back to it.
+//
+// Parity anchors (paths within the reference project):
+//   * SH basis, PI, x2phi/y2theta/toVector ......... shaders/sh_common.h:1-223
+//     (pinned against the reference header itself, compiled by oracle/Makefile
+//     into oracle/_ref/libshref.so, and against tests/golden fixtures)
+//   * reference bake ray setup (.xzy) ............... shaders/env_map.rgen:18-28
+//   * per-probe projection, weights, k=l(l+1)+m ..... shaders/sh.comp:23-42
+//   * skybox projection (phi - PI/2, basis at .xzy) . shaders/skybox_sh.comp:23-42
+//   * SH reconstruction (x1250) ..................... shaders/sh_sum.comp:35-52
+//   * probe grid order .............................. src/baker/light_baker.cpp:138-159
+//   * closest-hit + shadow ray structure ............ shaders/env_map.rchit:51-102,
+//                                                     shaders/shadow.rmiss:6-9
+// Pieces the reference does not have (cubemap solid angle, Fibonacci sphere
+// directions, Lambert+sun shading, the Morton LBVH) follow the published math
+// named at each function.  Those parts are "parity unpinned" against the
+// reference (no reference test or golden vector exists for them).
+//
+// Build with -ffp-contract=off: the few FP32 steps that must be bit-exact with
+// the device (Morton quantisation, cubemap texel selection, the probe grid)
+// rely on every operation being rounded on its own.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr double kPiRef = 3.1415926538;  // sh_common.h:1 (the reference's own PI)
+
+// --------------------------------------------------------------------------
+// SH basis, sh_common.h:26-152.  Same 6-digit constants, evaluated in FP64.
+// Index k = l(l+1)+m (sh.comp:39).
+// --------------------------------------------------------------------------
+int sh_count(int lmax) { return (lmax + 1) * (lmax + 1); }
+
+void sh_basis(int lmax, double x, double y, double z, double* o) {
+  o[0] = 0.282095;
+  if (lmax < 1) return;
+  o[1] = -0.488603 * y;
+  o[2] = 0.488603 * z;
+  o[3] = -0.488603 * x;
+  if (lmax < 2) return;
+  o[4] = 1.092548 * x * y;
+  o[5] = -1.092548 * y * z;
+  o[6] = 0.315392 * (-x * x - y * y + 2.0 * z * z);
+  o[7] = -1.092548 * x * z;
+  o[8] = 0.546274 * (x * x - y * y);
+  if (lmax < 3) return;
+  o[9] = -0.590044 * y * (3.0 * x * x - y * y);
+  o[10] = 2.890611 * x * y * z;
+  o[11] = -0.457046 * y * (4.0 * z * z - x * x - y * y);
+  o[12] = 0.373176 * z * (2.0 * z * z - 3.0 * x * x - 3.0 * y * y);
+  o[13] = -0.457046 * x * (4.0 * z * z - x * x - y * y);
+  o[14] = 1.445306 * z * (x * x - y * y);
+  o[15] = -0.590044 * x * (x * x - 3.0 * y * y);
+  if (lmax < 4) return;
+  const double x2 = x * x, y2 = y * y, z2 = z * z;
+  o[16] = 2.503343 * x * y * (x2 - y2);
+  o[17] = -1.770131 * y * z * (3.0 * x2 - y2);
+  o[18] = 0.946175 * x * y * (7.0 * z2 - 1.0);
+  o[19] = -0.669047 * y * z * (7.0 * z2 - 3.0);
+  o[20] = 0.105786 * (35.0 * z2 * z2 - 30.0 * z2 + 3.0);
+  o[21] = -0.669047 * x * z * (7.0 * z2 - 3.0);
+  o[22] = 0.473087 * (x2 - y2) * (7.0 * z2 - 1.0);
+  o[23] = -1.770131 * x * z * (x2 - 3.0 * y2);
+  o[24] = 0.625836 * (x2 * (x2 - 3.0 * y2) - y2 * (3.0 * x2 - y2));
+}
+
+// sh_common.h:8-22
+double x2phi(int x, int w) { return 2.0 * kPiRef * (double(x) + 0.5) / double(w); }
+double y2theta(int y, int h) { return kPiRef * (double(y) + 0.5) / double(h); }
+void to_vector(double phi, double theta, double* d) {
+  const double r = std::sin(theta);
+  double v[3] = {r * std::cos(phi), r * std::sin(phi), std::cos(theta)};
+  const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  d[0] = v[0] / n; d[1] = v[1] / n; d[2] = v[2] / n;
+}
+
+// --------------------------------------------------------------------------
+// Cubemap conventions (the reference declares Skybox_t::Type::eCubemap,
+// skybox_manager.hpp:18-23, but never implements it).  Faces +X,-X,+Y,-Y,+Z,-Z,
+// texel (x, y) row-major per face, the OpenGL major-axis table.
+// --------------------------------------------------------------------------
+void cube_face_dir(int face, double u, double v, double* d) {
+  switch (face) {
+    case 0: d[0] = 1.0; d[1] = -v; d[2] = -u; break;
+    case 1: d[0] = -1.0; d[1] = -v; d[2] = u; break;
+    case 2: d[0] = u; d[1] = 1.0; d[2] = v; break;
+    case 3: d[0] = u; d[1] = -1.0; d[2] = -v; break;
+    case 4: d[0] = u; d[1] = -v; d[2] = 1.0; break;
+    default: d[0] = -u; d[1] = -v; d[2] = -1.0; break;
+  }
+  const double n = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  d[0] /= n; d[1] /= n; d[2] /= n;
+}
+
+// Exact solid angle of the face rectangle [u0,u1]x[v0,v1] on the z=1 plane:
+// integral of (1+u^2+v^2)^(-3/2) du dv has the antiderivative
+// atan2(u*v, sqrt(u^2+v^2+1)).
+double area_element(double u, double v) { return std::atan2(u * v, std::sqrt(u * u + v * v + 1.0)); }
+double cube_texel_solid_angle(uint32_t n, uint32_t x, uint32_t y) {
+  const double s = 2.0 / double(n);
+  const double u0 = -1.0 + s * x, u1 = u0 + s, v0 = -1.0 + s * y, v1 = v0 + s;
+  return area_element(u0, v0) - area_element(u0, v1) - area_element(u1, v0) + area_element(u1, v1);
+}
+
+// Nearest-texel cubemap lookup.  Every step is one IEEE FP32 operation so the
+// device (which uses __fdiv_rn / __fadd_rn / __fmul_rn) picks the same texel.
+void cube_select(float x, float y, float z, uint32_t n, uint32_t* face, uint32_t* tx, uint32_t* ty) {
+  const float ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
+  float sc, tc, ma;
+  uint32_t f;
+  if (ax >= ay && ax >= az) {
+    if (x >= 0.f) { f = 0; sc = -z; tc = -y; ma = ax; } else { f = 1; sc = z; tc = -y; ma = ax; }
+  } else if (ay >= az) {
+    if (y >= 0.f) { f = 2; sc = x; tc = z; ma = ay; } else { f = 3; sc = x; tc = -z; ma = ay; }
+  } else {
+    if (z >= 0.f) { f = 4; sc = x; tc = -y; ma = az; } else { f = 5; sc = -x; tc = -y; ma = az; }
+  }
+  volatile float u = sc / ma;
+  volatile float v = tc / ma;
+  volatile float fu = u + 1.0f;
+  volatile float fv = v + 1.0f;
+  fu = fu * 0.5f; fv = fv * 0.5f;
+  fu = fu * float(n); fv = fv * float(n);
+  int ix = int(std::floor(fu)), iy = int(std::floor(fv));
+  ix = std::min(std::max(ix, 0), int(n) - 1);
+  iy = std::min(std::max(iy, 0), int(n) - 1);
+  *face = f; *tx = uint32_t(ix); *ty = uint32_t(iy);
+}
+
+// --------------------------------------------------------------------------
+// Ray / triangle (Moller-Trumbore 1997) in FP64, inclusive edges.
+// --------------------------------------------------------------------------
+struct Tri { double v0[3], e1[3], e2[3]; };
+
+inline void cross3(const double* a, const double* b, double* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+inline double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// Returns true when the ray's line crosses the triangle's plane; fills t and the
+// barycentrics (b1, b2); the hit counts only when both are >= 0, b1+b2 <= 1.
+inline bool ray_plane_bary(const Tri& tr, const double* o, const double* d, double* t, double* b1, double* b2) {
+  double p[3]; cross3(d, tr.e2, p);
+  const double det = dot3(tr.e1, p);
+  if (det == 0.0) return false;
+  const double inv = 1.0 / det;
+  const double s[3] = {o[0] - tr.v0[0], o[1] - tr.v0[1], o[2] - tr.v0[2]};
+  *b1 = dot3(s, p) * inv;
+  double q[3]; cross3(s, tr.e1, q);
+  *b2 = dot3(d, q) * inv;
+  *t = dot3(tr.e2, q) * inv;
+  return true;
+}
+
+// Signed distance (world units) from the plane point with barycentrics (b1,b2)
+// to the triangle's boundary: positive inside, negative outside.
+double edge_distance(const Tri& tr, double b1, double b2) {
+  const double b0 = 1.0 - b1 - b2;
+  double n[3]; cross3(tr.e1, tr.e2, n);
+  const double area2 = std::sqrt(dot3(n, n));
+  const double e0[3] = {tr.e2[0] - tr.e1[0], tr.e2[1] - tr.e1[1], tr.e2[2] - tr.e1[2]};
+  // height over edge opposite vertex i = area2 / |edge_i|
+  const double h0 = area2 / std::sqrt(dot3(e0, e0));
+  const double h1 = area2 / std::sqrt(dot3(tr.e2, tr.e2));
+  const double h2 = area2 / std::sqrt(dot3(tr.e1, tr.e1));
+  return std::min(b0 * h0, std::min(b1 * h1, b2 * h2));
+}
+
+// --------------------------------------------------------------------------
+// LBVH (Karras 2012, "Maximizing parallelism in the construction of BVHs,
+// octrees and k-d trees").  Bit-exact restatement of the device build:
+// FP32 centroid and quantisation, 30-bit Morton codes, stable sort by code,
+// integer split search.  Node numbering: internal 0..n-2 (root 0); a child
+// reference c >= 0 is internal, c < 0 is leaf ~c (index into the sorted order).
+// --------------------------------------------------------------------------
+uint32_t expand_bits10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+uint32_t quantise(float c, float lo, float scale) {
+  volatile float d = c - lo;
+  volatile float q = d * scale;
+  float qq = q;
+  if (!(qq > 0.f)) return 0u;
+  uint32_t u = uint32_t(qq);
+  return u > 1023u ? 1023u : u;
+}
+
+struct Bvh {
+  uint32_t n = 0;
+  std::vector<uint32_t> codes;     // sorted Morton codes
+  std::vector<uint32_t> order;     // sorted position -> original triangle
+  std::vector<int32_t> child;      // 2*(n-1)
+  std::vector<float> box;          // (2n-1)*6: internal 0..n-2 then leaves n-1..2n-2 (min xyz, max xyz)
+};
+
+int clz32(uint32_t v) { return v == 0 ? 32 : __builtin_clz(v); }
+
+int delta(const std::vector<uint32_t>& k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint32_t a = k[i], b = k[j];
+  if (a == b) return 32 + clz32(uint32_t(i) ^ uint32_t(j));
+  return clz32(a ^ b);
+}
+
+void build_lbvh(const float* pos, const uint32_t* idx, uint32_t ntris, Bvh* out) {
+  Bvh& b = *out;
+  b.n = ntris;
+  b.codes.assign(ntris, 0);
+  b.order.assign(ntris, 0);
+  b.child.assign(ntris > 1 ? 2 * (ntris - 1) : 0, 0);
+  b.box.assign(ntris ? (2 * ntris - 1) * 6 : 0, 0.f);
+  if (ntris == 0) return;
+  std::vector<float> tb(ntris * 6), cen(ntris * 3);
+  float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t t = 0; t < ntris; ++t) {
+    for (int a = 0; a < 3; ++a) {
+      const float p0 = pos[idx[3 * t] * 3 + a], p1 = pos[idx[3 * t + 1] * 3 + a], p2 = pos[idx[3 * t + 2] * 3 + a];
+      const float lo = std::min(p0, std::min(p1, p2)), hi = std::max(p0, std::max(p1, p2));
+      tb[t * 6 + a] = lo; tb[t * 6 + 3 + a] = hi;
+      volatile float s = lo + hi;
+      const float c = s * 0.5f;
+      cen[t * 3 + a] = c;
+      clo[a] = std::min(clo[a], c); chi[a] = std::max(chi[a], c);
+    }
+  }
+  float scale[3];
+  for (int a = 0; a < 3; ++a) {
+    volatile float e = chi[a] - clo[a];
+    scale[a] = (e > 0.f) ? 1024.0f / e : 0.0f;
+  }
+  std::vector<uint32_t> code(ntris);
+  for (uint32_t t = 0; t < ntris; ++t) {
+    const uint32_t qx = quantise(cen[t * 3], clo[0], scale[0]);
+    const uint32_t qy = quantise(cen[t * 3 + 1], clo[1], scale[1]);
+    const uint32_t qz = quantise(cen[t * 3 + 2], clo[2], scale[2]);
+    code[t] = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
+  }
+  std::vector<uint32_t> ord(ntris);
+  for (uint32_t t = 0; t < ntris; ++t) ord[t] = t;
+  std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t c) { return code[a] < code[c]; });
+  for (uint32_t i = 0; i < ntris; ++i) { b.order[i] = ord[i]; b.codes[i] = code[ord[i]]; }
+  const int n = int(ntris);
+  const uint32_t leaf0 = ntris - 1;
+  for (uint32_t i = 0; i < ntris; ++i)
+    for (int a = 0; a < 6; ++a) b.box[(leaf0 + i) * 6 + a] = tb[ord[i] * 6 + a];
+  if (n == 1) return;
+  std::vector<int32_t> parent(2 * n - 1, -1);
+  for (int i = 0; i < n - 1; ++i) {
+    const int d = (delta(b.codes, n, i, i + 1) - delta(b.codes, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(b.codes, n, i, i - d);
+    int lmax = 2;
+    while (delta(b.codes, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+      if (delta(b.codes, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = delta(b.codes, n, i, j);
+    int s = 0, t = l;
+    do {
+      t = (t + 1) >> 1;
+      if (delta(b.codes, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int g = i + s * d + std::min(d, 0);
+    const int lo = std::min(i, j), hi = std::max(i, j);
+    const int32_t left = (lo == g) ? ~int32_t(g) : int32_t(g);
+    const int32_t right = (hi == g + 1) ? ~int32_t(g + 1) : int32_t(g + 1);
+    b.child[2 * i] = left; b.child[2 * i + 1] = right;
+    parent[left >= 0 ? left : int(leaf0) + ~left] = i;
+    parent[right >= 0 ? right : int(leaf0) + ~right] = i;
+  }
+  // refit: post-order over internal nodes (min/max is order independent)
+  std::vector<int> stack;
+  std::vector<uint8_t> done(n - 1, 0);
+  stack.push_back(0);
+  while (!stack.empty()) {
+    const int i = stack.back();
+    bool ready = true;
+    for (int c = 0; c < 2; ++c) {
+      const int32_t ch = b.child[2 * i + c];
+      if (ch >= 0 && !done[ch]) { stack.push_back(ch); ready = false; }
+    }
+    if (!ready) continue;
+    stack.pop_back();
+    float* bx = &b.box[i * 6];
+    for (int a = 0; a < 3; ++a) { bx[a] = INFINITY; bx[3 + a] = -INFINITY; }
+    for (int c = 0; c < 2; ++c) {
+      const int32_t ch = b.child[2 * i + c];
+      const float* cb = &b.box[(ch >= 0 ? ch : int(leaf0) + ~ch) * 6];
+      for (int a = 0; a < 3; ++a) { bx[a] = std::min(bx[a], cb[a]); bx[3 + a] = std::max(bx[3 + a], cb[3 + a]); }
+    }
+    done[i] = 1;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Traversal in FP64 over the LBVH (exact FP32 boxes, padded by a relative
+// 1e-12 so the slab test never drops a triangle that FP64 would hit).
+// --------------------------------------------------------------------------
+struct Scene {
+  uint32_t ntris = 0;
+  std::vector<Tri> tris;      // by original index
+  std::vector<double> albedo; // ntris*3
+  Bvh bvh;
+};
+
+inline bool slab(const float* bx, const double* o, const double* inv, double tlo, double thi) {
+  double tn = tlo, tf = thi;
+  for (int a = 0; a < 3; ++a) {
+    const double pad = 1e-12 * (1.0 + std::fabs(double(bx[a])) + std::fabs(double(bx[3 + a])));
+    double t0 = (double(bx[a]) - pad - o[a]) * inv[a];
+    double t1 = (double(bx[3 + a]) + pad - o[a]) * inv[a];
+    if (std::isnan(t0) || std::isnan(t1)) continue;  // parallel ray on the slab plane: unbounded
+    if (t0 > t1) std::swap(t0, t1);
+    tn = std::max(tn, t0); tf = std::min(tf, t1);
+  }
+  return tn <= tf;
+}
+
+struct Hit { int32_t tri = -1; double t = 0, b1 = 0, b2 = 0; };
+
+// closest hit with t in (tmin, tmax); ties keep the lower triangle index
+Hit closest_hit(const Scene& sc, const double* o, const double* d, double tmin, double tmax) {
+  Hit h; double best = tmax;
+  const Bvh& b = sc.bvh;
+  if (b.n == 0) return h;
+  const double inv[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
+  auto test_leaf = [&](uint32_t slot) {
+    const int32_t tri = int32_t(b.order[slot]);
+    double t, b1, b2;
+    if (!ray_plane_bary(sc.tris[tri], o, d, &t, &b1, &b2)) return;
+    if (b1 < 0.0 || b2 < 0.0 || b1 + b2 > 1.0) return;
+    if (!(t > tmin)) return;
+    if (t < best || (t == best && h.tri >= 0 && tri < h.tri)) { best = t; h.tri = tri; h.t = t; h.b1 = b1; h.b2 = b2; }
+  };
+  if (b.n == 1) { test_leaf(0); return h; }
+  int32_t stack[128]; int sp = 0; stack[sp++] = 0;
+  const uint32_t leaf0 = b.n - 1;
+  while (sp) {
+    const int32_t nd = stack[--sp];
+    for (int c = 0; c < 2; ++c) {
+      const int32_t ch = b.child[2 * nd + c];
+      const float* bx = &b.box[(ch >= 0 ? ch : int(leaf0) + ~ch) * 6];
+      if (!slab(bx, o, inv, tmin, best)) continue;
+      if (ch < 0) test_leaf(uint32_t(~ch)); else stack[sp++] = ch;
+    }
+  }
+  return h;
+}
+
+// any hit with t in (tmin, tmax)
+bool any_hit(const Scene& sc, const double* o, const double* d, double tmin, double tmax) {
+  const Bvh& b = sc.bvh;
+  if (b.n == 0) return false;
+  const double inv[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
+  auto test_leaf = [&](uint32_t slot) {
+    double t, b1, b2;
+    if (!ray_plane_bary(sc.tris[b.order[slot]], o, d, &t, &b1, &b2)) return false;
+    return b1 >= 0.0 && b2 >= 0.0 && b1 + b2 <= 1.0 && t > tmin && t < tmax;
+  };
+  if (b.n == 1) return test_leaf(0);
+  int32_t stack[128]; int sp = 0; stack[sp++] = 0;
+  const uint32_t leaf0 = b.n - 1;
+  while (sp) {
+    const int32_t nd = stack[--sp];
+    for (int c = 0; c < 2; ++c) {
+      const int32_t ch = b.child[2 * nd + c];
+      const float* bx = &b.box[(ch >= 0 ? ch : int(leaf0) + ~ch) * 6];
+      if (!slab(bx, o, inv, tmin, tmax)) continue;
+      if (ch < 0) { if (test_leaf(uint32_t(~ch))) return true; } else stack[sp++] = ch;
+    }
+  }
+  return false;
+}
+
+// Largest signed edge distance over all triangles whose plane the ray crosses
+// inside (tmin, tmax): > 0 means occluded by that margin, < 0 visible by it.
+double shadow_margin(const Scene& sc, const double* o, const double* d, double tmin, double tmax) {
+  double best = -INFINITY;
+  for (uint32_t i = 0; i < sc.ntris; ++i) {
+    double t, b1, b2;
+    if (!ray_plane_bary(sc.tris[i], o, d, &t, &b1, &b2)) continue;
+    if (!(t > tmin && t < tmax)) continue;
+    best = std::max(best, edge_distance(sc.tris[i], b1, b2));
+  }
+  return best;
+}
+
+struct BakeCfg {
+  const float* probes; uint32_t np;
+  const float* dirs; uint32_t ns;
+  const double* basis; int K;        // ns x K, weight folded in
+  double sun[3]; double sun_scale;   // sun_scale = intensity / pi
+  double tmin, tmax, bias;
+  const float* sky; uint32_t sky_n;  // cubemap 6*n*n*3 or null
+  const int32_t* force_hit;          // optional per-ray decisions to replay (np*ns) or null
+  const uint8_t* force_vis;
+};
+
+void sky_radiance(const BakeCfg& c, const float* d, double* L) {
+  if (!c.sky) { L[0] = L[1] = L[2] = 0.0; return; }
+  uint32_t f, x, y;
+  cube_select(d[0], d[1], d[2], c.sky_n, &f, &x, &y);
+  const float* t = c.sky + ((size_t(f) * c.sky_n + y) * c.sky_n + x) * 3;
+  L[0] = t[0]; L[1] = t[1]; L[2] = t[2];
+}
+
+// vis codes: 0 occluded, 1 lit, 2 no shadow ray (miss, or n.l <= 0)
+void shade_ray(const Scene& sc, const BakeCfg& c, uint32_t p, uint32_t s, double* L, int32_t* hit_out,
+               uint8_t* vis_out, double* edge_out) {
+  const double o[3] = {c.probes[3 * p], c.probes[3 * p + 1], c.probes[3 * p + 2]};
+  const float* df = c.dirs + 3 * s;
+  const double d[3] = {df[0], df[1], df[2]};
+  Hit h;
+  const size_t r = size_t(p) * c.ns + s;
+  if (c.force_hit) {
+    h.tri = c.force_hit[r];
+    if (h.tri >= 0) ray_plane_bary(sc.tris[h.tri], o, d, &h.t, &h.b1, &h.b2);
+  } else {
+    h = closest_hit(sc, o, d, c.tmin, c.tmax);
+  }
+  if (hit_out) *hit_out = h.tri;
+  if (h.tri < 0) {
+    sky_radiance(c, df, L);
+    if (vis_out) *vis_out = 2;
+    if (edge_out) *edge_out = INFINITY;
+    return;
+  }
+  const Tri& tr = sc.tris[h.tri];
+  if (edge_out) *edge_out = edge_distance(tr, h.b1, h.b2);
+  double n[3]; cross3(tr.e1, tr.e2, n);
+  const double nl = std::sqrt(dot3(n, n));
+  n[0] /= nl; n[1] /= nl; n[2] /= nl;
+  if (dot3(n, d) > 0.0) { n[0] = -n[0]; n[1] = -n[1]; n[2] = -n[2]; }
+  const double ndl = dot3(n, c.sun);
+  if (!(ndl > 0.0)) {
+    L[0] = L[1] = L[2] = 0.0;
+    if (vis_out) *vis_out = 2;
+    return;
+  }
+  const double P[3] = {o[0] + h.t * d[0] + c.bias * n[0], o[1] + h.t * d[1] + c.bias * n[1], o[2] + h.t * d[2] + c.bias * n[2]};
+  bool lit;
+  if (c.force_vis && c.force_vis[r] != 2) lit = c.force_vis[r] == 1;
+  else lit = !any_hit(sc, P, c.sun, 0.0, c.tmax);
+  if (vis_out) *vis_out = lit ? 1 : 0;
+  const double k = lit ? c.sun_scale * ndl : 0.0;
+  for (int ch = 0; ch < 3; ++ch) L[ch] = sc.albedo[3 * h.tri + ch] * k;
+}
+
+Scene make_scene(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, const float* albedo) {
+  (void)nverts;
+  Scene sc;
+  sc.ntris = ntris;
+  sc.tris.resize(ntris);
+  sc.albedo.resize(size_t(ntris) * 3);
+  for (uint32_t t = 0; t < ntris; ++t) {
+    const float* a = pos + 3 * idx[3 * t];
+    const float* b = pos + 3 * idx[3 * t + 1];
+    const float* c = pos + 3 * idx[3 * t + 2];
+    for (int k = 0; k < 3; ++k) {
+      sc.tris[t].v0[k] = a[k];
+      sc.tris[t].e1[k] = double(b[k]) - double(a[k]);
+      sc.tris[t].e2[k] = double(c[k]) - double(a[k]);
+      sc.albedo[3 * t + k] = albedo ? albedo[3 * t + k] : 1.0;
+    }
+  }
+  build_lbvh(pos, idx, ntris, &sc.bvh);
+  return sc;
+}
+
+template <class F>
+void parallel_for(uint32_t n, int nthreads, F f) {
+  if (nthreads <= 1 || n < 2) { for (uint32_t i = 0; i < n; ++i) f(i); return; }
+  std::atomic<uint32_t> next{0};
+  std::vector<std::thread> th;
+  for (int w = 0; w < nthreads; ++w)
+    th.emplace_back([&] {
+      for (;;) {
+        const uint32_t i = next.fetch_add(1);
+        if (i >= n) break;
+        f(i);
+      }
+    });
+  for (auto& t : th) t.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_version(void) { return 1; }
+
+// ---- SH basis -------------------------------------------------------------
+void orc_sh_basis(int lmax, const double* dirs, uint32_t n, double* out) {
+  const int K = sh_count(lmax);
+  for (uint32_t i = 0; i < n; ++i) sh_basis(lmax, dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], out + size_t(i) * K);
+}
+
+void orc_x2phi_y2theta(int x, int w, int y, int h, double* phi, double* theta) {
+  *phi = x2phi(x, w); *theta = y2theta(y, h);
+}
+
+void orc_to_vector(double phi, double theta, double* d) { to_vector(phi, theta, d); }
+
+// ---- direction sets ---------------------------------------------------------
+// Spherical Fibonacci point set (Swinbank & Purser 2006; Keinert et al. 2015):
+// z_i = 1 - (2i+1)/N, phi_i = 2*pi*frac(i*(sqrt(5)-1)/2).  FP64, rounded once.
+void orc_dirs_fibonacci(uint32_t n, float* dirs32, double* weight) {
+  const double g = 0.6180339887498949;
+  const double two_pi = 6.283185307179586;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double z = 1.0 - (2.0 * i + 1.0) / double(n);
+    const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
+    double fr = double(i) * g; fr -= std::floor(fr);
+    const double phi = two_pi * fr;
+    dirs32[3 * i] = float(r * std::cos(phi));
+    dirs32[3 * i + 1] = float(r * std::sin(phi));
+    dirs32[3 * i + 2] = float(z);
+  }
+  if (weight) *weight = 4.0 * 3.141592653589793 / double(n);
+}
+
+// Reference bake sample set: one ray per equirect pixel, traced along
+// toVector(..).xzy (env_map.rgen:21) but projected with the un-swizzled
+// toVector (sh.comp:30) and weight (2pi/W)(pi/H)sin(theta) (sh.comp:32-33).
+void orc_dirs_equirect(uint32_t w, uint32_t h, float* trace32, double* basis_dirs, double* weights) {
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const size_t s = size_t(y) * w + x;
+      const double phi = x2phi(int(x), int(w)), theta = y2theta(int(y), int(h));
+      double d[3]; to_vector(phi, theta, d);
+      trace32[3 * s] = float(d[0]); trace32[3 * s + 1] = float(d[2]); trace32[3 * s + 2] = float(d[1]);
+      basis_dirs[3 * s] = d[0]; basis_dirs[3 * s + 1] = d[1]; basis_dirs[3 * s + 2] = d[2];
+      weights[s] = (2.0 * kPiRef / w) * (kPiRef / h) * std::sin(theta);
+    }
+}
+
+// ---- cubemap helpers ------------------------------------------------------
+void orc_cube_solid_angle(uint32_t n, double* out) {
+  for (uint32_t y = 0; y < n; ++y)
+    for (uint32_t x = 0; x < n; ++x) out[size_t(y) * n + x] = cube_texel_solid_angle(n, x, y);
+}
+
+void orc_cube_texel_dirs(uint32_t n, double* out) {
+  for (int f = 0; f < 6; ++f)
+    for (uint32_t y = 0; y < n; ++y)
+      for (uint32_t x = 0; x < n; ++x) {
+        const double u = 2.0 * (x + 0.5) / n - 1.0, v = 2.0 * (y + 0.5) / n - 1.0;
+        cube_face_dir(f, u, v, out + ((size_t(f) * n + y) * n + x) * 3);
+      }
+}
+
+void orc_cube_select(const float* dirs, uint32_t count, uint32_t n, uint32_t* out_index) {
+  for (uint32_t i = 0; i < count; ++i) {
+    uint32_t f, x, y;
+    cube_select(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], n, &f, &x, &y);
+    out_index[i] = (f * n + y) * n + x;
+  }
+}
+
+// ---- skybox projection ------------------------------------------------------
+// layout 0: cubemap 6 x n x n (w == h == n), basis at the world direction,
+//           weight = exact texel solid angle.
+// layout 1: panorama as skybox_sh.comp:27-41 (phi - PI/2, basis at dir.xzy).
+// layout 2: panorama as sh.comp:27-41 (env map form, basis at dir).
+// fmt 0: RGB fp32 texels; fmt 1: RGBA8 UNORM (value/255).  flags bit0 swaps
+// R and B like the reference's RGBA bytes in a B8G8R8A8 image
+// (skybox_manager.cpp:18, application.cpp:690).
+void orc_skybox_sh(const void* texels, int fmt, int layout, uint32_t w, uint32_t h, int lmax, uint32_t flags,
+                   double* out) {
+  const int K = sh_count(lmax);
+  std::vector<double> acc(size_t(K) * 3, 0.0);
+  double Y[25];
+  auto fetch = [&](size_t t, double* c) {
+    if (fmt == 0) {
+      const float* p = static_cast<const float*>(texels) + 3 * t;
+      c[0] = p[0]; c[1] = p[1]; c[2] = p[2];
+    } else {
+      const uint8_t* p = static_cast<const uint8_t*>(texels) + 4 * t;
+      c[0] = p[0] / 255.0; c[1] = p[1] / 255.0; c[2] = p[2] / 255.0;
+    }
+    if (flags & 1u) std::swap(c[0], c[2]);
+  };
+  if (layout == 0) {
+    const uint32_t n = w;
+    std::vector<double> sa(size_t(n) * n);
+    orc_cube_solid_angle(n, sa.data());
+    for (int f = 0; f < 6; ++f)
+      for (uint32_t y = 0; y < n; ++y)
+        for (uint32_t x = 0; x < n; ++x) {
+          const double u = 2.0 * (x + 0.5) / n - 1.0, v = 2.0 * (y + 0.5) / n - 1.0;
+          double d[3]; cube_face_dir(f, u, v, d);
+          sh_basis(lmax, d[0], d[1], d[2], Y);
+          double c[3]; fetch((size_t(f) * n + y) * n + x, c);
+          const double wgt = sa[size_t(y) * n + x];
+          for (int k = 0; k < K; ++k)
+            for (int ch = 0; ch < 3; ++ch) acc[3 * k + ch] += Y[k] * c[ch] * wgt;
+        }
+  } else {
+    const double area = (2.0 * kPiRef / w) * (kPiRef / h);
+    for (uint32_t y = 0; y < h; ++y)
+      for (uint32_t x = 0; x < w; ++x) {
+        double phi = x2phi(int(x), int(w));
+        if (layout == 1) phi -= kPiRef / 2.0;
+        const double theta = y2theta(int(y), int(h));
+        double d[3]; to_vector(phi, theta, d);
+        if (layout == 1) sh_basis(lmax, d[0], d[2], d[1], Y); else sh_basis(lmax, d[0], d[1], d[2], Y);
+        double c[3]; fetch(size_t(y) * w + x, c);
+        const double wgt = area * std::sin(theta);
+        for (int k = 0; k < K; ++k)
+          for (int ch = 0; ch < 3; ++ch) acc[3 * k + ch] += Y[k] * c[ch] * wgt;
+      }
+  }
+  for (int i = 0; i < 3 * K; ++i) out[i] = acc[i];
+}
+
+// ---- radiance tile projection (sh.comp's sum for a shared sample set) -------
+// radiance: rows x S (row = probe*3 + channel); basis: S x K with the sample
+// weight folded in.  out: probes x K x 3.
+void orc_project(const float* radiance, uint32_t rows, uint32_t S, const double* basis, int K, double* out,
+                 int nthreads) {
+  const uint32_t np = rows / 3;
+  parallel_for(np, nthreads, [&](uint32_t p) {
+    for (int ch = 0; ch < 3; ++ch) {
+      const float* r = radiance + (size_t(p) * 3 + ch) * S;
+      for (int k = 0; k < K; ++k) {
+        double a = 0.0;
+        for (uint32_t s = 0; s < S; ++s) a += double(r[s]) * basis[size_t(s) * K + k];
+        out[(size_t(p) * K + k) * 3 + ch] = a;
+      }
+    }
+  });
+}
+
+// ---- reconstruction (sh_sum.comp:35-52) -----------------------------------
+void orc_sh_eval_envmap(const double* coeffs, int lmax, uint32_t w, uint32_t h, double scale, double* out) {
+  const int K = sh_count(lmax);
+  double Y[25];
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      double d[3]; to_vector(x2phi(int(x), int(w)), y2theta(int(y), int(h)), d);
+      sh_basis(lmax, d[0], d[1], d[2], Y);
+      double* o = out + (size_t(y) * w + x) * 3;
+      o[0] = o[1] = o[2] = 0.0;
+      for (int k = 0; k < K; ++k)
+        for (int ch = 0; ch < 3; ++ch) o[ch] += coeffs[3 * k + ch] * Y[k];
+      for (int ch = 0; ch < 3; ++ch) o[ch] *= scale;
+    }
+}
+
+// ---- probe grid (light_baker.cpp:138-159), FP32 like glm::vec3 -------------
+uint32_t orc_probe_grid_ref_order(const float* bounds, const uint32_t* counts, float* out, float* step) {
+  float st[3];
+  for (int a = 0; a < 3; ++a) {
+    volatile float e = bounds[3 + a] - bounds[a];
+    volatile float c = float(counts[a]) - 1.f;
+    st[a] = e / c;
+    if (step) step[a] = st[a];
+  }
+  std::vector<float> pos = {bounds[0], bounds[1], bounds[2]};
+  for (int dim = 0; dim < 3; ++dim) {
+    const size_t m = pos.size() / 3;
+    for (size_t q = 0; q < m; ++q) {
+      float p[3] = {pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]};
+      for (int i = 0; i < int(counts[dim]) - 1; ++i) {
+        volatile float v = p[dim] + st[dim];
+        p[dim] = v;
+        pos.push_back(p[0]); pos.push_back(p[1]); pos.push_back(p[2]);
+      }
+    }
+  }
+  if (out) std::memcpy(out, pos.data(), pos.size() * sizeof(float));
+  return uint32_t(pos.size() / 3);
+}
+
+// ---- LBVH -----------------------------------------------------------------
+int orc_lbvh_build(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, uint32_t* codes,
+                   uint32_t* order, int32_t* child, float* box) {
+  (void)nverts;
+  Bvh b;
+  build_lbvh(pos, idx, ntris, &b);
+  if (codes) std::memcpy(codes, b.codes.data(), b.codes.size() * 4);
+  if (order) std::memcpy(order, b.order.data(), b.order.size() * 4);
+  if (child) std::memcpy(child, b.child.data(), b.child.size() * 4);
+  if (box) std::memcpy(box, b.box.data(), b.box.size() * 4);
+  return 0;
+}
+
+// ---- bake -------------------------------------------------------------------
+// Scene handle so several queries reuse one BVH.
+void* orc_scene_create(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, const float* albedo) {
+  return new Scene(make_scene(pos, nverts, idx, ntris, albedo));
+}
+void orc_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
+
+// Per probe p and sample s: closest hit in (tmin,tmax) along dirs[s]; on a hit
+// the Lambert term albedo * sun_intensity/pi * max(0, n.l) if the shadow ray
+// from hit + bias*n toward the sun is unoccluded; on a miss the cubemap sky
+// (nearest texel) or black.  out_sh: np x K x 3 (FP64).  Optional per-ray
+// outputs (np*ns): hit triangle, shadow code, edge distance, radiance (x3).
+void orc_bake(const void* scene, const float* probes, uint32_t np, const float* dirs, uint32_t ns, const double* basis,
+              int K, const float* sun_dir, float sun_intensity, float tmin, float tmax, float bias, const float* sky,
+              uint32_t sky_n, const int32_t* force_hit, const uint8_t* force_vis, int nthreads, double* out_sh,
+              int32_t* hit_ids, uint8_t* vis, double* edge, float* radiance) {
+  const Scene& sc = *static_cast<const Scene*>(scene);
+  BakeCfg c{};
+  c.probes = probes; c.np = np; c.dirs = dirs; c.ns = ns; c.basis = basis; c.K = K;
+  double sl = std::sqrt(double(sun_dir[0]) * sun_dir[0] + double(sun_dir[1]) * sun_dir[1] + double(sun_dir[2]) * sun_dir[2]);
+  for (int a = 0; a < 3; ++a) c.sun[a] = sun_dir[a] / sl;
+  c.sun_scale = double(sun_intensity) / 3.141592653589793;
+  c.tmin = tmin; c.tmax = tmax; c.bias = bias; c.sky = sky; c.sky_n = sky_n;
+  c.force_hit = force_hit; c.force_vis = force_vis;
+  parallel_for(np, nthreads, [&](uint32_t p) {
+    std::vector<double> acc(size_t(K) * 3, 0.0);
+    for (uint32_t s = 0; s < ns; ++s) {
+      const size_t r = size_t(p) * ns + s;
+      double L[3];
+      shade_ray(sc, c, p, s, L, hit_ids ? hit_ids + r : nullptr, vis ? vis + r : nullptr, edge ? edge + r : nullptr);
+      if (radiance) for (int ch = 0; ch < 3; ++ch) radiance[r * 3 + ch] = float(L[ch]);
+      const double* B = basis + size_t(s) * K;
+      for (int k = 0; k < K; ++k)
+        for (int ch = 0; ch < 3; ++ch) acc[3 * k + ch] += B[k] * L[ch];
+    }
+    if (out_sh) std::memcpy(out_sh + size_t(p) * K * 3, acc.data(), acc.size() * sizeof(double));
+  });
+}
+
+// FP64 facts about one ray and one triangle, for classifying decision
+// mismatches: t, barycentrics, signed edge distance (world units).
+int orc_ray_tri(const void* scene, const double* o, const double* d, int32_t tri, double* t, double* b1, double* b2,
+                double* edge) {
+  const Scene& sc = *static_cast<const Scene*>(scene);
+  if (tri < 0 || uint32_t(tri) >= sc.ntris) return 0;
+  if (!ray_plane_bary(sc.tris[tri], o, d, t, b1, b2)) return 0;
+  *edge = edge_distance(sc.tris[tri], *b1, *b2);
+  return 1;
+}
+
+double orc_shadow_margin(const void* scene, const double* o, const double* d, double tmin, double tmax) {
+  return shadow_margin(*static_cast<const Scene*>(scene), o, d, tmin, tmax);
+}
+
+void orc_closest_hit(const void* scene, const double* o, const double* d, double tmin, double tmax, int32_t* tri,
+                     double* t) {
+  const Hit h = closest_hit(*static_cast<const Scene*>(scene), o, d, tmin, tmax);
+  *tri = h.tri; *t = h.t;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+"""Probe bake (trace + shade + projection) vs the FP64 oracle.
+
+Protocol (tests/parity.py): per-ray hit triangles and shadow decisions must
+match the oracle except on rays FP32 cannot decide (within 1e-6 of an edge);
+their count is reported.  SH must be within 1e-4 relative (L2 per probe) of
+the oracle replayed with the device's decisions, and the direct comparison
+may exceed it only on probes that own an edge ray.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import parity
+import vlb
+
+pytestmark = pytest.mark.gpu
+
+
+def c1_inputs(seed=1, nboxes=64, counts=(16, 16, 16), S=256, n_sky=128):
+    pos, idx, alb = vlb.synth_box_scene(seed, nboxes)
+    sky = vlb.synth_cubemap(seed, n_sky)
+    sun = vlb.synth_sun(seed)
+    bounds = np.concatenate([np.minimum(pos.min(0), 0), np.maximum(pos.max(0), 0)]).astype(np.float32)
+    probes, _ = vlb.probe_grid_ref_order(bounds, counts)
+    return pos, idx, alb, sky, sun, probes, S
+
+
+def run_parity(ctx, pos, idx, alb, sky, sun, probes, S, lmax=2, precision=vlb.PREC_FP32, n_sky=128):
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(S)
+    skyh = ctx.sky(sky, n_sky) if sky is not None else None
+    p = vlb.bake_params(ds, lmax=lmax, precision=precision, sun=sun, sky=skyh)
+    sh, hit, vis, rad = ctx.bake(scene, probes, p, debug=True)
+    d32, w = O.dirs_fibonacci(S)
+    B = O.basis_matrix(d32.astype(np.float64), w, lmax)
+    orc = O.Scene(pos, idx, alb)
+    o_sh, o_hit, o_vis, o_edge, o_rad = orc.bake(probes, d32, B, sun, sky=sky, sky_n=n_sky if sky is not None else 0,
+                                                 per_ray=True)
+    cls = parity.classify(orc, probes, d32, sun, hit, vis, o_hit, o_vis, o_edge)
+    rep = orc.bake(probes, d32, B, sun, sky=sky, sky_n=n_sky if sky is not None else 0, force_hit=hit, force_vis=vis)
+    mism = ((hit != o_hit) | (vis != o_vis)).any(axis=1)
+    return sh, hit, vis, rad, o_sh, mism, cls, rep
+
+
+def test_config1_full_grid_parity(ctx):
+    pos, idx, alb, sky, sun, probes, S = c1_inputs()
+    sh, hit, vis, rad, o_sh, mism, cls, rep = run_parity(ctx, pos, idx, alb, sky, sun, probes, S)
+    print("C1 parity:", {k: v for k, v in cls.items() if k != "unexplained"})
+    assert not cls["unexplained"], cls["unexplained"][:10]
+    assert cls["hit_mismatch"] + cls["shadow_mismatch"] <= 1e-3 * cls["rays"]
+    err_rep = parity.per_probe_rel(sh, rep)
+    assert err_rep.max() < parity.SH_TOL, err_rep.max()
+    err = parity.per_probe_rel(sh, o_sh)
+    bad = err >= parity.SH_TOL
+    print(f"direct vs oracle: max {err.max():.3e}; probes over 1e-4: {int(bad.sum())}; probes with edge rays: "
+          f"{int(mism.sum())}")
+    assert not np.any(bad & ~mism)
+
+
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_paths_agree(ctx, lmax):
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=3, counts=(8, 8, 8))
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(S)
+    skyh = ctx.sky(sky, 128)
+    plain = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FP32, sun, sky=skyh))
+    fused = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FUSED, sun, sky=skyh))
+    mixed = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_MIXED, sun, sky=skyh))
+    assert parity.per_probe_rel(fused, plain).max() < 1e-5
+    e = parity.per_probe_rel(mixed, plain)
+    print(f"mixed vs fp32: max {e.max():.3e} mean {e.mean():.3e}")
+    assert e.max() < 2e-3  # BF16 radiance (8-bit mantissa) over 256 samples
+
+
+def test_lmax3_reference_layout_and_radiance(ctx):
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=5, counts=(4, 4, 4), S=64)
+    sh, hit, vis, rad, o_sh, o_hit, cls, rep = run_parity(ctx, pos, idx, alb, sky, sun, probes, S, lmax=3)
+    assert sh.shape == (64, 16, 3) and sh.dtype == np.float32  # 192 bytes per probe
+    assert parity.per_probe_rel(sh, rep).max() < parity.SH_TOL
+
+
+def test_empty_scene_sees_sky(ctx):
+    sky = vlb.synth_cubemap(4, 32)
+    pos = np.zeros((3, 3), np.float32)
+    idx = np.zeros((0, 3), np.uint32)
+    probes = np.float32([[0, 0, 0], [0.3, 0.2, 0.1]])
+    scene = ctx.scene(pos, idx)
+    ds = ctx.fibonacci(256)
+    sh = ctx.bake(scene, probes, vlb.bake_params(ds, 2, sun=(0, 1, 0), sky=ctx.sky(sky, 32)))
+    d32, w = O.dirs_fibonacci(256)
+    ref = O.Scene(pos, idx, np.zeros((0, 3))).bake(probes, d32, O.basis_matrix(d32.astype(np.float64), w, 2),
+                                                  [0, 1, 0], sky=sky, sky_n=32)
+    assert parity.per_probe_rel(sh, ref).max() < 1e-5
+    assert np.allclose(sh[0], sh[1])
+
+
+def test_single_triangle_and_black_sky(ctx):
+    pos = np.float32([[-1, 0, -1], [1, 0, -1], [0, 0, 1]])
+    idx = np.uint32([[0, 1, 2]])
+    alb = np.float32([[0.5, 0.25, 1.0]])
+    probes = np.float32([[0, 0.5, 0], [0.1, -0.2, 0.0], [5, 5, 5]])
+    sh, hit, vis, rad, o_sh, o_hit, cls, rep = run_parity(ctx, pos, idx, alb, None, [0.2, 1, 0.1], probes, 256)
+    assert not cls["unexplained"]
+    assert parity.per_probe_rel(sh, rep).max() < parity.SH_TOL
+
+
+def test_device_resident_probes_and_output(ctx):
+    torch = pytest.importorskip("torch")
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=9, counts=(4, 4, 4))
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(S)
+    p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun, sky=ctx.sky(sky, 128))
+    host = ctx.bake(scene, probes, p)
+    out = torch.empty((probes.shape[0], 9, 3), dtype=torch.float32, device="cuda")
+    ctx.bake(scene, torch.from_numpy(probes).cuda(), p, out=out)
+    ctx.synchronize()
+    assert np.array_equal(out.cpu().numpy(), host)
+
+
+def test_invalid_params(ctx):
+    pos, idx, alb = vlb.synth_box_scene(1, 2)
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(64)
+    p = vlb.bake_params(ds, 4)
+    with pytest.raises(vlb.VlbError) as e:
+        ctx.bake(scene, np.zeros((1, 3), np.float32), p)
+    assert e.value.status == vlb.ERR_INVALID
+    p = vlb.bake_params(ds, 2, sun=(0, 0, 0))
+    with pytest.raises(vlb.VlbError):
+        ctx.bake(scene, np.zeros((1, 3), np.float32), p)

@@ -1,0 +1,107 @@
+"""Host-side logic of libvlb.so that needs no GPU: ABI exports, the reference
+probe order, the seeded workload generators."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+import vlb
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _header_functions():
+    text = (ROOT / "include" / "vlb.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(vlb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_header_function():
+    names = _header_functions()
+    assert len(names) > 30
+    missing = [n for n in names if not hasattr(vlb.lib, n)]
+    assert not missing, missing
+
+
+def test_version_and_status_strings():
+    assert vlb.lib.vlb_version() == 1
+    assert vlb.lib.vlb_status_string(vlb.ERR_INVALID) == b"invalid argument"
+
+
+def test_probe_grid_matches_oracle_bit_exact():
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        lo = rng.uniform(-5, 5, 3).astype(np.float32)
+        hi = (lo + rng.uniform(0.1, 9, 3)).astype(np.float32)
+        counts = rng.integers(2, 9, 3)
+        a, sa = vlb.probe_grid_ref_order(np.concatenate([lo, hi]), counts)
+        b, sb = O.probe_grid_ref_order(np.concatenate([lo, hi]), counts)
+        assert np.array_equal(a, b) and np.array_equal(sa, sb)
+
+
+def test_probe_grid_reference_breadth_first_order(golden):
+    pos, step = vlb.probe_grid_ref_order([0, 0, 0, 1, 1, 1], [3, 3, 3])
+    assert np.array_equal(pos, golden["grid"])
+
+
+def test_probe_grid_single_count_axis():
+    # counts of 1 divide by zero in the reference too; the positions stay at b0
+    a, sa = vlb.probe_grid_ref_order([0, 0, 0, 1, 2, 3], [1, 2, 1])
+    b, sb = O.probe_grid_ref_order([0, 0, 0, 1, 2, 3], [1, 2, 1])
+    assert np.array_equal(a, b)
+    assert np.array_equal(sa, sb, equal_nan=True)
+
+
+def test_probe_grid_rejects_zero_counts():
+    with pytest.raises(vlb.VlbError):
+        vlb.probe_grid_ref_order([0, 0, 0, 1, 1, 1], [0, 2, 2])
+
+
+def test_box_scene_generator_matches_config_ranges():
+    pos, idx, alb = vlb.synth_box_scene(123, 64)
+    assert idx.shape == (778, 3) and pos.shape == (520, 3)
+    assert pos.min() >= 0.0 and pos.max() <= 1.0
+    boxes = pos[8:].reshape(64, 8, 3)
+    lo, hi = boxes.min(1), boxes.max(1)
+    c, e = (lo + hi) / 2, hi - lo
+    assert np.all((c >= 0.1 - 1e-6) & (c <= 0.9 + 1e-6))
+    assert np.all((e >= 0.05 - 1e-6) & (e <= 0.2 + 1e-6))
+    a = alb[10:]
+    assert np.all((a >= 0.2) & (a <= 0.8))
+    assert np.all(alb[:10] == 0.5)
+    # 12 triangles per box share one albedo
+    assert np.all(a.reshape(64, 12, 3) == a.reshape(64, 12, 3)[:, :1])
+    p2, i2, a2 = vlb.synth_box_scene(123, 64)
+    assert np.array_equal(pos, p2) and np.array_equal(idx, i2) and np.array_equal(alb, a2)
+    p3, _, _ = vlb.synth_box_scene(124, 64)
+    assert not np.array_equal(pos, p3)
+
+
+def test_box_scene_scales_to_config2():
+    pos, idx, alb = vlb.synth_box_scene(7, 4096)
+    assert idx.shape[0] == 49162
+
+
+def test_cubemap_generator():
+    cm = vlb.synth_cubemap(9, 32)
+    assert cm.shape == (6, 32, 32, 3)
+    assert cm.min() >= 0.3 - 1e-6
+    assert cm.max() > 1.0  # the lobes
+    assert np.array_equal(cm, vlb.synth_cubemap(9, 32))
+
+
+def test_sun_generator_upper_hemisphere():
+    for s in range(50):
+        d = vlb.synth_sun(s)
+        assert d[1] > 0 and abs(np.linalg.norm(d.astype(np.float64)) - 1) < 1e-6
+
+
+def test_context_creation_fails_cleanly_without_gpu():
+    from conftest import HAS_GPU
+
+    if HAS_GPU:
+        pytest.skip("a GPU is present")
+    with pytest.raises(vlb.VlbError):
+        vlb.Context(0)

@@ -1,0 +1,138 @@
+// k_project.cu -- projection of a radiance tile onto the SH basis
+// (shaders/sh.comp:23-42 for a sample set shared by all probes) and the
+// reconstruction of shaders/sh_sum.comp:35-52.
+//
+// Tile layout: row r = probe*3 + channel, S samples contiguous per row.  The
+// basis table is S x 16 FP32 with the sample weight folded in.  One thread
+// owns one row; a CTA stages a [128 rows x 64 samples] block of the tile in
+// shared memory with coalesced row-segment loads (rows padded to 65 words so
+// the per-thread column walk is bank-conflict free), and the matching 64 x 16
+// basis block is read as warp-wide broadcasts.  Each row's sum runs in FP32
+// over its samples in a fixed order, so the result does not depend on the
+// launch shape or on other probes in the tile.
+#include <cuda_bf16.h>
+
+#include "vlb_device.cuh"
+#include "vlb_internal.h"
+
+namespace vlbk {
+
+constexpr int kProjRows = 128;
+constexpr int kProjCols = 64;
+
+template <typename T>
+__device__ __forceinline__ float to_f32(T v);
+template <>
+__device__ __forceinline__ float to_f32<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float to_f32<uint16_t>(uint16_t v) { return __uint_as_float(uint32_t(v) << 16); }
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad, uint32_t rows, uint32_t S,
+                                                       const float* __restrict__ basis16, float* __restrict__ out) {
+  __shared__ float tile[kProjRows][kProjCols + 1];
+  __shared__ __align__(16) float bas[kProjCols][16];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t row0 = blockIdx.x * kProjRows;
+  const uint32_t row = row0 + tid;
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+
+  for (uint32_t s0 = 0; s0 < S; s0 += kProjCols) {
+    const uint32_t ns = min(uint32_t(kProjCols), S - s0);
+    // coalesced staging: each warp loads 32 rows, two 32-sample halves per row
+    for (uint32_t rr = warp; rr < kProjRows; rr += kProjRows / 32) {
+      const uint32_t gr = row0 + rr;
+#pragma unroll
+      for (int h = 0; h < kProjCols / 32; ++h) {
+        const uint32_t c = h * 32 + lane;
+        float v = 0.f;
+        if (gr < rows && c < ns) v = to_f32<T>(rad[size_t(gr) * S + s0 + c]);
+        tile[rr][c] = v;
+      }
+    }
+    for (uint32_t i = tid; i < kProjCols * 16; i += kProjRows) {
+      const uint32_t j = i / 16, k = i % 16;
+      bas[j][k] = (j < ns) ? basis16[size_t(s0 + j) * 16 + k] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (uint32_t j = 0; j < kProjCols; ++j) {
+      const float r = tile[tid][j];
+      const float4* b4 = reinterpret_cast<const float4*>(bas[j]);
+#pragma unroll
+      for (int q = 0; q < (K + 3) / 4; ++q) {
+        const float4 b = b4[q];
+        if (4 * q + 0 < K) acc[4 * q + 0] = fmaf(r, b.x, acc[4 * q + 0]);
+        if (4 * q + 1 < K) acc[4 * q + 1] = fmaf(r, b.y, acc[4 * q + 1]);
+        if (4 * q + 2 < K) acc[4 * q + 2] = fmaf(r, b.z, acc[4 * q + 2]);
+        if (4 * q + 3 < K) acc[4 * q + 3] = fmaf(r, b.w, acc[4 * q + 3]);
+      }
+    }
+    __syncthreads();
+  }
+  if (row < rows) {
+    const uint32_t p = row / 3, c = row - 3 * p;
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[(size_t(p) * K + k) * 3 + c] = acc[k];
+  }
+}
+
+template <typename T>
+static void launch_project(const T* rad, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K, float* out,
+                           cudaStream_t s) {
+  const uint32_t rows = nprobes * 3;
+  const uint32_t grid = (rows + kProjRows - 1) / kProjRows;
+  if (grid == 0) return;
+  if (K == 9) k_project<T, 9><<<grid, kProjRows, 0, s>>>(rad, rows, S, basis16, out);
+  else k_project<T, 16><<<grid, kProjRows, 0, s>>>(rad, rows, S, basis16, out);
+}
+
+void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
+                        float* out, cudaStream_t s) {
+  launch_project<float>(radiance, nprobes, S, basis16, K, out, s);
+}
+
+void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
+                              uint32_t K, float* out, cudaStream_t s) {
+  launch_project<uint16_t>(radiance, nprobes, S, basis16, K, out, s);
+}
+
+// sh_sum.comp:35-52 -- one thread per pixel, direction from the per-column
+// (cos phi, sin phi) and per-row (sin theta, cos theta) tables.
+template <int K>
+__global__ void k_sh_eval_envmap(const float* __restrict__ coeffs, uint32_t w, uint32_t h, float scale,
+                                 const float2* __restrict__ col, const float4* __restrict__ rowt, float* __restrict__ out) {
+  __shared__ float c[3 * K];
+  if (threadIdx.x < 3 * K) c[threadIdx.x] = coeffs[threadIdx.x];
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w * h) return;
+  const uint32_t y = i / w, x = i - y * w;
+  const float2 cs = col[x];
+  const float4 rw = rowt[y];
+  float Y[K];
+  sh_basis<(K == 9 ? 2 : 3)>(rw.x * cs.x, rw.x * cs.y, rw.y, Y);
+  float r = 0.f, g = 0.f, b = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    r = fmaf(c[3 * k], Y[k], r);
+    g = fmaf(c[3 * k + 1], Y[k], g);
+    b = fmaf(c[3 * k + 2], Y[k], b);
+  }
+  out[3 * size_t(i)] = scale * r;
+  out[3 * size_t(i) + 1] = scale * g;
+  out[3 * size_t(i) + 2] = scale * b;
+}
+
+void launch_sh_eval_envmap(const float* coeffs, uint32_t K, uint32_t w, uint32_t h, float scale, const float2* col_tab,
+                           const float4* row_tab, float* out, cudaStream_t s) {
+  const uint32_t n = w * h;
+  if (n == 0) return;
+  const uint32_t grid = (n + 255) / 256;
+  if (K == 9) k_sh_eval_envmap<9><<<grid, 256, 0, s>>>(coeffs, w, h, scale, col_tab, row_tab, out);
+  else k_sh_eval_envmap<16><<<grid, 256, 0, s>>>(coeffs, w, h, scale, col_tab, row_tab, out);
+}
+
+}  // namespace vlbk

@@ -1,0 +1,1024 @@
+// vlb_api.cpp -- host C++ behind the C ABI of include/vlb.h.
+//
+// Replaces the reference's Vulkan host layer for the bake path
+// (Application / SceneManager / SkyboxManager / LightBaker /
+// EnvMapGenerator).  Everything here is orchestration: argument checks,
+// staging of host arrays, scratch memory, kernel launches on the context's
+// stream, error reporting.  All arithmetic on the bake path runs in the CUDA
+// kernels of k_*.cu; there is no CPU fallback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "vlb_internal.h"
+
+namespace {
+
+constexpr double kPiRef = 3.1415926538;  // shaders/sh_common.h:1
+constexpr double kPi = 3.141592653589793;
+
+vlb_status fail(vlb_ctx* ctx, vlb_status s, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return s;
+}
+
+vlb_status cuda_fail(vlb_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? VLB_ERR_OOM : VLB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define VLB_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Grow-only named scratch buffer owned by the context.
+vlb_status scratch(vlb_ctx* ctx, const char* name, size_t bytes, void** out) {
+  auto& b = ctx->scratch[name];
+  if (b.bytes < bytes) {
+    if (b.p) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(b.p);
+      b.p = nullptr;
+      b.bytes = 0;
+    }
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, VLB_ERR_OOM, "scratch '%s': cudaMalloc(%zu) failed", name, want);
+    }
+    b.bytes = want;
+  }
+  *out = b.p;
+  return VLB_OK;
+}
+
+// A caller array on the device: used in place when it already is device
+// memory, otherwise copied into named scratch.
+vlb_status stage_in(vlb_ctx* ctx, const void* src, size_t bytes, const char* name, const void** dev) {
+  if (bytes == 0) { *dev = nullptr; return VLB_OK; }
+  if (is_device_ptr(src)) { *dev = src; return VLB_OK; }
+  void* p;
+  vlb_status st = scratch(ctx, name, bytes, &p);
+  if (st) return st;
+  VLB_CUDA(ctx, cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->host_inputs_pending = true;  // the call must not return before this copy has read src
+  *dev = p;
+  return VLB_OK;
+}
+
+struct OutBuf {
+  void* user = nullptr;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  bool host = false;
+};
+
+vlb_status stage_out(vlb_ctx* ctx, void* user, size_t bytes, const char* name, OutBuf* o) {
+  o->user = user; o->bytes = bytes;
+  if (!user || bytes == 0) { o->dev = nullptr; return VLB_OK; }
+  if (is_device_ptr(user)) { o->dev = user; o->host = false; return VLB_OK; }
+  o->host = true;
+  return scratch(ctx, name, bytes, &o->dev);
+}
+
+vlb_status copy_out(vlb_ctx* ctx, const OutBuf& o) {
+  if (o.host && o.user && o.bytes)
+    VLB_CUDA(ctx, cudaMemcpyAsync(o.user, o.dev, o.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return VLB_OK;
+}
+
+// Reads and clears the device error counters; needs a synchronised stream.
+vlb_status check_device_errors(vlb_ctx* ctx) {
+  int h[vlbk::kErrSlots];
+  VLB_CUDA(ctx, cudaMemcpy(h, ctx->d_err, sizeof h, cudaMemcpyDeviceToHost));
+  bool any = false;
+  for (int i = 0; i < vlbk::kErrSlots; ++i) any |= h[i] != 0;
+  if (!any) return VLB_OK;
+  VLB_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof h));
+  if (h[vlbk::kErrTimeout]) return fail(ctx, VLB_ERR_TIMEOUT, "a bounded device wait gave up (%d)", h[vlbk::kErrTimeout]);
+  if (h[vlbk::kErrStackOverflow])
+    return fail(ctx, VLB_ERR_INTERNAL, "BVH traversal stack overflow on %d rays", h[vlbk::kErrStackOverflow]);
+  return fail(ctx, VLB_ERR_INTERNAL, "device-side check failed (%d)", h[vlbk::kErrBadInput]);
+}
+
+vlb_status finish(vlb_ctx* ctx, bool sync) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+  sync = sync || ctx->host_inputs_pending;
+  ctx->host_inputs_pending = false;
+  if (!sync) return VLB_OK;
+  VLB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return check_device_errors(ctx);
+}
+
+// Brackets kernel launches with CUDA events when profiling is on.
+struct KScope {
+  vlb_ctx* ctx;
+  std::string name;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int nkernels;
+  KScope(vlb_ctx* c, const char* n, int k = 1) : ctx(c), name(n), nkernels(k) {
+    if (!ctx->profiling) return;
+    a = take(); b = take();
+    cudaEventRecord(a, ctx->stream);
+  }
+  cudaEvent_t take() {
+    if (!ctx->event_pool.empty()) { cudaEvent_t e = ctx->event_pool.back(); ctx->event_pool.pop_back(); return e; }
+    cudaEvent_t e; cudaEventCreate(&e); return e;
+  }
+  ~KScope() {
+    ctx->launches += uint64_t(nkernels);
+    if (!a) return;
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending.push_back({name, a, b});
+  }
+};
+
+void drain_profile(vlb_ctx* ctx) {
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      auto& s = ctx->stats[p.name];
+      s.launches += 1;
+      s.ms += ms;
+    }
+    ctx->event_pool.push_back(p.a);
+    ctx->event_pool.push_back(p.b);
+  }
+  ctx->pending.clear();
+  cudaGetLastError();
+}
+
+// ---- SH basis on the host (FP64), shaders/sh_common.h:26-116 ------------------
+void sh_basis16(double x, double y, double z, double* o) {
+  o[0] = 0.282095;
+  o[1] = -0.488603 * y; o[2] = 0.488603 * z; o[3] = -0.488603 * x;
+  o[4] = 1.092548 * x * y; o[5] = -1.092548 * y * z; o[6] = 0.315392 * (-x * x - y * y + 2.0 * z * z);
+  o[7] = -1.092548 * x * z; o[8] = 0.546274 * (x * x - y * y);
+  o[9] = -0.590044 * y * (3.0 * x * x - y * y); o[10] = 2.890611 * x * y * z;
+  o[11] = -0.457046 * y * (4.0 * z * z - x * x - y * y);
+  o[12] = 0.373176 * z * (2.0 * z * z - 3.0 * x * x - 3.0 * y * y);
+  o[13] = -0.457046 * x * (4.0 * z * z - x * x - y * y);
+  o[14] = 1.445306 * z * (x * x - y * y); o[15] = -0.590044 * x * (x * x - 3.0 * y * y);
+}
+
+// Builds the host + device halves of a direction set.
+vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>& bdirs, const std::vector<double>& w) {
+  const uint32_t n = d->n;
+  d->h_basis.assign(size_t(n) * 16, 0.0);
+  d->h_basis32.assign(size_t(n) * 16, 0.f);
+  for (uint32_t s = 0; s < n; ++s) {
+    double Y[16];
+    sh_basis16(bdirs[3 * s], bdirs[3 * s + 1], bdirs[3 * s + 2], Y);
+    for (int k = 0; k < 16; ++k) {
+      d->h_basis[size_t(s) * 16 + k] = w[s] * Y[k];
+      d->h_basis32[size_t(s) * 16 + k] = float(w[s] * Y[k]);
+    }
+  }
+  std::vector<float> d4(size_t(n) * 4, 0.f);
+  for (uint32_t s = 0; s < n; ++s)
+    for (int a = 0; a < 3; ++a) d4[4 * s + a] = d->h_dirs[3 * s + a];
+  VLB_CUDA(ctx, cudaMalloc(&d->d_dirs, size_t(n) * sizeof(float4)));
+  VLB_CUDA(ctx, cudaMalloc(&d->d_basis16, size_t(n) * 16 * sizeof(float)));
+  VLB_CUDA(ctx, cudaMemcpy(d->d_dirs, d4.data(), d4.size() * 4, cudaMemcpyHostToDevice));
+  VLB_CUDA(ctx, cudaMemcpy(d->d_basis16, d->h_basis32.data(), d->h_basis32.size() * 4, cudaMemcpyHostToDevice));
+  return VLB_OK;
+}
+
+// Panorama direction tables: per column (cos phi, sin phi), per row
+// (sin theta, cos theta, pixel weight); sh_common.h:14-22, sh.comp:28-33,
+// skybox_sh.comp:28 (phi - PI/2).
+void pano_tables(uint32_t w, uint32_t h, bool shift, std::vector<float>& col, std::vector<float>& row) {
+  col.assign(size_t(w) * 2, 0.f);
+  row.assign(size_t(h) * 4, 0.f);
+  const double area = (2.0 * kPiRef / w) * (kPiRef / h);
+  for (uint32_t x = 0; x < w; ++x) {
+    double phi = 2.0 * kPiRef * (double(x) + 0.5) / double(w);
+    if (shift) phi -= kPiRef / 2.0;
+    col[2 * x] = float(std::cos(phi));
+    col[2 * x + 1] = float(std::sin(phi));
+  }
+  for (uint32_t y = 0; y < h; ++y) {
+    const double th = kPiRef * (double(y) + 0.5) / double(h);
+    row[4 * y] = float(std::sin(th));
+    row[4 * y + 1] = float(std::cos(th));
+    row[4 * y + 2] = float(area * std::sin(th));
+  }
+}
+
+uint32_t k_of(uint32_t lmax) { return (lmax + 1) * (lmax + 1); }
+
+struct SplitMix64 {
+  uint64_t s;
+  explicit SplitMix64(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  // 24 random bits -> float in [0, 1), exact
+  float uniform() { return float(next() >> 40) * 0x1p-24f; }
+  float range(float lo, float hi) {
+    volatile float span = hi - lo;
+    volatile float t = span * uniform();
+    return lo + t;
+  }
+  void unit_dir(double* d, bool upper) {
+    for (;;) {
+      const double x = 2.0 * uniform() - 1.0, y = 2.0 * uniform() - 1.0, z = 2.0 * uniform() - 1.0;
+      const double r2 = x * x + y * y + z * z;
+      if (r2 > 1.0 || r2 < 1e-6) continue;
+      if (upper && y <= 0.0) continue;
+      const double r = std::sqrt(r2);
+      d[0] = x / r; d[1] = y / r; d[2] = z / r;
+      return;
+    }
+  }
+};
+
+void cube_face_dir(int face, double u, double v, double* d) {
+  switch (face) {
+    case 0: d[0] = 1.0; d[1] = -v; d[2] = -u; break;
+    case 1: d[0] = -1.0; d[1] = -v; d[2] = u; break;
+    case 2: d[0] = u; d[1] = 1.0; d[2] = v; break;
+    case 3: d[0] = u; d[1] = -1.0; d[2] = -v; break;
+    case 4: d[0] = u; d[1] = -v; d[2] = 1.0; break;
+    default: d[0] = -u; d[1] = -v; d[2] = -1.0; break;
+  }
+  const double n = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  d[0] /= n; d[1] /= n; d[2] /= n;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t vlb_version(void) { return VLB_VERSION; }
+
+const char* vlb_status_string(vlb_status s) {
+  switch (s) {
+    case VLB_OK: return "ok";
+    case VLB_ERR_INVALID: return "invalid argument";
+    case VLB_ERR_OOM: return "out of memory";
+    case VLB_ERR_TIMEOUT: return "timeout";
+    case VLB_ERR_CUDA: return "cuda error";
+    case VLB_ERR_UNSUPPORTED: return "unsupported";
+    case VLB_ERR_INTERNAL: return "internal device check";
+  }
+  return "unknown";
+}
+
+// ---- context -------------------------------------------------------------------
+vlb_status vlb_ctx_create(int device, vlb_ctx** out) {
+  if (!out) return VLB_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return VLB_ERR_CUDA; }
+  if (device < 0 || device >= ndev) return VLB_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return VLB_ERR_CUDA;
+  vlb_ctx* c = new (std::nothrow) vlb_ctx();
+  if (!c) return VLB_ERR_OOM;
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_err, vlbk::kErrSlots * sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->d_err, 0, vlbk::kErrSlots * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    vlb_ctx_destroy(c);
+    return VLB_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return VLB_OK;
+}
+
+void vlb_ctx_destroy(vlb_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drain_profile(ctx);
+  for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
+  for (auto& kv : ctx->cube_sa) cudaFree(kv.second);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+vlb_status vlb_ctx_set_stream(vlb_ctx* ctx, void* stream) {
+  if (!ctx) return VLB_ERR_INVALID;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return VLB_OK;
+}
+
+void* vlb_ctx_get_stream(vlb_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+vlb_status vlb_ctx_synchronize(vlb_ctx* ctx) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  return finish(ctx, true);
+}
+
+const char* vlb_last_error(const vlb_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+vlb_status vlb_ctx_set_profiling(vlb_ctx* ctx, int enable) {
+  if (!ctx) return VLB_ERR_INVALID;
+  ctx->profiling = enable != 0;
+  return VLB_OK;
+}
+
+vlb_status vlb_ctx_profile_read(vlb_ctx* ctx, vlb_kernel_time* out, uint32_t cap, uint32_t* n) {
+  if (!ctx || (!out && cap)) return VLB_ERR_INVALID;
+  VLB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  drain_profile(ctx);
+  uint32_t i = 0;
+  for (auto& kv : ctx->stats) {
+    if (i >= cap) break;
+    std::memset(out[i].name, 0, sizeof out[i].name);
+    std::strncpy(out[i].name, kv.first.c_str(), sizeof out[i].name - 1);
+    out[i].launches = kv.second.launches;
+    out[i].total_ms = kv.second.ms;
+    ++i;
+  }
+  if (n) *n = i;
+  return VLB_OK;
+}
+
+vlb_status vlb_ctx_profile_reset(vlb_ctx* ctx) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaStreamSynchronize(ctx->stream);
+  drain_profile(ctx);
+  ctx->stats.clear();
+  return VLB_OK;
+}
+
+uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---- probe grid (light_baker.cpp:138-159) ---------------------------------------
+vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts[3], float* out_xyz,
+                                    float grid_step[3]) {
+  if (!bounds || !counts || !out_xyz) return VLB_ERR_INVALID;
+  if (!counts[0] || !counts[1] || !counts[2]) return VLB_ERR_INVALID;
+  float st[3];
+  for (int a = 0; a < 3; ++a) {
+    volatile float e = bounds[3 + a] - bounds[a];
+    volatile float c = float(counts[a]) - 1.f;
+    st[a] = e / c;
+    if (grid_step) grid_step[a] = st[a];
+  }
+  size_t m = 1;
+  out_xyz[0] = bounds[0]; out_xyz[1] = bounds[1]; out_xyz[2] = bounds[2];
+  for (int dim = 0; dim < 3; ++dim) {
+    const size_t prev = m;
+    for (size_t q = 0; q < prev; ++q) {
+      float p[3] = {out_xyz[3 * q], out_xyz[3 * q + 1], out_xyz[3 * q + 2]};
+      for (uint32_t i = 0; i + 1 < counts[dim]; ++i) {
+        volatile float v = p[dim] + st[dim];
+        p[dim] = v;
+        out_xyz[3 * m] = p[0]; out_xyz[3 * m + 1] = p[1]; out_xyz[3 * m + 2] = p[2];
+        ++m;
+      }
+    }
+  }
+  return VLB_OK;
+}
+
+// ---- scene ----------------------------------------------------------------------------
+vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t stride_bytes, uint32_t nverts,
+                            const uint32_t* indices, uint32_t ntris, const float* tri_albedo, vlb_scene** out) {
+  if (!ctx || !out) return VLB_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  if (stride_bytes < 12 || stride_bytes % 4) return fail(ctx, VLB_ERR_INVALID, "position stride %u", stride_bytes);
+  if (ntris && (!positions || !indices || nverts == 0)) return fail(ctx, VLB_ERR_INVALID, "missing geometry");
+  if (ntris > (1u << 30)) return fail(ctx, VLB_ERR_INVALID, "too many triangles (%u)", ntris);
+  const uint32_t sf = stride_bytes / 4;
+  // Host copies for validation and bounds (scene creation is not on the hot path).
+  std::vector<float> hpos(size_t(nverts) * sf);
+  std::vector<uint32_t> hidx(size_t(ntris) * 3);
+  if (nverts) VLB_CUDA(ctx, cudaMemcpy(hpos.data(), positions, hpos.size() * 4, cudaMemcpyDefault));
+  if (ntris) VLB_CUDA(ctx, cudaMemcpy(hidx.data(), indices, hidx.size() * 4, cudaMemcpyDefault));
+  for (size_t i = 0; i < hidx.size(); ++i)
+    if (hidx[i] >= nverts) return fail(ctx, VLB_ERR_INVALID, "index %u out of range at %zu", hidx[i], i);
+  vlb_scene* sc = new (std::nothrow) vlb_scene();
+  if (!sc) return VLB_ERR_OOM;
+  sc->ctx = ctx; sc->ntris = ntris; sc->nverts = nverts;
+  for (int a = 0; a < 3; ++a) { sc->bounds[a] = INFINITY; sc->bounds[3 + a] = -INFINITY; }
+  for (uint32_t v = 0; v < nverts; ++v)
+    for (int a = 0; a < 3; ++a) {
+      sc->bounds[a] = std::min(sc->bounds[a], hpos[size_t(v) * sf + a]);
+      sc->bounds[3 + a] = std::max(sc->bounds[3 + a], hpos[size_t(v) * sf + a]);
+    }
+  if (nverts == 0) for (int a = 0; a < 6; ++a) sc->bounds[a] = 0.f;
+  if (ntris == 0) { *out = sc; return VLB_OK; }
+  const uint32_t n = ntris;
+  auto alloc = [&](void** p, size_t bytes) -> bool {
+    if (cudaMalloc(p, std::max<size_t>(bytes, 16)) != cudaSuccess) { cudaGetLastError(); return false; }
+    sc->bytes += bytes;
+    return true;
+  };
+  float* dpos = nullptr; uint32_t* didx = nullptr; float* dalb = nullptr; void* scr = nullptr;
+  bool ok = alloc((void**)&sc->codes, size_t(n) * 4) && alloc((void**)&sc->order, size_t(n) * 4) &&
+            alloc((void**)&sc->child, size_t(2) * (n - 1 + (n == 1)) * 4) &&
+            alloc((void**)&sc->box, size_t(2 * n - 1) * 6 * 4) &&
+            alloc((void**)&sc->nodes, size_t(n - 1 + (n == 1)) * 64) && alloc((void**)&sc->tris, size_t(n) * 48) &&
+            alloc((void**)&sc->albedo, size_t(n) * 16);
+  const size_t scr_bytes = vlbk::lbvh_scratch_bytes(n);
+  ok = ok && cudaMalloc((void**)&dpos, hpos.size() * 4) == cudaSuccess &&
+       cudaMalloc((void**)&didx, hidx.size() * 4) == cudaSuccess &&
+       (!tri_albedo || cudaMalloc((void**)&dalb, size_t(n) * 12) == cudaSuccess) &&
+       cudaMalloc(&scr, scr_bytes) == cudaSuccess;
+  vlb_status st = VLB_OK;
+  if (!ok) {
+    cudaGetLastError();
+    st = fail(ctx, VLB_ERR_OOM, "scene allocation failed (%u triangles)", n);
+  } else {
+    cudaMemcpyAsync(dpos, hpos.data(), hpos.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(didx, hidx.data(), hidx.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (tri_albedo) cudaMemcpyAsync(dalb, tri_albedo, size_t(n) * 12, cudaMemcpyDefault, ctx->stream);
+    vlbk::LbvhBuild b{};
+    b.positions = dpos; b.stride_floats = sf; b.nverts = nverts; b.indices = didx; b.albedo = dalb; b.ntris = n;
+    b.codes = sc->codes; b.order = sc->order; b.child = sc->child; b.box = sc->box; b.nodes = sc->nodes;
+    b.tris = sc->tris; b.tri_albedo = sc->albedo; b.scratch = scr; b.scratch_bytes = scr_bytes;
+    int launches = 0;
+    {
+      KScope k(ctx, "lbvh_build", 0);
+      vlbk::launch_lbvh_build(b, ctx->stream, &launches);
+      k.nkernels = launches;
+    }
+    st = finish(ctx, true);
+  }
+  cudaFree(dpos); cudaFree(didx); if (dalb) cudaFree(dalb); cudaFree(scr);
+  if (st != VLB_OK) { vlb_scene_destroy(sc); return st; }
+  *out = sc;
+  return VLB_OK;
+}
+
+void vlb_scene_destroy(vlb_scene* s) {
+  if (!s) return;
+  if (s->ctx) { cudaSetDevice(s->ctx->device); cudaStreamSynchronize(s->ctx->stream); }
+  cudaFree(s->codes); cudaFree(s->order); cudaFree(s->child); cudaFree(s->box);
+  cudaFree(s->nodes); cudaFree(s->tris); cudaFree(s->albedo);
+  delete s;
+}
+
+uint32_t vlb_scene_triangle_count(const vlb_scene* s) { return s ? s->ntris : 0; }
+
+vlb_status vlb_scene_bounds(const vlb_scene* s, int include_origin, float out[6]) {
+  if (!s || !out) return VLB_ERR_INVALID;
+  for (int a = 0; a < 6; ++a) out[a] = s->bounds[a];
+  if (include_origin)
+    for (int a = 0; a < 3; ++a) { out[a] = std::min(out[a], 0.f); out[3 + a] = std::max(out[3 + a], 0.f); }
+  return VLB_OK;
+}
+
+vlb_status vlb_scene_bvh_export(const vlb_scene* s, uint32_t* codes, uint32_t* order, int32_t* children,
+                                float* boxes) {
+  if (!s) return VLB_ERR_INVALID;
+  vlb_ctx* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  VLB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const size_t n = s->ntris;
+  if (n == 0) return VLB_OK;
+  if (codes) VLB_CUDA(ctx, cudaMemcpy(codes, s->codes, n * 4, cudaMemcpyDefault));
+  if (order) VLB_CUDA(ctx, cudaMemcpy(order, s->order, n * 4, cudaMemcpyDefault));
+  if (children && n > 1) VLB_CUDA(ctx, cudaMemcpy(children, s->child, 2 * (n - 1) * 4, cudaMemcpyDefault));
+  if (boxes) VLB_CUDA(ctx, cudaMemcpy(boxes, s->box, (2 * n - 1) * 24, cudaMemcpyDefault));
+  return VLB_OK;
+}
+
+uint64_t vlb_scene_device_bytes(const vlb_scene* s) { return s ? s->bytes : 0; }
+
+// ---- direction sets -------------------------------------------------------------------
+vlb_status vlb_dirset_create_fibonacci(vlb_ctx* ctx, uint32_t n, vlb_frame frame, vlb_dirset** out) {
+  if (!ctx || !out || n == 0 || (frame != VLB_FRAME_WORLD && frame != VLB_FRAME_XZY)) return VLB_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  vlb_dirset* d = new (std::nothrow) vlb_dirset();
+  if (!d) return VLB_ERR_OOM;
+  d->ctx = ctx; d->n = n;
+  d->h_dirs.resize(size_t(n) * 3);
+  std::vector<double> bd(size_t(n) * 3), w(n, 4.0 * kPi / double(n));
+  const double g = 0.6180339887498949, two_pi = 6.283185307179586;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double z = 1.0 - (2.0 * i + 1.0) / double(n);
+    const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
+    double fr = double(i) * g;
+    fr -= std::floor(fr);
+    const double phi = two_pi * fr;
+    const float f[3] = {float(r * std::cos(phi)), float(r * std::sin(phi)), float(z)};
+    for (int a = 0; a < 3; ++a) d->h_dirs[3 * i + a] = f[a];
+    if (frame == VLB_FRAME_WORLD) { bd[3 * i] = f[0]; bd[3 * i + 1] = f[1]; bd[3 * i + 2] = f[2]; }
+    else { bd[3 * i] = f[0]; bd[3 * i + 1] = f[2]; bd[3 * i + 2] = f[1]; }
+  }
+  vlb_status st = dirset_finish(ctx, d, bd, w);
+  if (st) { vlb_dirset_destroy(d); return st; }
+  *out = d;
+  return VLB_OK;
+}
+
+vlb_status vlb_dirset_create_equirect(vlb_ctx* ctx, uint32_t w, uint32_t h, vlb_dirset** out) {
+  if (!ctx || !out || !w || !h || uint64_t(w) * h > (1u << 28)) return VLB_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  vlb_dirset* d = new (std::nothrow) vlb_dirset();
+  if (!d) return VLB_ERR_OOM;
+  const uint32_t n = w * h;
+  d->ctx = ctx; d->n = n;
+  d->h_dirs.resize(size_t(n) * 3);
+  std::vector<double> bd(size_t(n) * 3), wt(n);
+  for (uint32_t y = 0; y < h; ++y)
+    for (uint32_t x = 0; x < w; ++x) {
+      const size_t s = size_t(y) * w + x;
+      const double phi = 2.0 * kPiRef * (double(x) + 0.5) / double(w);
+      const double th = kPiRef * (double(y) + 0.5) / double(h);
+      const double r = std::sin(th);
+      double v[3] = {r * std::cos(phi), r * std::sin(phi), std::cos(th)};
+      const double nn = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      for (int a = 0; a < 3; ++a) v[a] /= nn;
+      d->h_dirs[3 * s] = float(v[0]); d->h_dirs[3 * s + 1] = float(v[2]); d->h_dirs[3 * s + 2] = float(v[1]);
+      bd[3 * s] = v[0]; bd[3 * s + 1] = v[1]; bd[3 * s + 2] = v[2];
+      wt[s] = (2.0 * kPiRef / w) * (kPiRef / h) * std::sin(th);
+    }
+  vlb_status st = dirset_finish(ctx, d, bd, wt);
+  if (st) { vlb_dirset_destroy(d); return st; }
+  *out = d;
+  return VLB_OK;
+}
+
+vlb_status vlb_dirset_create(vlb_ctx* ctx, const float* trace_dirs, const float* basis_dirs, const double* weights,
+                             uint32_t n, vlb_dirset** out) {
+  if (!ctx || !out || !trace_dirs || !weights || n == 0) return VLB_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  vlb_dirset* d = new (std::nothrow) vlb_dirset();
+  if (!d) return VLB_ERR_OOM;
+  d->ctx = ctx; d->n = n;
+  d->h_dirs.assign(trace_dirs, trace_dirs + size_t(n) * 3);
+  std::vector<double> bd(size_t(n) * 3), w(weights, weights + n);
+  const float* b = basis_dirs ? basis_dirs : trace_dirs;
+  for (size_t i = 0; i < size_t(n) * 3; ++i) bd[i] = b[i];
+  vlb_status st = dirset_finish(ctx, d, bd, w);
+  if (st) { vlb_dirset_destroy(d); return st; }
+  *out = d;
+  return VLB_OK;
+}
+
+void vlb_dirset_destroy(vlb_dirset* d) {
+  if (!d) return;
+  if (d->ctx) { cudaSetDevice(d->ctx->device); cudaStreamSynchronize(d->ctx->stream); }
+  cudaFree(d->d_dirs);
+  cudaFree(d->d_basis16);
+  delete d;
+}
+
+uint32_t vlb_dirset_count(const vlb_dirset* d) { return d ? d->n : 0; }
+
+vlb_status vlb_dirset_export(const vlb_dirset* d, float* trace_dirs, float* basis) {
+  if (!d) return VLB_ERR_INVALID;
+  vlb_ctx* ctx = d->ctx;
+  cudaSetDevice(ctx->device);
+  if (trace_dirs) {
+    std::vector<float> d4(size_t(d->n) * 4);
+    VLB_CUDA(ctx, cudaMemcpy(d4.data(), d->d_dirs, d4.size() * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t s = 0; s < d->n; ++s)
+      for (int a = 0; a < 3; ++a) trace_dirs[3 * s + a] = d4[4 * s + a];
+  }
+  if (basis) VLB_CUDA(ctx, cudaMemcpy(basis, d->d_basis16, size_t(d->n) * 64, cudaMemcpyDeviceToHost));
+  return VLB_OK;
+}
+
+// ---- skybox SH ---------------------------------------------------------------------------
+static vlb_status cube_sa_table(vlb_ctx* ctx, uint32_t n, const float** out) {
+  auto it = ctx->cube_sa.find(n);
+  if (it != ctx->cube_sa.end()) { *out = it->second; return VLB_OK; }
+  float* p = nullptr;
+  VLB_CUDA(ctx, cudaMalloc(&p, size_t(n) * n * 4));
+  {
+    KScope k(ctx, "cube_solid_angle");
+    vlbk::launch_cube_solid_angle(p, n, ctx->stream);
+  }
+  ctx->cube_sa[n] = p;
+  *out = p;
+  return VLB_OK;
+}
+
+vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt, vlb_sky_layout layout,
+                                 uint32_t w, uint32_t h, uint32_t count, uint32_t lmax, uint32_t flags, float* out) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (!texels || !out) return fail(ctx, VLB_ERR_INVALID, "null texels or output");
+  if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
+  if (fmt != VLB_TEXEL_RGB32F && fmt != VLB_TEXEL_RGBA8) return fail(ctx, VLB_ERR_INVALID, "texel format %d", fmt);
+  if (layout != VLB_SKY_CUBEMAP && layout != VLB_SKY_PANORAMA && layout != VLB_SKY_ENVMAP)
+    return fail(ctx, VLB_ERR_INVALID, "layout %d", layout);
+  if (!w || !h || !count) return fail(ctx, VLB_ERR_INVALID, "empty image");
+  if (layout == VLB_SKY_CUBEMAP && w != h) return fail(ctx, VLB_ERR_INVALID, "cubemap faces must be square");
+  const uint64_t T64 = layout == VLB_SKY_CUBEMAP ? 6ull * w * w : uint64_t(w) * h;
+  if (T64 >= (1ull << 31) || T64 * count >= (1ull << 40)) return fail(ctx, VLB_ERR_INVALID, "image too large");
+  const uint32_t T = uint32_t(T64);
+  const uint32_t TB = fmt == VLB_TEXEL_RGB32F ? 12 : 4;
+  const uint32_t K = k_of(lmax), V = 3 * K;
+  const void* dtex;
+  vlb_status st = stage_in(ctx, texels, size_t(T) * count * TB, "sky_in", &dtex);
+  if (st) return st;
+  vlbk::SkyboxArgs a{};
+  a.texels = dtex; a.fmt = fmt; a.layout = layout; a.w = w; a.h = h; a.count = count; a.lmax = lmax;
+  a.flags = flags; a.texels_per_map = T; a.err = ctx->d_err;
+  if (layout == VLB_SKY_CUBEMAP) {
+    st = cube_sa_table(ctx, w, &a.solid_angle);
+    if (st) return st;
+  } else {
+    std::vector<float> col, row;
+    pano_tables(w, h, layout == VLB_SKY_PANORAMA, col, row);
+    void *dc, *dr;
+    if ((st = scratch(ctx, "pano_col", col.size() * 4, &dc)) || (st = scratch(ctx, "pano_row", row.size() * 4, &dr)))
+      return st;
+    VLB_CUDA(ctx, cudaMemcpyAsync(dc, col.data(), col.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    VLB_CUDA(ctx, cudaMemcpyAsync(dr, row.data(), row.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    VLB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // host vectors go out of scope
+    a.col_tab = static_cast<const float2*>(dc);
+    a.row_tab = static_cast<const float4*>(dr);
+  }
+  // Work units: enough slabs per map for ~2 CTAs per SM in total.
+  const uint32_t chunk = 1024;
+  const uint32_t max_slabs = (T + chunk - 1) / chunk;
+  uint32_t spm = std::max<uint32_t>(1, uint32_t((2ull * ctx->num_sms + count - 1) / count));
+  spm = std::min(spm, max_slabs);
+  uint32_t slab = ((T + spm - 1) / spm + chunk - 1) / chunk * chunk;
+  spm = (T + slab - 1) / slab;
+  a.slab_texels = slab; a.slabs_per_map = spm;
+  void* part;
+  if ((st = scratch(ctx, "sky_partial", size_t(count) * spm * V * 4, &part))) return st;
+  a.partial = static_cast<float*>(part);
+  const bool tma = (reinterpret_cast<uintptr_t>(dtex) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
+  OutBuf ob;
+  if ((st = stage_out(ctx, out, size_t(count) * V * 4, "sky_out", &ob))) return st;
+  {
+    KScope k(ctx, tma ? "skybox_sh_tma" : "skybox_sh");
+    vlbk::launch_skybox_sh(a, tma, ctx->num_sms, ctx->stream);
+  }
+  {
+    KScope k(ctx, "sh_finalize");
+    vlbk::launch_sh_finalize(a.partial, count, spm, V, static_cast<float*>(ob.dev), ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob))) return st;
+  return finish(ctx, ob.host);
+}
+
+vlb_status vlb_skybox_sh(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt, vlb_sky_layout layout, uint32_t w,
+                         uint32_t h, uint32_t lmax, uint32_t flags, float* out) {
+  return vlb_skybox_sh_batched(ctx, texels, fmt, layout, w, h, 1, lmax, flags, out);
+}
+
+vlb_status vlb_sky_create(vlb_ctx* ctx, const float* cubemap_rgb, uint32_t n, vlb_sky** out) {
+  if (!ctx || !out || !cubemap_rgb || n == 0 || n > 16384) return VLB_ERR_INVALID;
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  vlb_sky* s = new (std::nothrow) vlb_sky();
+  if (!s) return VLB_ERR_OOM;
+  s->ctx = ctx; s->n = n;
+  const size_t bytes = size_t(6) * n * n * 12;
+  if (cudaMalloc(&s->d_texels, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return fail(ctx, VLB_ERR_OOM, "sky allocation");
+  }
+  if (cudaMemcpy(s->d_texels, cubemap_rgb, bytes, cudaMemcpyDefault) != cudaSuccess) {
+    cudaGetLastError();
+    vlb_sky_destroy(s);
+    return fail(ctx, VLB_ERR_CUDA, "sky upload");
+  }
+  *out = s;
+  return VLB_OK;
+}
+
+void vlb_sky_destroy(vlb_sky* s) {
+  if (!s) return;
+  if (s->ctx) { cudaSetDevice(s->ctx->device); cudaStreamSynchronize(s->ctx->stream); }
+  cudaFree(s->d_texels);
+  delete s;
+}
+
+// ---- bake ------------------------------------------------------------------------------------
+void vlb_bake_params_default(vlb_bake_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->lmax = 3;
+  p->precision = VLB_PREC_FP32;
+  p->sun_dir[0] = 0.f; p->sun_dir[1] = 1.f; p->sun_dir[2] = 0.f;
+  p->sun_intensity = 5.f;
+  p->tmin = 0.001f; p->tmax = 10000.f;
+  p->shadow_bias = 0.005f;
+}
+
+static uint32_t pick_dirs_per_warp(const vlb_ctx* ctx, uint32_t nprobes, uint32_t S) {
+  const uint64_t groups = (nprobes + 31) / 32;
+  const uint64_t target = uint64_t(ctx->num_sms) * 32;  // warps in flight
+  uint64_t nsc = (target + groups - 1) / groups;
+  nsc = std::max<uint64_t>(1, std::min<uint64_t>(nsc, S));
+  return uint32_t((S + nsc - 1) / nsc);
+}
+
+vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                       const vlb_bake_params* p, float* out, const vlb_bake_debug* dbg) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
+  if (scene->ctx != ctx || p->dirs->ctx != ctx || (p->sky && p->sky->ctx != ctx))
+    return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
+  if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
+  if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
+  if (nprobes == 0) return VLB_OK;
+  if (!probe_xyz || !out) return fail(ctx, VLB_ERR_INVALID, "null probes or output");
+  const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
+                              double(p->sun_dir[2]) * p->sun_dir[2]);
+  if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
+  if (!(p->tmax > p->tmin) || p->tmin < 0.f) return fail(ctx, VLB_ERR_INVALID, "bad ray interval");
+  const uint32_t S = p->dirs->n, K = k_of(p->lmax), V = 3 * K;
+  const uint64_t rays = uint64_t(nprobes) * S;
+  vlb_status st;
+  const void* dprobes;
+  if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
+  vlbk::TraceArgs a{};
+  a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
+  a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
+  a.dirs = p->dirs->d_dirs; a.S = S;
+  a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
+  a.sun_scale = float(double(p->sun_intensity) / kPi);
+  a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
+  a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
+  a.basis16 = p->dirs->d_basis16; a.K = K; a.err = ctx->d_err;
+  OutBuf ob, oh, os, orad;
+  if ((st = stage_out(ctx, out, size_t(nprobes) * V * 4, "bake_out", &ob))) return st;
+  if (dbg) {
+    if ((st = stage_out(ctx, dbg->hit_tri, rays * 4, "dbg_hit", &oh)) ||
+        (st = stage_out(ctx, dbg->shadow, rays, "dbg_shadow", &os)) ||
+        (st = stage_out(ctx, dbg->radiance, rays * 12, "dbg_rad", &orad)))
+      return st;
+    a.hit_tri = static_cast<int32_t*>(oh.dev);
+    a.shadow = static_cast<uint8_t*>(os.dev);
+    a.dbg_radiance = static_cast<float*>(orad.dev);
+  }
+  a.dirs_per_warp = pick_dirs_per_warp(ctx, nprobes, S);
+  if (p->precision == VLB_PREC_FUSED) {
+    const uint32_t nsc = (S + a.dirs_per_warp - 1) / a.dirs_per_warp;
+    void* part;
+    if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * nsc * V * 4, &part))) return st;
+    a.partial = static_cast<float*>(part);
+    if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "per-ray radiance is not kept by the fused path");
+    uint32_t chunks = 0;
+    {
+      KScope k(ctx, "trace_fused");
+      vlbk::launch_trace_fused(a, ctx->stream, &chunks);
+    }
+    {
+      KScope k(ctx, "sh_finalize");
+      vlbk::launch_sh_finalize(a.partial, nprobes, chunks, V, static_cast<float*>(ob.dev), ctx->stream);
+    }
+  } else {
+    const bool bf16 = p->precision == VLB_PREC_MIXED;
+    void* tile;
+    if ((st = scratch(ctx, "bake_tile", rays * 3 * (bf16 ? 2 : 4), &tile))) return st;
+    if (bf16) a.radiance_bf16 = static_cast<uint16_t*>(tile);
+    else a.radiance = static_cast<float*>(tile);
+    {
+      KScope k(ctx, "trace_tile");
+      vlbk::launch_trace_tile(a, ctx->stream);
+    }
+    {
+      KScope k(ctx, bf16 ? "project_bf16" : "project_f32");
+      if (bf16)
+        vlbk::launch_project_bf16_simt(a.radiance_bf16, nprobes, S, p->dirs->d_basis16, K,
+                                       static_cast<float*>(ob.dev), ctx->stream);
+      else
+        vlbk::launch_project_f32(a.radiance, nprobes, S, p->dirs->d_basis16, K, static_cast<float*>(ob.dev),
+                                 ctx->stream);
+    }
+  }
+  if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) || (st = copy_out(ctx, orad)))
+    return st;
+  return finish(ctx, ob.host || oh.host || os.host || orad.host);
+}
+
+vlb_status vlb_bake(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                    const vlb_bake_params* params, float* out) {
+  return vlb_bake_ex(ctx, scene, probe_xyz, nprobes, params, out, nullptr);
+}
+
+vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                                const vlb_bake_params* p, uint64_t out[4]) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (!scene || !p || !p->dirs || !out) return fail(ctx, VLB_ERR_INVALID, "scene, params, dirs and out are required");
+  if (scene->ctx != ctx || p->dirs->ctx != ctx) return fail(ctx, VLB_ERR_INVALID, "handles of another context");
+  if (nprobes == 0 || !probe_xyz) return fail(ctx, VLB_ERR_INVALID, "no probes");
+  const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
+                              double(p->sun_dir[2]) * p->sun_dir[2]);
+  if (!(sl > 0.0)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
+  const uint32_t S = p->dirs->n;
+  vlb_status st;
+  const void* dprobes;
+  if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
+  void *tile, *cnt;
+  if ((st = scratch(ctx, "bake_tile", size_t(nprobes) * S * 12, &tile)) || (st = scratch(ctx, "trace_counters", 64, &cnt)))
+    return st;
+  VLB_CUDA(ctx, cudaMemsetAsync(cnt, 0, 64, ctx->stream));
+  vlbk::TraceArgs a{};
+  a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
+  a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
+  a.dirs = p->dirs->d_dirs; a.S = S;
+  a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
+  a.sun_scale = float(double(p->sun_intensity) / kPi);
+  a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
+  a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
+  a.radiance = static_cast<float*>(tile);
+  a.counters = static_cast<unsigned long long*>(cnt);
+  a.err = ctx->d_err;
+  a.dirs_per_warp = pick_dirs_per_warp(ctx, nprobes, S);
+  {
+    KScope k(ctx, "trace_tile_counted");
+    vlbk::launch_trace_tile(a, ctx->stream);
+  }
+  if ((st = finish(ctx, true))) return st;
+  unsigned long long h[3];
+  VLB_CUDA(ctx, cudaMemcpy(h, cnt, sizeof h, cudaMemcpyDeviceToHost));
+  out[0] = uint64_t(nprobes) * S;
+  out[1] = h[2];
+  out[2] = h[0];
+  out[3] = h[1];
+  return VLB_OK;
+}
+
+// ---- projection / reconstruction --------------------------------------------------------
+vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint32_t nprobes, const vlb_dirset* dirs,
+                       uint32_t lmax, float* out) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (!dirs || dirs->ctx != ctx) return fail(ctx, VLB_ERR_INVALID, "direction set missing or from another context");
+  if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
+  if (dtype != VLB_DTYPE_F32 && dtype != VLB_DTYPE_BF16) return fail(ctx, VLB_ERR_INVALID, "dtype %d", dtype);
+  if (nprobes == 0) return VLB_OK;
+  if (!radiance || !out) return fail(ctx, VLB_ERR_INVALID, "null radiance or output");
+  const uint32_t S = dirs->n, K = k_of(lmax);
+  const size_t eb = dtype == VLB_DTYPE_F32 ? 4 : 2;
+  vlb_status st;
+  const void* drad;
+  if ((st = stage_in(ctx, radiance, size_t(nprobes) * 3 * S * eb, "proj_in", &drad))) return st;
+  OutBuf ob;
+  if ((st = stage_out(ctx, out, size_t(nprobes) * K * 12, "proj_out", &ob))) return st;
+  {
+    KScope k(ctx, dtype == VLB_DTYPE_F32 ? "project_f32" : "project_bf16");
+    if (dtype == VLB_DTYPE_F32)
+      vlbk::launch_project_f32(static_cast<const float*>(drad), nprobes, S, dirs->d_basis16, K,
+                               static_cast<float*>(ob.dev), ctx->stream);
+    else
+      vlbk::launch_project_bf16_simt(static_cast<const uint16_t*>(drad), nprobes, S, dirs->d_basis16, K,
+                                     static_cast<float*>(ob.dev), ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob))) return st;
+  return finish(ctx, ob.host);
+}
+
+vlb_status vlb_sh_eval_envmap(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, uint32_t w, uint32_t h, float scale,
+                              float* out) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
+  if (!coeffs || !out || !w || !h || uint64_t(w) * h >= (1ull << 31)) return fail(ctx, VLB_ERR_INVALID, "bad image");
+  const uint32_t K = k_of(lmax);
+  vlb_status st;
+  const void* dc;
+  if ((st = stage_in(ctx, coeffs, size_t(K) * 12, "eval_coeffs", &dc))) return st;
+  std::vector<float> col, row;
+  pano_tables(w, h, false, col, row);
+  void *dcol, *drow;
+  if ((st = scratch(ctx, "eval_col", col.size() * 4, &dcol)) || (st = scratch(ctx, "eval_row", row.size() * 4, &drow)))
+    return st;
+  VLB_CUDA(ctx, cudaMemcpyAsync(dcol, col.data(), col.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  VLB_CUDA(ctx, cudaMemcpyAsync(drow, row.data(), row.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  OutBuf ob;
+  if ((st = stage_out(ctx, out, size_t(w) * h * 12, "eval_out", &ob))) return st;
+  {
+    KScope k(ctx, "sh_eval_envmap");
+    vlbk::launch_sh_eval_envmap(static_cast<const float*>(dc), K, w, h, scale, static_cast<const float2*>(dcol),
+                                static_cast<const float4*>(drow), static_cast<float*>(ob.dev), ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob))) return st;
+  VLB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host tables above must outlive their copies
+  return finish(ctx, ob.host);
+}
+
+// ---- synthetic inputs ------------------------------------------------------------------------
+vlb_status vlb_synth_box_scene(uint64_t seed, uint32_t nboxes, float* positions, uint32_t* indices, float* albedo,
+                               uint32_t* nverts, uint32_t* ntris) {
+  if (nboxes > (1u << 24)) return VLB_ERR_INVALID;
+  const uint32_t nv = 8 + 8 * nboxes, nt = 10 + 12 * nboxes;
+  if (nverts) *nverts = nv;
+  if (ntris) *ntris = nt;
+  if (!positions && !indices && !albedo) return VLB_OK;
+  if (!positions || !indices || !albedo) return VLB_ERR_INVALID;
+  // corner c = x + 2y + 4z of a box
+  static const uint32_t room_quads[5][4] = {{0, 4, 5, 1}, {0, 2, 6, 4}, {1, 5, 7, 3}, {0, 1, 3, 2}, {4, 6, 7, 5}};
+  static const uint32_t box_quads[6][4] = {{0, 4, 5, 1}, {2, 3, 7, 6}, {0, 2, 6, 4},
+                                           {1, 5, 7, 3}, {0, 1, 3, 2}, {4, 6, 7, 5}};
+  uint32_t tv = 0, tt = 0;
+  auto corners = [&](const float* lo, const float* hi) {
+    for (uint32_t c = 0; c < 8; ++c) {
+      positions[3 * (tv + c)] = (c & 1) ? hi[0] : lo[0];
+      positions[3 * (tv + c) + 1] = (c & 2) ? hi[1] : lo[1];
+      positions[3 * (tv + c) + 2] = (c & 4) ? hi[2] : lo[2];
+    }
+  };
+  auto quad = [&](const uint32_t* q, const float* rgb) {
+    const uint32_t t[2][3] = {{q[0], q[1], q[2]}, {q[0], q[2], q[3]}};
+    for (int i = 0; i < 2; ++i) {
+      for (int k = 0; k < 3; ++k) { indices[3 * tt + k] = tv + t[i][k]; albedo[3 * tt + k] = rgb[k]; }
+      ++tt;
+    }
+  };
+  const float lo0[3] = {0.f, 0.f, 0.f}, hi0[3] = {1.f, 1.f, 1.f}, grey[3] = {0.5f, 0.5f, 0.5f};
+  corners(lo0, hi0);
+  for (auto& q : room_quads) quad(q, grey);
+  tv += 8;
+  SplitMix64 rng(seed ^ 0x5CE9E5CE9E5CE9EULL);
+  for (uint32_t b = 0; b < nboxes; ++b) {
+    float c[3], e[3], rgb[3];
+    for (int a = 0; a < 3; ++a) c[a] = rng.range(0.1f, 0.9f);
+    for (int a = 0; a < 3; ++a) e[a] = rng.range(0.05f, 0.2f);
+    for (int a = 0; a < 3; ++a) rgb[a] = rng.range(0.2f, 0.8f);
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+      volatile float half = e[a] * 0.5f;
+      lo[a] = c[a] - half;
+      hi[a] = c[a] + half;
+    }
+    corners(lo, hi);
+    for (auto& q : box_quads) quad(q, rgb);
+    tv += 8;
+  }
+  return VLB_OK;
+}
+
+vlb_status vlb_synth_cubemap(uint64_t seed, uint32_t n, float* out) {
+  if (!out || n == 0 || n > 16384) return VLB_ERR_INVALID;
+  SplitMix64 rng(seed ^ 0xC0BE0C0BE0C0BEULL);
+  double mu[3][3], sharp[3], inten[3][3];
+  for (int j = 0; j < 3; ++j) {
+    rng.unit_dir(mu[j], false);
+    sharp[j] = 20.0 + 180.0 * rng.uniform();
+    for (int c = 0; c < 3; ++c) inten[j][c] = 1.0 + 49.0 * rng.uniform();
+  }
+  for (int f = 0; f < 6; ++f)
+    for (uint32_t y = 0; y < n; ++y)
+      for (uint32_t x = 0; x < n; ++x) {
+        double d[3];
+        cube_face_dir(f, 2.0 * (x + 0.5) / n - 1.0, 2.0 * (y + 0.5) / n - 1.0, d);
+        double v[3] = {0.3, 0.3, 0.3};
+        for (int j = 0; j < 3; ++j) {
+          const double g = std::exp(sharp[j] * (d[0] * mu[j][0] + d[1] * mu[j][1] + d[2] * mu[j][2] - 1.0));
+          for (int c = 0; c < 3; ++c) v[c] += inten[j][c] * g;
+        }
+        float* o = out + ((size_t(f) * n + y) * n + x) * 3;
+        o[0] = float(v[0]); o[1] = float(v[1]); o[2] = float(v[2]);
+      }
+  return VLB_OK;
+}
+
+vlb_status vlb_synth_sun(uint64_t seed, float out_dir[3]) {
+  if (!out_dir) return VLB_ERR_INVALID;
+  SplitMix64 rng(seed ^ 0x5E45E45E45E45EULL);
+  double d[3];
+  rng.unit_dir(d, true);
+  for (int a = 0; a < 3; ++a) out_dir[a] = float(d[a]);
+  return VLB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+// vlb_internal.h -- host-side structures and kernel launchers shared by the
+// C ABI (vlb_api.cpp) and the CUDA translation units.  Not installed.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/vlb.h"
+
+namespace vlbk {
+
+// Device error counters (one int each) kept per context.
+enum ErrSlot : int {
+  kErrStackOverflow = 0,  // BVH traversal stack overflow
+  kErrTimeout = 1,        // bounded mbarrier / flag wait gave up
+  kErrBadInput = 2,       // device-side argument check
+  kErrSlots = 8
+};
+
+// Sizes of the bake's trace kernels.
+constexpr int kTraceStack = 64;
+
+// ---- skybox projection ------------------------------------------------------
+struct SkyboxArgs {
+  const void* texels;     // device, count maps back to back
+  int fmt;                // vlb_texel_format
+  int layout;             // vlb_sky_layout
+  uint32_t w, h;          // cubemap: w == h == face size
+  uint32_t count;         // maps
+  uint32_t lmax;          // 2 or 3
+  uint32_t flags;         // VLB_SKY_REF_BGRA_SWAP
+  uint32_t texels_per_map;
+  uint32_t slab_texels;   // texels per work unit (multiple of the chunk)
+  uint32_t slabs_per_map;
+  const float* solid_angle;  // cubemap: w*w table (same for every face)
+  const float2* col_tab;     // panorama: w entries (cos phi, sin phi)
+  const float4* row_tab;     // panorama: h entries (sin theta, cos theta, weight, 0)
+  float* partial;            // count*slabs_per_map*K*3
+  int* err;
+};
+void launch_cube_solid_angle(float* out, uint32_t n, cudaStream_t s);
+// Returns the number of CTAs launched.
+int launch_skybox_sh(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s);
+// out[m][v] = sum_j partial[m][j][v] in FP64, j in fixed order.
+void launch_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, uint32_t nvals, float* out,
+                        cudaStream_t s);
+
+// ---- projection of a radiance tile --------------------------------------------
+void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
+                        float* out, cudaStream_t s);
+void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
+                              uint32_t K, float* out, cudaStream_t s);
+void launch_sh_eval_envmap(const float* coeffs, uint32_t K, uint32_t w, uint32_t h, float scale, const float2* col_tab,
+                           const float4* row_tab, float* out, cudaStream_t s);
+
+// ---- LBVH ---------------------------------------------------------------------
+struct LbvhBuild {
+  // inputs
+  const float* positions;  // device
+  uint32_t stride_floats;
+  uint32_t nverts;
+  const uint32_t* indices;  // device
+  const float* albedo;      // device ntris*3 or null
+  uint32_t ntris;
+  // outputs (device, allocated by the caller)
+  uint32_t* codes;   // n sorted
+  uint32_t* order;   // n sorted -> original
+  int32_t* child;    // 2(n-1)
+  float* box;        // (2n-1)*6
+  float4* nodes;     // (n-1)*4
+  float4* tris;      // n*3 (sorted order): v0|id, e1, e2
+  float4* tri_albedo;  // n (by original index)
+  // scratch (device)
+  void* scratch;
+  size_t scratch_bytes;
+};
+size_t lbvh_scratch_bytes(uint32_t ntris);
+void launch_lbvh_build(const LbvhBuild& b, cudaStream_t s, int* launches);
+
+// ---- trace + shade --------------------------------------------------------------
+struct TraceArgs {
+  const float4* nodes;
+  const float4* tris;
+  const float4* albedo;
+  uint32_t ntris;
+  const float* probes;    // device nprobes*3
+  uint32_t nprobes;
+  const float4* dirs;     // device S (xyz)
+  uint32_t S;
+  float3 sun;             // unit
+  float sun_scale;        // intensity / pi
+  float tmin, tmax, bias;
+  const float* sky;       // device cubemap or null
+  uint32_t sky_n;
+  // outputs
+  float* radiance;        // [nprobes][3][S] fp32 or null
+  uint16_t* radiance_bf16;  // [nprobes][3][S] bf16 or null
+  int32_t* hit_tri;       // [nprobes*S] or null
+  uint8_t* shadow;        // [nprobes*S] or null
+  float* dbg_radiance;    // [nprobes*S*3] or null
+  // fused projection
+  const float* basis16;   // S x 16 fp32 weighted basis
+  uint32_t K;
+  float* partial;         // [chunks][nprobes][K*3]
+  uint32_t dirs_per_warp;
+  unsigned long long* counters;  // null, or [nodes fetched, triangles tested, shadow rays]
+  int* err;
+};
+void launch_trace_tile(const TraceArgs& a, cudaStream_t s);
+void launch_trace_fused(const TraceArgs& a, cudaStream_t s, uint32_t* chunks_out);
+
+}  // namespace vlbk
+
+// ---- host objects behind the opaque handles ------------------------------------
+struct vlb_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int* d_err = nullptr;  // vlbk::kErrSlots ints
+  uint64_t launches = 0;
+  bool host_inputs_pending = false;  // a host array was copied in by the current call
+  bool profiling = false;
+  struct Pending { std::string name; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  struct Stat { uint32_t launches = 0; double ms = 0; };
+  std::map<std::string, Stat> stats;
+  struct Buf { void* p = nullptr; size_t bytes = 0; };
+  std::map<std::string, Buf> scratch;
+  std::map<uint32_t, float*> cube_sa;  // solid-angle tables by face size
+};
+
+struct vlb_scene {
+  vlb_ctx* ctx = nullptr;
+  uint32_t ntris = 0, nverts = 0;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+  uint32_t* codes = nullptr;
+  uint32_t* order = nullptr;
+  int32_t* child = nullptr;
+  float* box = nullptr;
+  float4* nodes = nullptr;
+  float4* tris = nullptr;
+  float4* albedo = nullptr;
+  uint64_t bytes = 0;
+};
+
+struct vlb_dirset {
+  vlb_ctx* ctx = nullptr;
+  uint32_t n = 0;
+  float4* d_dirs = nullptr;     // n trace directions
+  float* d_basis16 = nullptr;   // n x 16 weighted basis, FP32
+  std::vector<float> h_dirs;    // n*3
+  std::vector<double> h_basis;  // n*16 FP64 weighted basis
+  std::vector<float> h_basis32; // n*16
+};
+
+struct vlb_sky {
+  vlb_ctx* ctx = nullptr;
+  uint32_t n = 0;
+  float* d_texels = nullptr;
+};

@@ -1,0 +1,407 @@
+"""ctypes binding of libvlb.so (include/vlb.h) for tests, bench.py and scripts.
+
+Arrays may be numpy arrays (host memory) or torch tensors (host or CUDA); the
+library reads each pointer's residency itself.  Every failed call raises
+VlbError carrying the status code and the context's message.  The library
+must exist: importing this module on a machine where libvlb.so was not built
+raises immediately -- there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("VLB_LIB", _PKG / "_build" / "libvlb.so"))
+
+OK, ERR_INVALID, ERR_OOM, ERR_TIMEOUT, ERR_CUDA, ERR_UNSUPPORTED, ERR_INTERNAL = range(7)
+FRAME_WORLD, FRAME_XZY = 0, 1
+SKY_CUBEMAP, SKY_PANORAMA, SKY_ENVMAP = 0, 1, 2
+TEXEL_RGB32F, TEXEL_RGBA8 = 0, 1
+SKY_REF_BGRA_SWAP = 1
+PREC_FP32, PREC_FUSED, PREC_MIXED = 0, 1, 2
+DTYPE_F32, DTYPE_BF16 = 0, 1
+
+
+class VlbError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"vlb status {status}: {message}")
+        self.status = status
+        self.message = message
+
+
+class KernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
+
+
+class BakeParams(C.Structure):
+    _fields_ = [
+        ("lmax", C.c_uint32), ("precision", C.c_uint32), ("flags", C.c_uint32),
+        ("sun_dir", C.c_float * 3), ("sun_intensity", C.c_float),
+        ("tmin", C.c_float), ("tmax", C.c_float), ("shadow_bias", C.c_float),
+        ("dirs", C.c_void_p), ("sky", C.c_void_p),
+    ]
+
+
+class BakeDebug(C.Structure):
+    _fields_ = [("hit_tri", C.c_void_p), ("shadow", C.c_void_p), ("radiance", C.c_void_p)]
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"libvlb.so not found at {LIB_PATH}; run __graft_entry__.build() first")
+    lib = C.CDLL(str(LIB_PATH))
+    P, U32, I32, U64, F32 = C.c_void_p, C.c_uint32, C.c_int, C.c_uint64, C.c_float
+    sig = {
+        "vlb_version": (U32, []),
+        "vlb_status_string": (C.c_char_p, [I32]),
+        "vlb_ctx_create": (I32, [I32, C.POINTER(P)]),
+        "vlb_ctx_destroy": (None, [P]),
+        "vlb_ctx_set_stream": (I32, [P, P]),
+        "vlb_ctx_get_stream": (P, [P]),
+        "vlb_ctx_synchronize": (I32, [P]),
+        "vlb_last_error": (C.c_char_p, [P]),
+        "vlb_ctx_set_profiling": (I32, [P, I32]),
+        "vlb_ctx_profile_read": (I32, [P, P, U32, C.POINTER(U32)]),
+        "vlb_ctx_profile_reset": (I32, [P]),
+        "vlb_ctx_launch_count": (U64, [P]),
+        "vlb_probe_grid_ref_order": (I32, [P, P, P, P]),
+        "vlb_scene_create": (I32, [P, P, U32, U32, P, U32, P, C.POINTER(P)]),
+        "vlb_scene_destroy": (None, [P]),
+        "vlb_scene_triangle_count": (U32, [P]),
+        "vlb_scene_bounds": (I32, [P, I32, P]),
+        "vlb_scene_bvh_export": (I32, [P, P, P, P, P]),
+        "vlb_scene_device_bytes": (U64, [P]),
+        "vlb_dirset_create_fibonacci": (I32, [P, U32, I32, C.POINTER(P)]),
+        "vlb_dirset_create_equirect": (I32, [P, U32, U32, C.POINTER(P)]),
+        "vlb_dirset_create": (I32, [P, P, P, P, U32, C.POINTER(P)]),
+        "vlb_dirset_destroy": (None, [P]),
+        "vlb_dirset_count": (U32, [P]),
+        "vlb_dirset_export": (I32, [P, P, P]),
+        "vlb_skybox_sh": (I32, [P, P, I32, I32, U32, U32, U32, U32, P]),
+        "vlb_skybox_sh_batched": (I32, [P, P, I32, I32, U32, U32, U32, U32, U32, P]),
+        "vlb_sky_create": (I32, [P, P, U32, C.POINTER(P)]),
+        "vlb_sky_destroy": (None, [P]),
+        "vlb_bake_params_default": (None, [P]),
+        "vlb_bake": (I32, [P, P, P, U32, P, P]),
+        "vlb_bake_ex": (I32, [P, P, P, U32, P, P, P]),
+        "vlb_bake_trace_stats": (I32, [P, P, P, U32, P, P]),
+        "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
+        "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
+        "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
+        "vlb_synth_cubemap": (I32, [U64, U32, P]),
+        "vlb_synth_sun": (I32, [U64, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (contiguous), or None."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr()
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def k_of(lmax: int) -> int:
+    return (lmax + 1) * (lmax + 1)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib.vlb_ctx_create(device, C.byref(h))
+        if st != OK:
+            raise VlbError(st, f"vlb_ctx_create(device={device}) failed: {lib.vlb_status_string(st).decode()}")
+        self.h = h
+
+    def check(self, st: int) -> None:
+        if st != OK:
+            raise VlbError(st, lib.vlb_last_error(self.h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib.vlb_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # stream / timing
+    def set_stream(self, stream_handle: int | None) -> None:
+        self.check(lib.vlb_ctx_set_stream(self.h, stream_handle))
+
+    @property
+    def stream(self) -> int:
+        return lib.vlb_ctx_get_stream(self.h) or 0
+
+    def synchronize(self) -> None:
+        self.check(lib.vlb_ctx_synchronize(self.h))
+
+    def set_profiling(self, on: bool) -> None:
+        self.check(lib.vlb_ctx_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self) -> dict:
+        buf = (KernelTime * 64)()
+        n = C.c_uint32()
+        self.check(lib.vlb_ctx_profile_read(self.h, buf, 64, C.byref(n)))
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(n.value)}
+
+    def profile_reset(self) -> None:
+        self.check(lib.vlb_ctx_profile_reset(self.h))
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib.vlb_ctx_launch_count(self.h))
+
+    # objects
+    def scene(self, positions, indices, albedo=None, stride_bytes: int = 12) -> "Scene":
+        return Scene(self, positions, indices, albedo, stride_bytes)
+
+    def fibonacci(self, n: int, frame: int = FRAME_WORLD) -> "DirSet":
+        h = C.c_void_p()
+        self.check(lib.vlb_dirset_create_fibonacci(self.h, n, frame, C.byref(h)))
+        return DirSet(self, h)
+
+    def equirect(self, w: int, h: int) -> "DirSet":
+        hh = C.c_void_p()
+        self.check(lib.vlb_dirset_create_equirect(self.h, w, h, C.byref(hh)))
+        return DirSet(self, hh)
+
+    def dirset(self, trace_dirs, weights, basis_dirs=None) -> "DirSet":
+        td = _f32(trace_dirs).reshape(-1, 3)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        bd = None if basis_dirs is None else _f32(basis_dirs).reshape(-1, 3)
+        h = C.c_void_p()
+        self.check(lib.vlb_dirset_create(self.h, _ptr(td), _ptr(bd), _ptr(w), td.shape[0], C.byref(h)))
+        return DirSet(self, h)
+
+    def sky(self, cubemap, n: int) -> "Sky":
+        cm = cubemap if hasattr(cubemap, "data_ptr") else _f32(cubemap)
+        h = C.c_void_p()
+        self.check(lib.vlb_sky_create(self.h, _ptr(cm), n, C.byref(h)))
+        return Sky(self, h, n)
+
+    # entry points
+    def skybox_sh(self, texels, layout: int, w: int, h: int, lmax: int = 3, fmt: int = TEXEL_RGB32F,
+                  flags: int = 0, count: int = 1, out=None):
+        K = k_of(lmax)
+        ret = out if out is not None else np.empty((count, K, 3), np.float32)
+        self.check(lib.vlb_skybox_sh_batched(self.h, _ptr(texels), fmt, layout, w, h, count, lmax, flags, _ptr(ret)))
+        if out is None and count == 1:
+            return ret[0]
+        return ret
+
+    def bake(self, scene: "Scene", probes, params: BakeParams, out=None, debug: bool = False):
+        n = int(probes.shape[0]) if hasattr(probes, "shape") else len(probes) // 3
+        K = k_of(params.lmax)
+        if not hasattr(probes, "data_ptr"):
+            probes = _f32(probes).reshape(-1, 3)
+        ret = out if out is not None else np.empty((n, K, 3), np.float32)
+        if not debug:
+            self.check(lib.vlb_bake(self.h, scene.h, _ptr(probes), n, C.byref(params), _ptr(ret)))
+            return ret
+        S = params_dirs_count(params)
+        hit = np.empty(n * S, np.int32)
+        vis = np.empty(n * S, np.uint8)
+        rad = np.empty(n * S * 3, np.float32) if params.precision != PREC_FUSED else None
+        dbg = BakeDebug(_ptr(hit), _ptr(vis), _ptr(rad))
+        self.check(lib.vlb_bake_ex(self.h, scene.h, _ptr(probes), n, C.byref(params), _ptr(ret), C.byref(dbg)))
+        return ret, hit.reshape(n, S), vis.reshape(n, S), (None if rad is None else rad.reshape(n, S, 3))
+
+    def project(self, radiance, nprobes: int, dirs: "DirSet", lmax: int, dtype: int = DTYPE_F32, out=None):
+        K = k_of(lmax)
+        ret = out if out is not None else np.empty((nprobes, K, 3), np.float32)
+        self.check(lib.vlb_project(self.h, _ptr(radiance), dtype, nprobes, dirs.h, lmax, _ptr(ret)))
+        return ret
+
+    def sh_eval_envmap(self, coeffs, lmax: int, w: int, h: int, scale: float = 1250.0):
+        c = _f32(coeffs).reshape(-1)
+        out = np.empty((h, w, 3), np.float32)
+        self.check(lib.vlb_sh_eval_envmap(self.h, _ptr(c), lmax, w, h, scale, _ptr(out)))
+        return out
+
+
+def params_dirs_count(p: BakeParams) -> int:
+    return int(lib.vlb_dirset_count(p.dirs))
+
+
+def trace_stats(ctx: Context, scene: "Scene", probes, params: BakeParams) -> dict:
+    """Rays, shadow rays, BVH nodes fetched and triangles tested for one bake."""
+    pr = probes if hasattr(probes, "data_ptr") else _f32(probes).reshape(-1, 3)
+    n = int(pr.shape[0])
+    out = np.zeros(4, np.uint64)
+    ctx.check(lib.vlb_bake_trace_stats(ctx.h, scene.h, _ptr(pr), n, C.byref(params), _ptr(out)))
+    return {"rays": int(out[0]), "shadow_rays": int(out[1]), "nodes": int(out[2]), "tris": int(out[3])}
+
+
+class Scene:
+    def __init__(self, ctx: Context, positions, indices, albedo, stride_bytes: int):
+        self.ctx = ctx
+        pos = positions if hasattr(positions, "data_ptr") else _f32(positions)
+        idx = indices if hasattr(indices, "data_ptr") else np.ascontiguousarray(indices, dtype=np.uint32)
+        alb = None if albedo is None else (albedo if hasattr(albedo, "data_ptr") else _f32(albedo))
+        nverts = (pos.numel() if hasattr(pos, "numel") else pos.size) * 4 // stride_bytes
+        ntris = (idx.numel() if hasattr(idx, "numel") else idx.size) // 3
+        h = C.c_void_p()
+        ctx.check(lib.vlb_scene_create(ctx.h, _ptr(pos), stride_bytes, nverts, _ptr(idx), ntris, _ptr(alb),
+                                       C.byref(h)))
+        self.h = h
+        self.ntris = ntris
+
+    def bounds(self, include_origin: bool = True) -> np.ndarray:
+        b = np.empty(6, np.float32)
+        self.ctx.check(lib.vlb_scene_bounds(self.h, 1 if include_origin else 0, _ptr(b)))
+        return b
+
+    def bvh_export(self) -> dict:
+        n = self.ntris
+        codes = np.empty(n, np.uint32)
+        order = np.empty(n, np.uint32)
+        child = np.empty(max(0, 2 * (n - 1)), np.int32)
+        box = np.empty(max(0, (2 * n - 1) * 6), np.float32)
+        self.ctx.check(lib.vlb_scene_bvh_export(self.h, _ptr(codes), _ptr(order), _ptr(child) if child.size else None,
+                                                _ptr(box) if box.size else None))
+        return {"codes": codes, "order": order, "child": child, "box": box.reshape(-1, 6)}
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib.vlb_scene_device_bytes(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib.vlb_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DirSet:
+    def __init__(self, ctx: Context, h):
+        self.ctx = ctx
+        self.h = h
+        self.n = int(lib.vlb_dirset_count(h))
+
+    def export(self):
+        d = np.empty((self.n, 3), np.float32)
+        b = np.empty((self.n, 16), np.float32)
+        self.ctx.check(lib.vlb_dirset_export(self.h, _ptr(d), _ptr(b)))
+        return d, b
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib.vlb_dirset_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Sky:
+    def __init__(self, ctx: Context, h, n: int):
+        self.ctx = ctx
+        self.h = h
+        self.n = n
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib.vlb_sky_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bake_params(dirs: DirSet, lmax: int = 2, precision: int = PREC_FP32, sun=(0.0, 1.0, 0.0),
+                sun_intensity: float = 5.0, sky: Sky | None = None) -> BakeParams:
+    p = BakeParams()
+    lib.vlb_bake_params_default(C.byref(p))
+    p.lmax = lmax
+    p.precision = precision
+    for i in range(3):
+        p.sun_dir[i] = float(sun[i])
+    p.sun_intensity = sun_intensity
+    p.dirs = dirs.h
+    p.sky = sky.h if sky is not None else None
+    return p
+
+
+# ---- host-only helpers (no GPU needed) ------------------------------------------------
+def probe_grid_ref_order(bounds, counts):
+    b = _f32(bounds)
+    c = np.ascontiguousarray(counts, dtype=np.uint32)
+    n = int(np.prod(c))
+    out = np.empty((n, 3), np.float32)
+    step = np.empty(3, np.float32)
+    st = lib.vlb_probe_grid_ref_order(_ptr(b), _ptr(c), _ptr(out), _ptr(step))
+    if st != OK:
+        raise VlbError(st, "vlb_probe_grid_ref_order")
+    return out, step
+
+
+def synth_box_scene(seed: int, nboxes: int):
+    nv, nt = C.c_uint32(), C.c_uint32()
+    lib.vlb_synth_box_scene(seed, nboxes, None, None, None, C.byref(nv), C.byref(nt))
+    pos = np.empty((nv.value, 3), np.float32)
+    idx = np.empty((nt.value, 3), np.uint32)
+    alb = np.empty((nt.value, 3), np.float32)
+    st = lib.vlb_synth_box_scene(seed, nboxes, _ptr(pos), _ptr(idx), _ptr(alb), C.byref(nv), C.byref(nt))
+    if st != OK:
+        raise VlbError(st, "vlb_synth_box_scene")
+    return pos, idx, alb
+
+
+def synth_cubemap(seed: int, n: int) -> np.ndarray:
+    out = np.empty((6, n, n, 3), np.float32)
+    st = lib.vlb_synth_cubemap(seed, n, _ptr(out))
+    if st != OK:
+        raise VlbError(st, "vlb_synth_cubemap")
+    return out
+
+
+def synth_sun(seed: int) -> np.ndarray:
+    out = np.empty(3, np.float32)
+    st = lib.vlb_synth_sun(seed, _ptr(out))
+    if st != OK:
+        raise VlbError(st, "vlb_synth_sun")
+    return out
