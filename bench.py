@@ -251,8 +251,8 @@ def main():
     timed(chosen, min(args.steps, 20), profile=True)
     prof = ctx.profile()
     # per-ray work counts for the algorithmic bytes (one debug bake, untimed)
-    _, hit, vis, _ = ctx.bake(scene, probes, params["fp32"], debug=True)
-    shadow_rays = int((vis != 2).sum())
+    stats = ctx_trace_stats(ctx, scene, probes, params["fp32"])
+    shadow_rays = stats["shadow_rays"]
 
     def agg(ms):
         t = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
@@ -283,12 +283,10 @@ def main():
         return 0
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    # roofline of the dominant kernel: algorithmic bytes = per-ray node + triangle fetches
+    # roofline of the dominant kernel: algorithmic bytes = node + triangle fetches per launch
     kname = "trace_fused"
     klaunch, kms = prof.get(kname, (0, 0.0))
     k_avg_ms = kms / max(klaunch, 1)
-    rays_primary = P * NDIRS
-    stats = ctx_trace_stats(ctx, scene, probes, params["fp32"])
     bytes_per_launch = stats["bytes"]
     achieved = bytes_per_launch / (k_avg_ms * 1e-3) / 1e9 if k_avg_ms > 0 else None
     traffic = load_traffic(kname)
@@ -312,14 +310,20 @@ def main():
         "grays_per_s": value * NDIRS / 1e9, "grays_incl_shadow_per_s": value * (NDIRS + shadow_rays / P) / 1e9,
         "latency_ms": {"p50": p50, "p99": p99},
         "plain_fp32": {"value": plain, "unit": "probes/s", "p99_ms": sorted(ms_plain)[-1]},
-        "sh_rel_err_vs_fp64": {"max": float(err.max()), "mean": float(err.mean()), "probes": len(sample)},
+        "sh_rel_err_vs_fp64": {"max": float(err.max()), "mean": float(err.mean()),
+                               "p99": float(np.quantile(err, 0.99)),
+                               "frac_within_1e-4": float((err < 1e-4).mean()), "probes": len(sample),
+                               "note": "probes above 1e-4 own a ray within 1e-6 of a triangle edge or of tmin "
+                                       "(FP32 decision); with those decisions replayed in FP64 every probe is "
+                                       "within 1e-4 (tests/test_gpu_bake.py)"},
         "e2e": {"value": e2e_value, "unit": "probes/s", "h2d_bytes_per_step": int(P * 12),
                 "d2h_bytes_per_step": int(P * K * 12)},
         "gpu_launches": int(launches),
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
                      "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": k_avg_ms,
-                     "nodes_per_ray": stats["nodes_per_ray"], "tris_per_ray": stats["tris_per_ray"],
+                     "node_tests_per_ray": stats["node_tests_per_ray"],
+                     "node_fetches_x32_per_ray": stats["node_fetches_per_packet_ray"],
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
         "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)} for k, v in prof.items()},
         "cpu_baseline": {"value": len(sample) / cpu_dt, "unit": "probes/s", "cores": os.cpu_count() or 1,
@@ -333,13 +337,16 @@ def main():
 
 
 def ctx_trace_stats(ctx, scene, probes, params):
-    """Nodes visited and triangles tested per ray (instrumented bake)."""
+    """Per-launch traversal work of the instrumented bake: node and triangle
+    fetches are counted once per 32-ray packet visit (the bytes the kernel
+    requests), node tests once per ray."""
     import vlb
 
     st = vlb.trace_stats(ctx, scene, probes, params)
-    rays = st["rays"]
-    return {"bytes": st["nodes"] * 64 + st["tris"] * 48, "nodes_per_ray": st["nodes"] / rays,
-            "tris_per_ray": st["tris"] / rays}
+    rays = st["rays"] + st["shadow_rays"]
+    return {"bytes": st["node_fetches"] * 64 + st["tri_fetches"] * 48,
+            "node_fetches_per_packet_ray": st["node_fetches"] * 32 / rays,
+            "node_tests_per_ray": st["node_tests"] / rays, "shadow_rays": st["shadow_rays"]}
 
 
 if __name__ == "__main__":

@@ -202,10 +202,12 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
                        const vlb_bake_params* params, float* out, const vlb_bake_debug* debug);
 /* Measurement aid (no reference counterpart; the reference's traversal is
  * inside the driver): one instrumented bake of the same rays, counting
- * out[0] primary rays, out[1] shadow rays, out[2] BVH nodes fetched (64 B
- * each), out[3] triangles tested (48 B each).  Host output. */
+ * out[0] primary rays, out[1] shadow rays, out[2] BVH node fetches (64 B
+ * each, one per 32-ray packet visit), out[3] triangle fetches (48 B each,
+ * per packet), out[4] node tests summed over rays, out[5] reserved (0).
+ * Host output. */
 vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
-                                const vlb_bake_params* params, uint64_t out[4]);
+                                const vlb_bake_params* params, uint64_t out[6]);
 
 /* ---- projection and reconstruction ----------------------------------------
  * Replaces dispatchBakingKernel / shaders/sh.comp:23-42 for a radiance tile

@@ -190,6 +190,69 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t* __res
   }
 }
 
+// `passes` stable 8-bit passes from bit 0; the sorted pairs end in (kin, vin)
+// (the pointers are swapped in place).  Returns the number of kernels.
+static int radix_passes(uint32_t*& kin, uint32_t*& vin, uint32_t*& kout, uint32_t*& vout, uint32_t n,
+                        uint32_t* hist, int passes, cudaStream_t st) {
+  const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
+  int L = 0;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int shift = 8 * pass;
+    k_rs_hist<<<nblk, kRsThreads, 0, st>>>(kin, n, shift, hist, nblk); ++L;
+    k_scan_exclusive<<<1, 1024, 0, st>>>(hist, nblk * 256); ++L;
+    k_rs_scatter<<<nblk, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, hist, nblk); ++L;
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  return L;
+}
+
+// ---- probe ordering ------------------------------------------------------------------
+// 24-bit Morton code of each probe position quantised inside the scene box;
+// sorting by it groups spatially close probes into the same warp.
+__global__ void k_probe_codes(const float* __restrict__ probes, uint32_t n, float lox, float loy, float loz,
+                              float sx, float sy, float sz, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  auto q = [](float c, float lo, float s) -> uint32_t {
+    const float v = (c - lo) * s;
+    if (!(v > 0.f)) return 0u;
+    return min(__float2uint_rz(v), 255u);
+  };
+  const uint32_t x = q(probes[3 * size_t(i)], lox, sx), y = q(probes[3 * size_t(i) + 1], loy, sy),
+                 z = q(probes[3 * size_t(i) + 2], loz, sz);
+  keys[i] = (expand_bits10(x) << 2) | (expand_bits10(y) << 1) | expand_bits10(z);
+  vals[i] = i;
+}
+
+size_t probe_order_scratch_bytes(uint32_t n) {
+  const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
+  return (size_t(n) * 4 + 255) / 256 * 256 * 3 + size_t(nblk) * 256 * 4;
+}
+
+int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
+                       cudaStream_t st) {
+  if (n == 0) return 0;
+  const size_t a = (size_t(n) * 4 + 255) / 256 * 256;
+  char* base = static_cast<char*>(scratch);
+  uint32_t* ka = reinterpret_cast<uint32_t*>(base);
+  uint32_t* kb = reinterpret_cast<uint32_t*>(base + a);
+  uint32_t* vb = reinterpret_cast<uint32_t*>(base + 2 * a);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(base + 3 * a);
+  float s[3];
+  for (int i = 0; i < 3; ++i) {
+    const float e = bounds[3 + i] - bounds[i];
+    s[i] = e > 0.f ? 256.0f / e : 0.f;
+  }
+  k_probe_codes<<<(n + 255) / 256, 256, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka,
+                                                 order);
+  uint32_t *kin = ka, *vin = order, *kout = kb, *vout = vb;
+  // 24-bit keys: 3 passes; the odd pass count leaves the result in vb, copy it back
+  int L = 1 + radix_passes(kin, vin, kout, vout, n, hist, 3, st);
+  if (vin != order) cudaMemcpyAsync(order, vin, size_t(n) * 4, cudaMemcpyDeviceToDevice, st);
+  return L;
+}
+
 // ---- Karras split search ---------------------------------------------------------
 __device__ __forceinline__ int kdelta(const uint32_t* __restrict__ k, int n, int i, int j) {
   if (j < 0 || j >= n) return -1;
@@ -337,14 +400,7 @@ void launch_lbvh_build(const LbvhBuild& b, cudaStream_t st, int* launches) {
   k_morton<<<g, 256, 0, st>>>(s.cen, n, s.params, s.ka, s.va); ++L;
   const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
   uint32_t *kin = s.ka, *kout = s.kb, *vin = s.va, *vout = s.vb;
-  for (int pass = 0; pass < 4; ++pass) {
-    const int shift = 8 * pass;
-    k_rs_hist<<<nblk, kRsThreads, 0, st>>>(kin, n, shift, s.hist, nblk); ++L;
-    k_scan_exclusive<<<1, 1024, 0, st>>>(s.hist, nblk * 256); ++L;
-    k_rs_scatter<<<nblk, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, s.hist, nblk); ++L;
-    std::swap(kin, kout);
-    std::swap(vin, vout);
-  }
+  L += radix_passes(kin, vin, kout, vout, n, s.hist, 4, st);
   cudaMemcpyAsync(b.codes, kin, size_t(n) * 4, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(b.order, vin, size_t(n) * 4, cudaMemcpyDeviceToDevice, st);
   k_leaf_boxes<<<g, 256, 0, st>>>(b.order, s.tb, n, b.box); ++L;

@@ -739,43 +739,60 @@ void vlb_bake_params_default(vlb_bake_params* p) {
   p->shadow_bias = 0.005f;
 }
 
-static uint32_t pick_dirs_per_warp(const vlb_ctx* ctx, uint32_t nprobes, uint32_t S) {
-  const uint64_t groups = (nprobes + 31) / 32;
-  const uint64_t target = uint64_t(ctx->num_sms) * 32;  // warps in flight
-  uint64_t nsc = (target + groups - 1) / groups;
-  nsc = std::max<uint64_t>(1, std::min<uint64_t>(nsc, S));
-  return uint32_t((S + nsc - 1) / nsc);
+// Common part of a bake launch: validated parameters -> trace arguments,
+// probes staged on the device and sorted into spatially compact packets.
+static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                                const vlb_bake_params* p, vlbk::TraceArgs* out) {
+  if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
+  if (scene->ctx != ctx || p->dirs->ctx != ctx || (p->sky && p->sky->ctx != ctx))
+    return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
+  if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
+  if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
+  if (!probe_xyz) return fail(ctx, VLB_ERR_INVALID, "null probes");
+  const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
+                              double(p->sun_dir[2]) * p->sun_dir[2]);
+  if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
+  if (!(p->tmax > p->tmin) || p->tmin < 0.f) return fail(ctx, VLB_ERR_INVALID, "bad ray interval");
+  vlb_status st;
+  const void* dprobes;
+  if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
+  void *order, *oscr;
+  if ((st = scratch(ctx, "probe_order", size_t(nprobes) * 4, &order)) ||
+      (st = scratch(ctx, "probe_order_tmp", vlbk::probe_order_scratch_bytes(nprobes), &oscr)))
+    return st;
+  {
+    float b[6];
+    for (int a = 0; a < 6; ++a) b[a] = scene->bounds[a];
+    KScope k(ctx, "probe_order", 0);
+    k.nkernels = vlbk::launch_probe_order(static_cast<const float*>(dprobes), nprobes, b,
+                                          static_cast<uint32_t*>(order), oscr, ctx->stream);
+  }
+  vlbk::TraceArgs& a = *out;
+  a = vlbk::TraceArgs{};
+  a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
+  a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
+  a.order = static_cast<const uint32_t*>(order);
+  a.dirs = p->dirs->d_dirs; a.S = p->dirs->n;
+  a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
+  a.sun_scale = float(double(p->sun_intensity) / kPi);
+  a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
+  a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
+  a.basis16 = p->dirs->d_basis16; a.K = k_of(p->lmax); a.err = ctx->d_err;
+  vlbk::plan_trace(a, ctx->num_sms);
+  return VLB_OK;
 }
 
 vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
                        const vlb_bake_params* p, float* out, const vlb_bake_debug* dbg) {
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
-  if (scene->ctx != ctx || p->dirs->ctx != ctx || (p->sky && p->sky->ctx != ctx))
-    return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
-  if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
-  if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
   if (nprobes == 0) return VLB_OK;
-  if (!probe_xyz || !out) return fail(ctx, VLB_ERR_INVALID, "null probes or output");
-  const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
-                              double(p->sun_dir[2]) * p->sun_dir[2]);
-  if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
-  if (!(p->tmax > p->tmin) || p->tmin < 0.f) return fail(ctx, VLB_ERR_INVALID, "bad ray interval");
-  const uint32_t S = p->dirs->n, K = k_of(p->lmax), V = 3 * K;
+  if (!out) return fail(ctx, VLB_ERR_INVALID, "null output");
+  vlbk::TraceArgs a;
+  vlb_status st = prepare_trace(ctx, scene, probe_xyz, nprobes, p, &a);
+  if (st) return st;
+  const uint32_t S = a.S, K = a.K, V = 3 * K;
   const uint64_t rays = uint64_t(nprobes) * S;
-  vlb_status st;
-  const void* dprobes;
-  if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
-  vlbk::TraceArgs a{};
-  a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
-  a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
-  a.dirs = p->dirs->d_dirs; a.S = S;
-  a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
-  a.sun_scale = float(double(p->sun_intensity) / kPi);
-  a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
-  a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
-  a.basis16 = p->dirs->d_basis16; a.K = K; a.err = ctx->d_err;
   OutBuf ob, oh, os, orad;
   if ((st = stage_out(ctx, out, size_t(nprobes) * V * 4, "bake_out", &ob))) return st;
   if (dbg) {
@@ -787,22 +804,21 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     a.shadow = static_cast<uint8_t*>(os.dev);
     a.dbg_radiance = static_cast<float*>(orad.dev);
   }
-  a.dirs_per_warp = pick_dirs_per_warp(ctx, nprobes, S);
   if (p->precision == VLB_PREC_FUSED) {
-    const uint32_t nsc = (S + a.dirs_per_warp - 1) / a.dirs_per_warp;
-    void* part;
-    if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * nsc * V * 4, &part))) return st;
-    a.partial = static_cast<float*>(part);
     if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "per-ray radiance is not kept by the fused path");
-    uint32_t chunks = 0;
-    {
-      KScope k(ctx, "trace_fused");
-      vlbk::launch_trace_fused(a, ctx->stream, &chunks);
+    a.out = static_cast<float*>(ob.dev);
+    if (a.block_chunks > 1) {
+      void *part, *done;
+      const size_t groups = (size_t(nprobes) + 31) / 32;
+      if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * a.block_chunks * V * 4, &part)) ||
+          (st = scratch(ctx, "bake_group_done", groups * 4, &done)))
+        return st;
+      VLB_CUDA(ctx, cudaMemsetAsync(done, 0, groups * 4, ctx->stream));
+      a.partial = static_cast<float*>(part);
+      a.group_done = static_cast<uint32_t*>(done);
     }
-    {
-      KScope k(ctx, "sh_finalize");
-      vlbk::launch_sh_finalize(a.partial, nprobes, chunks, V, static_cast<float*>(ob.dev), ctx->stream);
-    }
+    KScope k(ctx, "trace_fused");
+    vlbk::launch_trace_fused(a, ctx->stream);
   } else {
     const bool bf16 = p->precision == VLB_PREC_MIXED;
     void* tile;
@@ -834,46 +850,33 @@ vlb_status vlb_bake(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz
 }
 
 vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
-                                const vlb_bake_params* p, uint64_t out[4]) {
+                                const vlb_bake_params* p, uint64_t out[6]) {
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  if (!scene || !p || !p->dirs || !out) return fail(ctx, VLB_ERR_INVALID, "scene, params, dirs and out are required");
-  if (scene->ctx != ctx || p->dirs->ctx != ctx) return fail(ctx, VLB_ERR_INVALID, "handles of another context");
-  if (nprobes == 0 || !probe_xyz) return fail(ctx, VLB_ERR_INVALID, "no probes");
-  const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
-                              double(p->sun_dir[2]) * p->sun_dir[2]);
-  if (!(sl > 0.0)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
-  const uint32_t S = p->dirs->n;
-  vlb_status st;
-  const void* dprobes;
-  if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
+  if (!out || nprobes == 0) return fail(ctx, VLB_ERR_INVALID, "no probes or no output");
+  vlbk::TraceArgs a;
+  vlb_status st = prepare_trace(ctx, scene, probe_xyz, nprobes, p, &a);
+  if (st) return st;
   void *tile, *cnt;
-  if ((st = scratch(ctx, "bake_tile", size_t(nprobes) * S * 12, &tile)) || (st = scratch(ctx, "trace_counters", 64, &cnt)))
+  if ((st = scratch(ctx, "bake_tile", size_t(nprobes) * a.S * 12, &tile)) ||
+      (st = scratch(ctx, "trace_counters", 64, &cnt)))
     return st;
   VLB_CUDA(ctx, cudaMemsetAsync(cnt, 0, 64, ctx->stream));
-  vlbk::TraceArgs a{};
-  a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
-  a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
-  a.dirs = p->dirs->d_dirs; a.S = S;
-  a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
-  a.sun_scale = float(double(p->sun_intensity) / kPi);
-  a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
-  a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
   a.radiance = static_cast<float*>(tile);
   a.counters = static_cast<unsigned long long*>(cnt);
-  a.err = ctx->d_err;
-  a.dirs_per_warp = pick_dirs_per_warp(ctx, nprobes, S);
   {
     KScope k(ctx, "trace_tile_counted");
     vlbk::launch_trace_tile(a, ctx->stream);
   }
   if ((st = finish(ctx, true))) return st;
-  unsigned long long h[3];
+  unsigned long long h[4];
   VLB_CUDA(ctx, cudaMemcpy(h, cnt, sizeof h, cudaMemcpyDeviceToHost));
-  out[0] = uint64_t(nprobes) * S;
+  out[0] = uint64_t(nprobes) * a.S;
   out[1] = h[2];
   out[2] = h[0];
   out[3] = h[1];
+  out[4] = h[3];
+  out[5] = 0;
   return VLB_OK;
 }
 

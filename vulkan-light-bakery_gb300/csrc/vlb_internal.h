@@ -80,6 +80,12 @@ struct LbvhBuild {
 };
 size_t lbvh_scratch_bytes(uint32_t ntris);
 void launch_lbvh_build(const LbvhBuild& b, cudaStream_t s, int* launches);
+// Permutation of the probes by 24-bit Morton code inside `bounds` (min xyz,
+// max xyz), so that each 32-probe packet is spatially compact.  Returns the
+// number of kernels launched.
+size_t probe_order_scratch_bytes(uint32_t n);
+int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
+                       cudaStream_t s);
 
 // ---- trace + shade --------------------------------------------------------------
 struct TraceArgs {
@@ -88,6 +94,7 @@ struct TraceArgs {
   const float4* albedo;
   uint32_t ntris;
   const float* probes;    // device nprobes*3
+  const uint32_t* order;  // device permutation: packet slot -> probe index
   uint32_t nprobes;
   const float4* dirs;     // device S (xyz)
   uint32_t S;
@@ -105,13 +112,21 @@ struct TraceArgs {
   // fused projection
   const float* basis16;   // S x 16 fp32 weighted basis
   uint32_t K;
-  float* partial;         // [chunks][nprobes][K*3]
+  float* partial;         // [nprobes][block chunks][K*3]
+  uint32_t* group_done;   // [probe groups] completion counters (zero before the launch)
+  float* out;             // [nprobes][K][3]
+  // decomposition: a warp owns one 32-probe packet and dirs_per_warp
+  // consecutive directions; a CTA owns kTraceWarps consecutive chunks of one packet
   uint32_t dirs_per_warp;
-  unsigned long long* counters;  // null, or [nodes fetched, triangles tested, shadow rays]
+  uint32_t block_chunks;  // CTAs per packet
+  unsigned long long* counters;  // null, or [warp node fetches, warp triangle fetches, shadow rays, lane node tests]
   int* err;
 };
+constexpr int kTraceWarps = 4;
+// Chooses dirs_per_warp / block_chunks for nprobes x S rays on num_sms SMs.
+void plan_trace(TraceArgs& a, int num_sms);
 void launch_trace_tile(const TraceArgs& a, cudaStream_t s);
-void launch_trace_fused(const TraceArgs& a, cudaStream_t s, uint32_t* chunks_out);
+void launch_trace_fused(const TraceArgs& a, cudaStream_t s);
 
 }  // namespace vlbk
 

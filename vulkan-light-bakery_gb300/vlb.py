@@ -260,9 +260,10 @@ def trace_stats(ctx: Context, scene: "Scene", probes, params: BakeParams) -> dic
     """Rays, shadow rays, BVH nodes fetched and triangles tested for one bake."""
     pr = probes if hasattr(probes, "data_ptr") else _f32(probes).reshape(-1, 3)
     n = int(pr.shape[0])
-    out = np.zeros(4, np.uint64)
+    out = np.zeros(6, np.uint64)
     ctx.check(lib.vlb_bake_trace_stats(ctx.h, scene.h, _ptr(pr), n, C.byref(params), _ptr(out)))
-    return {"rays": int(out[0]), "shadow_rays": int(out[1]), "nodes": int(out[2]), "tris": int(out[3])}
+    return {"rays": int(out[0]), "shadow_rays": int(out[1]), "node_fetches": int(out[2]),
+            "tri_fetches": int(out[3]), "node_tests": int(out[4])}
 
 
 class Scene:
@@ -363,6 +364,8 @@ def bake_params(dirs: DirSet, lmax: int = 2, precision: int = PREC_FP32, sun=(0.
     p.sun_intensity = sun_intensity
     p.dirs = dirs.h
     p.sky = sky.h if sky is not None else None
+    # the struct carries raw handles: keep their owners alive as long as it lives
+    p._owners = (dirs, sky)
     return p
 
 
