@@ -153,6 +153,22 @@ vlb_status vlb_skybox_sh(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt,
 vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_format fmt, vlb_sky_layout layout,
                                  uint32_t w, uint32_t h, uint32_t count, uint32_t lmax, uint32_t flags, float* out);
 
+/* No counterpart in the reference.  The same projection as vlb_skybox_sh
+ * for callers that cannot allocate device memory when they call it (a
+ * renderer whose device memory is all handed to its own pool, a host that
+ * allows cudaMalloc only at start-up).  It takes no context and allocates
+ * nothing: its scratch is a 557,312-byte __device__ array inside the
+ * library, held by every GPU that loads the library until the process exits.
+ * One map per call; lmax 2 or 3; cubemap faces up to 256, panoramas up to
+ * 8192 x 8192; texels and out must be device memory of the current device
+ * (host pointers and larger sizes return VLB_ERR_INVALID).  stream: a
+ * cudaStream_t or NULL; the call returns when the result is in out.  The
+ * first call on a device looks up the array's device address, so make it
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race and must be serialised by the caller. */
+vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format fmt, vlb_sky_layout layout, uint32_t w,
+                                 uint32_t h, uint32_t lmax, uint32_t flags, float* out, void* stream);
+
 /* Resident cubemap sky used on ray misses during a bake (the reference's
  * miss shader shaders/main.rmiss:37-41 reads an unbound set; this defines
  * it): nearest-texel lookup of a 6 x n x n RGB FP32 cubemap. */

@@ -83,6 +83,7 @@ def _load() -> C.CDLL:
         "vlb_dirset_export": (I32, [P, P, P]),
         "vlb_skybox_sh": (I32, [P, P, I32, I32, U32, U32, U32, U32, P]),
         "vlb_skybox_sh_batched": (I32, [P, P, I32, I32, U32, U32, U32, U32, U32, P]),
+        "vlb_skybox_sh_noalloc": (I32, [P, I32, I32, U32, U32, U32, U32, P, P]),
         "vlb_sky_create": (I32, [P, P, U32, C.POINTER(P)]),
         "vlb_sky_destroy": (None, [P]),
         "vlb_bake_params_default": (None, [P]),
