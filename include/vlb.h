@@ -186,14 +186,17 @@ void vlb_sky_destroy(vlb_sky* sky);
  * its accumulator between probes; that carry-over is not reproduced). */
 typedef enum vlb_precision {
   VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 projection */
-  VLB_PREC_FUSED = 1, /* trace + projection in one kernel, FP32 */
-  VLB_PREC_MIXED = 2  /* BF16 radiance tile, tcgen05 projection with split BF16 basis */
+  VLB_PREC_FUSED = 1, /* FP32, fastest schedule: trace + projection in one kernel when the probe count
+                         is large enough to fill the GPU one packet per warp, else the tile schedule */
+  VLB_PREC_MIXED = 2  /* BF16 radiance tile, BF16 projection */
 } vlb_precision;
+/* vlb_bake_params.flags: with VLB_PREC_FUSED, always run the one-kernel schedule. */
+#define VLB_BAKE_FORCE_FUSED_KERNEL 1u
 
 typedef struct vlb_bake_params {
   uint32_t lmax;          /* 2: 9 coefficients, 3: 16 (the reference) */
   uint32_t precision;     /* vlb_precision */
-  uint32_t flags;         /* reserved, 0 */
+  uint32_t flags;         /* VLB_BAKE_* bits, normally 0 */
   float sun_dir[3];       /* direction toward the sun (normalised by the library) */
   float sun_intensity;    /* hit radiance = albedo * intensity/pi * max(0, n.l) * visibility */
   float tmin, tmax;       /* primary ray interval; shaders/env_map.rgen:22-23 use .001, 10000 */

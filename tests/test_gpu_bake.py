@@ -65,6 +65,13 @@ def test_paths_agree(ctx, lmax):
     skyh = ctx.sky(sky, 128)
     plain = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FP32, sun, sky=skyh))
     fused = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FUSED, sun, sky=skyh))
+    pk = vlb.bake_params(ds, lmax, vlb.PREC_FUSED, sun, sky=skyh)
+    pk.flags = vlb.BAKE_FORCE_FUSED_KERNEL
+    kernel = ctx.bake(scene, probes, pk)
+    assert parity.per_probe_rel(kernel, plain).max() < 1e-5
+    # the one-kernel schedule is deterministic and independent of the batch
+    kernel2 = ctx.bake(scene, probes[::-1].copy(), pk)[::-1]
+    assert np.array_equal(kernel, kernel2)
     mixed = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_MIXED, sun, sky=skyh))
     assert parity.per_probe_rel(fused, plain).max() < 1e-5
     e = parity.per_probe_rel(mixed, plain)

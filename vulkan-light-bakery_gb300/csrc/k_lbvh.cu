@@ -15,6 +15,8 @@
 //   7. packing into the traversal layout: internal node = 4 float4 holding
 //      both children's boxes and references; triangle = 3 float4 (v0 | id,
 //      e1, e2) in leaf order.
+#include <algorithm>
+
 #include "vlb_device.cuh"
 #include "vlb_internal.h"
 
@@ -225,9 +227,96 @@ __global__ void k_probe_codes(const float* __restrict__ probes, uint32_t n, floa
   vals[i] = i;
 }
 
+// Whole probe ordering in one CTA for n <= kSmallSort: codes, then three
+// stable 8-bit LSD passes (histogram, scan, ranked scatter) through global
+// ping-pong buffers, with the same warp ranking as k_rs_scatter.  One launch
+// instead of ten for the probe counts of a typical bake request.
+constexpr uint32_t kSmallSort = 16384;
+
+__global__ void __launch_bounds__(1024) k_probe_order_small(const float* __restrict__ probes, uint32_t n, float lox,
+                                                            float loy, float loz, float sx, float sy, float sz,
+                                                            uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
+                                                            uint32_t* order) {
+  constexpr int W = 32;
+  __shared__ uint32_t base[256];
+  __shared__ uint32_t wcnt[W][256];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto q = [](float c, float lo, float s) -> uint32_t {
+    const float v = (c - lo) * s;
+    if (!(v > 0.f)) return 0u;
+    return min(__float2uint_rz(v), 255u);
+  };
+  for (uint32_t i = tid; i < n; i += 1024) {
+    const uint32_t x = q(probes[3 * size_t(i)], lox, sx), y = q(probes[3 * size_t(i) + 1], loy, sy),
+                   z = q(probes[3 * size_t(i) + 2], loz, sz);
+    ka[i] = (expand_bits10(x) << 2) | (expand_bits10(y) << 1) | expand_bits10(z);
+    va[i] = i;
+  }
+  for (uint32_t j = tid; j < W * 256; j += 1024) wcnt[j / 256][j % 256] = 0;
+  __syncthreads();
+  for (int pass = 0; pass < 3; ++pass) {
+    const int shift = 8 * pass;
+    const uint32_t* kin = (pass & 1) ? kb : ka;
+    const uint32_t* vin = (pass & 1) ? vb : va;
+    uint32_t* kout = (pass & 1) ? ka : kb;
+    uint32_t* vout = pass == 2 ? order : ((pass & 1) ? va : vb);
+    if (tid < 256) base[tid] = 0;
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += 1024) atomicAdd(&base[(kin[i] >> shift) & 255u], 1u);
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of the 256 counts: 8 per lane
+      uint32_t v[8], s = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) { v[j] = base[lane * 8 + j]; s += v[j]; }
+      uint32_t incl = s;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= uint32_t(o)) incl += t;
+      }
+      uint32_t run = incl - s;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) { base[lane * 8 + j] = run; run += v[j]; }
+    }
+    __syncthreads();
+    for (uint32_t r0 = 0; r0 < n; r0 += 1024) {
+      const uint32_t i = r0 + tid;
+      const bool valid = i < n;
+      const uint32_t key = valid ? kin[i] : 0u, val = valid ? vin[i] : 0u;
+      const uint32_t d = valid ? ((key >> shift) & 255u) : (256u + lane);
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t rank = __popc(peers & lanemask_lt());
+      if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+      __syncthreads();
+      uint32_t run = 0;
+      if (tid < 256) {
+        for (int w = 0; w < W; ++w) {
+          const uint32_t c = wcnt[w][tid];
+          wcnt[w][tid] = run;
+          run += c;
+        }
+      }
+      __syncthreads();
+      if (valid) {
+        const uint32_t dst = base[d] + wcnt[warp][d] + rank;
+        kout[dst] = key;
+        vout[dst] = val;
+      }
+      __syncthreads();
+      if (tid < 256) {
+        base[tid] += run;
+        for (int w = 0; w < W; ++w) wcnt[w][tid] = 0;
+      }
+      __syncthreads();
+    }
+  }
+}
+
 size_t probe_order_scratch_bytes(uint32_t n) {
   const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
-  return (size_t(n) * 4 + 255) / 256 * 256 * 3 + size_t(nblk) * 256 * 4;
+  const size_t a = (size_t(n) * 4 + 255) / 256 * 256;
+  // multi-pass sort: 3 key/value buffers + histogram; one-CTA sort: 4 buffers
+  return std::max(3 * a + size_t(nblk) * 256 * 4, 4 * a);
 }
 
 int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
@@ -243,6 +332,12 @@ int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], u
   for (int i = 0; i < 3; ++i) {
     const float e = bounds[3 + i] - bounds[i];
     s[i] = e > 0.f ? 256.0f / e : 0.f;
+  }
+  if (n <= kSmallSort) {
+    uint32_t* va = reinterpret_cast<uint32_t*>(base + 3 * a);  // fourth buffer (see probe_order_scratch_bytes)
+    k_probe_order_small<<<1, 1024, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka, va,
+                                            kb, vb, order);
+    return 1;
   }
   k_probe_codes<<<(n + 255) / 256, 256, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka,
                                                  order);

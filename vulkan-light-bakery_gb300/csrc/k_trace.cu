@@ -8,11 +8,12 @@
 // all of them at once: 32 parallel rays from nearby origins.  The warp walks
 // ONE node stack: each node and triangle is fetched once per warp (a uniform
 // address, broadcast to the lanes), every lane tests its own ray, and warp
-// ballots decide which children to visit.  All control flow is warp-uniform,
-// so no lane idles on a divergent path.  A lane's result is exactly its own
-// closest hit -- the warp visits a superset of the nodes the lane needs -- and
-// equal distances resolve to the lower triangle index, so results do not
-// depend on which probes share the packet.
+// ballots decide which children to visit.  All control flow is warp-uniform.
+// The stack is warp-uniform too, so it lives in registers spread over the
+// lanes (entry i in lane i % 32) and a pop is one shuffle.  A lane's result is
+// exactly its own closest hit -- the warp visits a superset of the nodes the
+// lane needs -- and equal distances resolve to the lower triangle index, so
+// results do not depend on which probes share the packet.
 //
 // Per ray:
 //   closest hit in (tmin, tmax)                    [env_map.rgen:22-26]
@@ -23,13 +24,18 @@
 // BVH2 nodes hold both children's boxes (4 x float4 = 64 B); triangles are
 // 3 x float4 in leaf order.
 //
-// Fused mode: each lane accumulates its probe's K x 3 coefficients over the
-// warp's directions (the basis row is warp-uniform); the CTA's warps are
-// consecutive direction chunks of the same packet and are summed in shared
-// memory in a fixed order; the last CTA of a packet (atomic ticket) adds the
-// CTA partials in FP64 in a fixed order and writes the output.  Tile mode
-// writes the [probe][3][S] radiance tile instead (the plain path).
+// Scheduling: persistent, independent warps take work items (packet,
+// direction chunk) from an atomic counter -- no CTA-wide barrier, so a warp
+// that drew cheap directions moves on at once.  Fused mode accumulates each
+// probe's K x 3 coefficients over the chunk in shared memory
+// (lane-contiguous), writes one partial per item, and the last item of a
+// packet (atomic ticket) adds the partials in FP64 in chunk order.  Every
+// probe's sums therefore have the same order whatever the batch and the
+// scheduling.  Tile mode writes the [probe][3][S] radiance tile instead (the
+// plain path).
 #include <cuda_bf16.h>
+
+#include <algorithm>
 
 #include "vlb_device.cuh"
 #include "vlb_internal.h"
@@ -49,6 +55,17 @@ struct Work {
   uint32_t wnodes = 0, wtris = 0, shadow = 0, lnodes = 0;
 };
 
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 __device__ __forceinline__ float safe_inv(float d) {
   return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
 }
@@ -59,15 +76,24 @@ __device__ __forceinline__ void make_ray(RayCtx& r, float ox, float oy, float oz
   r.oix = ox * r.ix; r.oiy = oy * r.iy; r.oiz = oz * r.iz;
 }
 
+// Slab test for a ray in octant OCT (bit a set: 1/d_a < 0).  The octant is
+// the same for every lane of a packet (one direction per packet), so the
+// entry and exit planes of each axis are chosen at compile time and no
+// per-axis min/max is needed.
+template <int OCT>
 __device__ __forceinline__ bool slab(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
                                      float tmin, float tmax, float* tnear) {
-  const float t0x = fmaf(lx, r.ix, -r.oix), t1x = fmaf(hx, r.ix, -r.oix);
-  const float t0y = fmaf(ly, r.iy, -r.oiy), t1y = fmaf(hy, r.iy, -r.oiy);
-  const float t0z = fmaf(lz, r.iz, -r.oiz), t1z = fmaf(hz, r.iz, -r.oiz);
-  const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-  const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+  const float tnx = fmaf((OCT & 1) ? hx : lx, r.ix, -r.oix), tfx = fmaf((OCT & 1) ? lx : hx, r.ix, -r.oix);
+  const float tny = fmaf((OCT & 2) ? hy : ly, r.iy, -r.oiy), tfy = fmaf((OCT & 2) ? ly : hy, r.iy, -r.oiy);
+  const float tnz = fmaf((OCT & 4) ? hz : lz, r.iz, -r.oiz), tfz = fmaf((OCT & 4) ? lz : hz, r.iz, -r.oiz);
+  const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
+  const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
   *tnear = tn;
   return tn <= tf;
+}
+
+__device__ __forceinline__ int octant_of(float dx, float dy, float dz) {
+  return (safe_inv(dx) < 0.f ? 1 : 0) | (safe_inv(dy) < 0.f ? 2 : 0) | (safe_inv(dz) < 0.f ? 4 : 0);
 }
 
 // Moller-Trumbore, inclusive edges; returns t or -1.
@@ -85,18 +111,38 @@ __device__ __forceinline__ float tri_hit(const RayCtx& r, const float4 v0, const
   return (e2.x * qx + e2.y * qy + e2.z * qz) * inv;
 }
 
+// Warp-uniform stack of up to kTraceStack (64) node references held in two
+// registers per lane: entry i sits in lane i % 32, register i / 32.
+struct WarpStack {
+  int r0 = 0, r1 = 0, sp = 0;
+  __device__ __forceinline__ void push(int v, uint32_t lane, int* err) {
+    if (sp >= kTraceStack) {
+      if (lane == 0) atomicAdd(err + kErrStackOverflow, 1);
+      return;
+    }
+    if (lane == uint32_t(sp & 31)) {
+      if (sp < 32) r0 = v; else r1 = v;
+    }
+    ++sp;
+  }
+  __device__ __forceinline__ int pop() {
+    --sp;
+    return __shfl_sync(kFull, sp < 32 ? r0 : r1, sp & 31);
+  }
+};
+
 // Warp-cooperative traversal.  ANY = false: closest hit in (tmin, tbest)
 // with ties to the lower triangle id; ANY = true: a lane stops (active =
 // false, best_slot >= 0) at its first hit in (tmin, tbest).  Must be called
-// by all 32 lanes; lanes with active == false only vote "no".
-template <bool ANY, bool COUNT>
+// by all 32 lanes; lanes with active == false only vote "no".  OCT is the
+// packet's (warp-uniform) ray octant.
+template <int OCT, bool ANY, bool COUNT>
 __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, const float4* __restrict__ nodes,
                                                 const float4* __restrict__ tris, uint32_t ntris, float tmin,
                                                 float& tbest, int& best_slot, int& best_id, int* err, Work& w) {
   if (ntris == 0 || !__any_sync(kFull, active)) return;
   const uint32_t lane = threadIdx.x & 31;
-  int stack[kTraceStack];
-  int sp = 0;
+  WarpStack st;
   int cur = ntris > 1 ? 0 : ~0;
   for (;;) {
     if (cur >= 0) {
@@ -106,8 +152,8 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
       bool h0 = false, h1 = false;
       float tn0 = 0.f, tn1 = 0.f;
       if (active) {
-        h0 = slab(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, tbest, &tn0);
-        h1 = slab(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, tbest, &tn1);
+        h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, tbest, &tn0);
+        h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, tbest, &tn1);
       }
       const unsigned b0 = __ballot_sync(kFull, h0), b1 = __ballot_sync(kFull, h1);
       const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
@@ -118,8 +164,7 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
           const unsigned pref0 = __ballot_sync(kFull, h0 && (!h1 || tn0 <= tn1));
           first0 = 2 * __popc(pref0) >= __popc(b0 | b1);
         }
-        if (sp < kTraceStack) stack[sp++] = first0 ? c1 : c0;
-        else if (lane == 0) atomicAdd(err + kErrStackOverflow, 1);
+        st.push(first0 ? c1 : c0, lane, err);
         cur = first0 ? c0 : c1;
         continue;
       }
@@ -144,9 +189,22 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
         if (!__any_sync(kFull, active)) break;
       }
     }
-    if (sp == 0) break;
-    cur = stack[--sp];
+    if (st.sp == 0) break;
+    cur = st.pop();
   }
+}
+
+// Dispatch on the packet's octant (a warp-uniform branch).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(int oct, const RayCtx& r, bool& active, const float4* __restrict__ nodes,
+                                         const float4* __restrict__ tris, uint32_t ntris, float tmin, float& tbest,
+                                         int& best_slot, int& best_id, int* err, Work& w) {
+#define VLB_OCT(o) \
+  case o: packet_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot, best_id, err, w); break;
+  switch (oct) {
+    VLB_OCT(0) VLB_OCT(1) VLB_OCT(2) VLB_OCT(3) VLB_OCT(4) VLB_OCT(5) VLB_OCT(6) VLB_OCT(7)
+  }
+#undef VLB_OCT
 }
 
 // Nearest cubemap texel; each step one IEEE FP32 operation (matches the
@@ -188,11 +246,12 @@ __device__ __forceinline__ Shaded trace_sample(const TraceArgs& a, bool valid, f
   bool act = valid;
   float tb = a.tmax;
   int slot = -1, id = -1;
-  packet_traverse<false, COUNT>(ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id, a.err, w);
+  traverse<false, COUNT>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id, a.err,
+                         w);
   Shaded o{0.f, 0.f, 0.f, -1, 2};
   RayCtx sh = ray;
   bool need = false;
-  float ndl = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+  float ndl = 0.f;
   if (valid) {
     if (slot < 0) {
       if (a.sky) {
@@ -202,7 +261,7 @@ __device__ __forceinline__ Shaded trace_sample(const TraceArgs& a, bool valid, f
     } else {
       const float4 e1 = __ldg(a.tris + 3 * slot + 1), e2 = __ldg(a.tris + 3 * slot + 2);
       o.tri = id;
-      nx = e1.y * e2.z - e1.z * e2.y; ny = e1.z * e2.x - e1.x * e2.z; nz = e1.x * e2.y - e1.y * e2.x;
+      float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
       const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
       nx *= rn; ny *= rn; nz *= rn;
       if (nx * d.x + ny * d.y + nz * d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
@@ -218,7 +277,9 @@ __device__ __forceinline__ Shaded trace_sample(const TraceArgs& a, bool valid, f
   bool sact = need;
   float stb = a.tmax;
   int sslot = -1, sid = -1;
-  packet_traverse<true, COUNT>(sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb, sslot, sid, a.err, w);
+  // inactive lanes keep their primary ray: the octant comes from the sun, uniform
+  traverse<true, COUNT>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb, sslot,
+                        sid, a.err, w);
   if (need) {
     const bool occ = sslot >= 0;
     o.vis = occ ? 0 : 1;
@@ -231,8 +292,105 @@ __device__ __forceinline__ Shaded trace_sample(const TraceArgs& a, bool valid, f
   return o;
 }
 
-template <bool COUNT>
-__device__ __forceinline__ void flush_counts(const TraceArgs& a, const Work& w) {
+// MODE 0: radiance tile (+ optional per-ray debug arrays); MODE 1: fused projection.
+// Every warp is persistent and independent: lane 0 takes the next work item
+// (packet, direction chunk) from the counter; no CTA-wide barrier anywhere.
+template <int MODE, int K, bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs a) {
+  constexpr int V = 3 * K;
+  constexpr int AW = MODE == 1 ? kTraceWarps : 1, AV = MODE == 1 ? V : 1;
+  __shared__ float acc[AW][AV][32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t npg = (a.nprobes + 31) / 32;
+  const uint32_t total = npg * a.chunks;
+  Work w;
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(a.work_counter, 1u);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= total) break;
+    // chunk-major: the warps in flight trace neighbouring chunks of the
+    // octant-grouped direction order, i.e. mostly one traversal variant
+    const uint32_t chunk = item / npg, pg = item - chunk * npg;
+    const uint32_t slot = pg * 32 + lane;
+    const bool valid = slot < a.nprobes;
+    const uint32_t p = valid ? a.order[slot] : 0;
+    const float ox = valid ? a.probes[3 * size_t(p)] : 0.f, oy = valid ? a.probes[3 * size_t(p) + 1] : 0.f,
+                oz = valid ? a.probes[3 * size_t(p) + 2] : 0.f;
+    const uint32_t s0 = min(a.S, chunk * a.dirs_per_warp), s1 = min(a.S, s0 + a.dirs_per_warp);
+    if constexpr (MODE == 1) {
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[warp][v][lane] = 0.f;
+    }
+    for (uint32_t t = s0; t < s1; ++t) {
+      const uint32_t s = __ldg(a.dir_order + t);  // direction index (caller order)
+      const Shaded o = trace_sample<COUNT>(a, valid, ox, oy, oz, __ldg(a.dirs + s), w);
+      if constexpr (MODE == 1) {
+        const float4* b4 = reinterpret_cast<const float4*>(a.basis16 + size_t(s) * 16);
+#pragma unroll
+        for (int q = 0; q < (K + 3) / 4; ++q) {
+          const float4 b = __ldg(b4 + q);
+          const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int k = 4 * q + e;
+            if (k < K) {
+              acc[warp][3 * k][lane] = fmaf(bb[e], o.r, acc[warp][3 * k][lane]);
+              acc[warp][3 * k + 1][lane] = fmaf(bb[e], o.g, acc[warp][3 * k + 1][lane]);
+              acc[warp][3 * k + 2][lane] = fmaf(bb[e], o.b, acc[warp][3 * k + 2][lane]);
+            }
+          }
+        }
+      }
+      if (!valid) continue;
+      const size_t ri = size_t(p) * a.S + s;
+      if (a.hit_tri) a.hit_tri[ri] = o.tri;
+      if (a.shadow) a.shadow[ri] = o.vis;
+      if constexpr (MODE == 0) {
+        const size_t row = size_t(p) * 3;
+        if (a.radiance) {
+          a.radiance[row * a.S + s] = o.r;
+          a.radiance[(row + 1) * a.S + s] = o.g;
+          a.radiance[(row + 2) * a.S + s] = o.b;
+        }
+        if (a.radiance_bf16) {
+          a.radiance_bf16[row * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
+          a.radiance_bf16[(row + 1) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
+          a.radiance_bf16[(row + 2) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
+        }
+        if (a.dbg_radiance) {
+          a.dbg_radiance[3 * ri] = o.r; a.dbg_radiance[3 * ri + 1] = o.g; a.dbg_radiance[3 * ri + 2] = o.b;
+        }
+      }
+    }
+    if constexpr (MODE == 1) {
+      __syncwarp();
+      if (a.chunks == 1) {
+        if (valid)
+          for (int v = 0; v < V; ++v) a.out[size_t(p) * V + v] = acc[warp][v][lane];
+        continue;
+      }
+      if (valid)
+        for (int v = 0; v < V; ++v) a.partial[(size_t(p) * a.chunks + chunk) * V + v] = acc[warp][v][lane];
+      // the last item of this packet adds the chunk partials in FP64, in chunk order
+      __threadfence();
+      __syncwarp();
+      uint32_t ticket = 0;
+      if (lane == 0) ticket = atomicAdd(a.group_done + pg, 1u);
+      ticket = __shfl_sync(kFull, ticket, 0);
+      if (ticket == a.chunks - 1) {
+        __threadfence();
+        if (valid) {
+          const float* src = a.partial + size_t(p) * a.chunks * V;
+          for (int v = 0; v < V; ++v) {
+            double s = 0.0;
+            for (uint32_t j = 0; j < a.chunks; ++j) s += double(__ldcg(src + size_t(j) * V + v));
+            a.out[size_t(p) * V + v] = float(s);
+          }
+        }
+      }
+    }
+  }
   if constexpr (COUNT) {
     atomicAdd(a.counters + 0, (unsigned long long)w.wnodes);
     atomicAdd(a.counters + 1, (unsigned long long)w.wtris);
@@ -241,150 +399,40 @@ __device__ __forceinline__ void flush_counts(const TraceArgs& a, const Work& w) 
   }
 }
 
-// Plain path: writes the [probe][3][S] radiance tile (FP32 and/or BF16).
-template <bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_tile(const TraceArgs a) {
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t pg = blockIdx.x / a.block_chunks, bc = blockIdx.x - pg * a.block_chunks;
-  const uint32_t chunk = bc * kTraceWarps + warp;
-  const uint32_t slot = pg * 32 + lane;
-  const bool valid = slot < a.nprobes;
-  const uint32_t p = valid ? (a.order ? a.order[slot] : slot) : 0;
-  const float ox = valid ? a.probes[3 * size_t(p)] : 0.f, oy = valid ? a.probes[3 * size_t(p) + 1] : 0.f,
-              oz = valid ? a.probes[3 * size_t(p) + 2] : 0.f;
-  const uint32_t s0 = min(a.S, chunk * a.dirs_per_warp), s1 = min(a.S, s0 + a.dirs_per_warp);
-  Work w;
-  for (uint32_t s = s0; s < s1; ++s) {
-    const Shaded o = trace_sample<COUNT>(a, valid, ox, oy, oz, __ldg(a.dirs + s), w);
-    if (!valid) continue;
-    const size_t row = size_t(p) * 3;
-    if (a.radiance) {
-      a.radiance[row * a.S + s] = o.r;
-      a.radiance[(row + 1) * a.S + s] = o.g;
-      a.radiance[(row + 2) * a.S + s] = o.b;
-    }
-    if (a.radiance_bf16) {
-      a.radiance_bf16[row * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
-      a.radiance_bf16[(row + 1) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
-      a.radiance_bf16[(row + 2) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
-    }
-    const size_t ri = size_t(p) * a.S + s;
-    if (a.hit_tri) a.hit_tri[ri] = o.tri;
-    if (a.shadow) a.shadow[ri] = o.vis;
-    if (a.dbg_radiance) {
-      a.dbg_radiance[3 * ri] = o.r; a.dbg_radiance[3 * ri + 1] = o.g; a.dbg_radiance[3 * ri + 2] = o.b;
-    }
-  }
-  flush_counts<COUNT>(a, w);
-}
-
-template <int K>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_fused(const TraceArgs a) {
-  constexpr int V = 3 * K;
-  __shared__ float red[kTraceWarps][32][V + 1];
-  __shared__ uint32_t ticket;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t pg = blockIdx.x / a.block_chunks, bc = blockIdx.x - pg * a.block_chunks;
-  const uint32_t chunk = bc * kTraceWarps + warp;
-  const uint32_t slot = pg * 32 + lane;
-  const bool valid = slot < a.nprobes;
-  const uint32_t p = valid ? (a.order ? a.order[slot] : slot) : 0;
-  const float ox = valid ? a.probes[3 * size_t(p)] : 0.f, oy = valid ? a.probes[3 * size_t(p) + 1] : 0.f,
-              oz = valid ? a.probes[3 * size_t(p) + 2] : 0.f;
-  const uint32_t s0 = min(a.S, chunk * a.dirs_per_warp), s1 = min(a.S, s0 + a.dirs_per_warp);
-  float acc[V];
-#pragma unroll
-  for (int v = 0; v < V; ++v) acc[v] = 0.f;
-  Work w;
-  for (uint32_t s = s0; s < s1; ++s) {
-    const Shaded o = trace_sample<false>(a, valid, ox, oy, oz, __ldg(a.dirs + s), w);
-    const float4* b4 = reinterpret_cast<const float4*>(a.basis16 + size_t(s) * 16);
-#pragma unroll
-    for (int q = 0; q < (K + 3) / 4; ++q) {
-      const float4 b = __ldg(b4 + q);
-      const float bb[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int k = 4 * q + e;
-        if (k < K) {
-          acc[3 * k] = fmaf(bb[e], o.r, acc[3 * k]);
-          acc[3 * k + 1] = fmaf(bb[e], o.g, acc[3 * k + 1]);
-          acc[3 * k + 2] = fmaf(bb[e], o.b, acc[3 * k + 2]);
-        }
-      }
-    }
-    if (valid) {
-      const size_t ri = size_t(p) * a.S + s;
-      if (a.hit_tri) a.hit_tri[ri] = o.tri;
-      if (a.shadow) a.shadow[ri] = o.vis;
-    }
-  }
-  // CTA reduction over its warps (consecutive direction chunks), fixed order
-#pragma unroll
-  for (int v = 0; v < V; ++v) red[warp][lane][v] = acc[v];
-  __syncthreads();
-  const bool direct = a.block_chunks == 1;
-  for (uint32_t e = threadIdx.x; e < 32u * V; e += kTraceThreads) {
-    const uint32_t l = e / V, v = e - l * V;
-    const uint32_t sl = pg * 32 + l;
-    if (sl >= a.nprobes) continue;
-    float s = 0.f;
-#pragma unroll
-    for (int wi = 0; wi < kTraceWarps; ++wi) s += red[wi][l][v];
-    const uint32_t pp = a.order ? a.order[sl] : sl;
-    if (direct) a.out[size_t(pp) * V + v] = s;
-    else a.partial[(size_t(pp) * a.block_chunks + bc) * V + v] = s;
-  }
-  if (direct) return;
-  // the last CTA of this packet sums the CTA partials in FP64, fixed order
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) ticket = atomicAdd(a.group_done + pg, 1u);
-  __syncthreads();
-  if (ticket != a.block_chunks - 1) return;
-  __threadfence();
-  for (uint32_t e = threadIdx.x; e < 32u * V; e += kTraceThreads) {
-    const uint32_t l = e / V, v = e - l * V;
-    const uint32_t sl = pg * 32 + l;
-    if (sl >= a.nprobes) continue;
-    const uint32_t pp = a.order ? a.order[sl] : sl;
-    const float* src = a.partial + size_t(pp) * a.block_chunks * V + v;
-    double s = 0.0;
-    for (uint32_t j = 0; j < a.block_chunks; ++j) s += double(__ldcg(src + size_t(j) * V));
-    a.out[size_t(pp) * V + v] = float(s);
-  }
-}
-
-void plan_trace(TraceArgs& a, int num_sms) {
+void plan_trace(TraceArgs& a, int num_sms, bool fused) {
   const uint64_t npg = (uint64_t(a.nprobes) + 31) / 32;
-  const uint64_t target = uint64_t(num_sms) * 48;  // warps
-  uint64_t nsc = (target + npg - 1) / npg;
-  uint64_t bcn = (nsc + kTraceWarps - 1) / kTraceWarps;
-  nsc = bcn * kTraceWarps;
-  uint64_t dpw = (a.S + nsc - 1) / nsc;
-  if (dpw == 0) dpw = 1;
-  const uint64_t nsc_eff = (a.S + dpw - 1) / dpw;
-  bcn = (nsc_eff + kTraceWarps - 1) / kTraceWarps;
+  // items: ~8 per resident warp for balance (tile mode); in fused mode each
+  // extra chunk costs a K x 3 partial per probe, so stop at ~2 per warp
+  const uint64_t warps = uint64_t(num_sms) * 32;
+  const uint64_t target = fused ? 2 * warps : 8 * warps;
+  uint64_t chunks = (target + npg - 1) / npg;
+  chunks = std::max<uint64_t>(1, std::min<uint64_t>(chunks, a.S ? a.S : 1));
+  const uint64_t dpw = std::max<uint64_t>(1, (uint64_t(a.S) + chunks - 1) / chunks);
   a.dirs_per_warp = uint32_t(dpw);
-  a.block_chunks = uint32_t(bcn > 0 ? bcn : 1);
+  a.chunks = uint32_t(std::max<uint64_t>(1, (uint64_t(a.S) + dpw - 1) / dpw));
 }
 
-static uint32_t trace_grid(const TraceArgs& a) {
-  return uint32_t(((uint64_t(a.nprobes) + 31) / 32) * a.block_chunks);
+template <int MODE, int K, bool COUNT>
+static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  const uint64_t items = ((uint64_t(a.nprobes) + 31) / 32) * a.chunks;
+  if (!items) return;
+  static int per_sm = 0;  // resident CTAs per SM for this instantiation
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<MODE, K, COUNT>, kTraceThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t ctas = std::min<uint64_t>((items + kTraceWarps - 1) / kTraceWarps, uint64_t(num_sms) * per_sm);
+  k_trace<MODE, K, COUNT><<<uint32_t(ctas), kTraceThreads, 0, s>>>(a);
 }
 
-void launch_trace_tile(const TraceArgs& a, cudaStream_t s) {
-  const uint32_t g = trace_grid(a);
-  if (!g) return;
-  if (a.counters) k_trace_tile<true><<<g, kTraceThreads, 0, s>>>(a);
-  else k_trace_tile<false><<<g, kTraceThreads, 0, s>>>(a);
+void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  if (a.counters) launch<0, 1, true>(a, num_sms, s);
+  else launch<0, 1, false>(a, num_sms, s);
 }
 
-void launch_trace_fused(const TraceArgs& a, cudaStream_t s) {
-  const uint32_t g = trace_grid(a);
-  if (!g) return;
-  if (a.K == 9) k_trace_fused<9><<<g, kTraceThreads, 0, s>>>(a);
-  else k_trace_fused<16><<<g, kTraceThreads, 0, s>>>(a);
+void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  if (a.K == 9) launch<1, 9, false>(a, num_sms, s);
+  else launch<1, 16, false>(a, num_sms, s);
 }
 
 }  // namespace vlbk

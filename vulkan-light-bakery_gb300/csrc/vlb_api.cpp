@@ -208,6 +208,23 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
   VLB_CUDA(ctx, cudaMalloc(&d->d_basis16, size_t(n) * 16 * sizeof(float)));
   VLB_CUDA(ctx, cudaMemcpy(d->d_dirs, d4.data(), d4.size() * 4, cudaMemcpyHostToDevice));
   VLB_CUDA(ctx, cudaMemcpy(d->d_basis16, d->h_basis32.data(), d->h_basis32.size() * 4, cudaMemcpyHostToDevice));
+  // trace order: directions grouped by ray octant (sign of 1/d per axis, as
+  // the traversal sees it), stable; warps in flight then share one traversal
+  // variant.  Outputs stay indexed by the caller's direction order.
+  std::vector<uint32_t> order(n);
+  auto oct = [&](uint32_t s) {
+    int o = 0;
+    for (int a = 0; a < 3; ++a) {
+      const float c = d->h_dirs[3 * s + a];
+      const bool neg = std::fabs(c) > 1e-30f ? c < 0.f : std::signbit(c);
+      o |= neg ? (1 << a) : 0;
+    }
+    return o;
+  };
+  for (uint32_t s = 0; s < n; ++s) order[s] = s;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return oct(x) < oct(y); });
+  VLB_CUDA(ctx, cudaMalloc(&d->d_order, size_t(n) * 4));
+  VLB_CUDA(ctx, cudaMemcpy(d->d_order, order.data(), size_t(n) * 4, cudaMemcpyHostToDevice));
   return VLB_OK;
 }
 
@@ -596,6 +613,7 @@ void vlb_dirset_destroy(vlb_dirset* d) {
   if (d->ctx) { cudaSetDevice(d->ctx->device); cudaStreamSynchronize(d->ctx->stream); }
   cudaFree(d->d_dirs);
   cudaFree(d->d_basis16);
+  cudaFree(d->d_order);
   delete d;
 }
 
@@ -772,13 +790,17 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
   a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
   a.order = static_cast<const uint32_t*>(order);
-  a.dirs = p->dirs->d_dirs; a.S = p->dirs->n;
+  a.dirs = p->dirs->d_dirs; a.dir_order = p->dirs->d_order; a.S = p->dirs->n;
   a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
   a.sun_scale = float(double(p->sun_intensity) / kPi);
   a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
   a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
   a.basis16 = p->dirs->d_basis16; a.K = k_of(p->lmax); a.err = ctx->d_err;
-  vlbk::plan_trace(a, ctx->num_sms);
+  vlbk::plan_trace(a, ctx->num_sms, p->precision == VLB_PREC_FUSED);
+  void* wc;
+  if ((st = scratch(ctx, "trace_work", 256, &wc))) return st;
+  VLB_CUDA(ctx, cudaMemsetAsync(wc, 0, 4, ctx->stream));
+  a.work_counter = static_cast<uint32_t*>(wc);
   return VLB_OK;
 }
 
@@ -804,13 +826,21 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     a.shadow = static_cast<uint8_t*>(os.dev);
     a.dbg_radiance = static_cast<float*>(orad.dev);
   }
-  if (p->precision == VLB_PREC_FUSED) {
-    if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "per-ray radiance is not kept by the fused path");
+  // VLB_PREC_FUSED runs the one-kernel schedule when every packet's directions
+  // fit at most two work items (large probe counts); smaller bakes are faster
+  // through the radiance tile, which then stays in L2.
+  bool fused = p->precision == VLB_PREC_FUSED && a.chunks <= 2 && !a.dbg_radiance;
+  if (p->precision == VLB_PREC_FUSED && (p->flags & VLB_BAKE_FORCE_FUSED_KERNEL)) {
+    if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "the fused kernel keeps no per-ray radiance");
+    fused = true;
+  }
+  if (p->precision == VLB_PREC_FUSED && !fused) vlbk::plan_trace(a, ctx->num_sms, false);
+  if (fused) {
     a.out = static_cast<float*>(ob.dev);
-    if (a.block_chunks > 1) {
+    if (a.chunks > 1) {
       void *part, *done;
       const size_t groups = (size_t(nprobes) + 31) / 32;
-      if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * a.block_chunks * V * 4, &part)) ||
+      if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * a.chunks * V * 4, &part)) ||
           (st = scratch(ctx, "bake_group_done", groups * 4, &done)))
         return st;
       VLB_CUDA(ctx, cudaMemsetAsync(done, 0, groups * 4, ctx->stream));
@@ -818,7 +848,7 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
       a.group_done = static_cast<uint32_t*>(done);
     }
     KScope k(ctx, "trace_fused");
-    vlbk::launch_trace_fused(a, ctx->stream);
+    vlbk::launch_trace_fused(a, ctx->num_sms, ctx->stream);
   } else {
     const bool bf16 = p->precision == VLB_PREC_MIXED;
     void* tile;
@@ -827,7 +857,7 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     else a.radiance = static_cast<float*>(tile);
     {
       KScope k(ctx, "trace_tile");
-      vlbk::launch_trace_tile(a, ctx->stream);
+      vlbk::launch_trace_tile(a, ctx->num_sms, ctx->stream);
     }
     {
       KScope k(ctx, bf16 ? "project_bf16" : "project_f32");
@@ -866,7 +896,7 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a.counters = static_cast<unsigned long long*>(cnt);
   {
     KScope k(ctx, "trace_tile_counted");
-    vlbk::launch_trace_tile(a, ctx->stream);
+    vlbk::launch_trace_tile(a, ctx->num_sms, ctx->stream);
   }
   if ((st = finish(ctx, true))) return st;
   unsigned long long h[4];

@@ -96,7 +96,8 @@ struct TraceArgs {
   const float* probes;    // device nprobes*3
   const uint32_t* order;  // device permutation: packet slot -> probe index
   uint32_t nprobes;
-  const float4* dirs;     // device S (xyz)
+  const float4* dirs;     // device S (xyz), caller order
+  const uint32_t* dir_order;  // device S: trace position -> direction index (grouped by octant)
   uint32_t S;
   float3 sun;             // unit
   float sun_scale;        // intensity / pi
@@ -114,19 +115,24 @@ struct TraceArgs {
   uint32_t K;
   float* partial;         // [nprobes][block chunks][K*3]
   uint32_t* group_done;   // [probe groups] completion counters (zero before the launch)
+  uint32_t* work_counter; // next (packet, CTA chunk) item for the persistent CTAs (zero before the launch)
   float* out;             // [nprobes][K][3]
-  // decomposition: a warp owns one 32-probe packet and dirs_per_warp
-  // consecutive directions; a CTA owns kTraceWarps consecutive chunks of one packet
+  // decomposition: a work item is one 32-probe packet and one chunk of
+  // dirs_per_warp consecutive directions; persistent warps pull items
   uint32_t dirs_per_warp;
-  uint32_t block_chunks;  // CTAs per packet
+  uint32_t chunks;        // direction chunks per packet
   unsigned long long* counters;  // null, or [warp node fetches, warp triangle fetches, shadow rays, lane node tests]
   int* err;
 };
 constexpr int kTraceWarps = 4;
-// Chooses dirs_per_warp / block_chunks for nprobes x S rays on num_sms SMs.
-void plan_trace(TraceArgs& a, int num_sms);
-void launch_trace_tile(const TraceArgs& a, cudaStream_t s);
-void launch_trace_fused(const TraceArgs& a, cudaStream_t s);
+// Chooses dirs_per_warp / chunks for nprobes x S rays on num_sms SMs: fine
+// items for load balance, coarser in fused mode where each item leaves a
+// K x 3 partial per probe.
+void plan_trace(TraceArgs& a, int num_sms, bool fused);
+// Persistent launches: at most num_sms x (resident CTAs per SM) CTAs pull
+// items from a.work_counter, which must be zero before the launch.
+void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s);
+void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s);
 
 }  // namespace vlbk
 
@@ -169,6 +175,7 @@ struct vlb_dirset {
   vlb_ctx* ctx = nullptr;
   uint32_t n = 0;
   float4* d_dirs = nullptr;     // n trace directions
+  uint32_t* d_order = nullptr;  // n direction indices sorted by ray octant (stable)
   float* d_basis16 = nullptr;   // n x 16 weighted basis, FP32
   std::vector<float> h_dirs;    // n*3
   std::vector<double> h_basis;  // n*16 FP64 weighted basis

@@ -23,6 +23,7 @@ SKY_CUBEMAP, SKY_PANORAMA, SKY_ENVMAP = 0, 1, 2
 TEXEL_RGB32F, TEXEL_RGBA8 = 0, 1
 SKY_REF_BGRA_SWAP = 1
 PREC_FP32, PREC_FUSED, PREC_MIXED = 0, 1, 2
+BAKE_FORCE_FUSED_KERNEL = 1
 DTYPE_F32, DTYPE_BF16 = 0, 1
 
 
