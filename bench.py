@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
+    ap.add_argument("--only", choices=["skybox", "projection"], default=None,
+                    help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
 
@@ -201,6 +203,11 @@ def main():
     torch.cuda.set_stream(stream)
     ctx = vlb.Context(local)
     ctx.set_stream(stream.cuda_stream)
+    if args.only:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        fn = skybox_measure if args.only == "skybox" else projection_measure
+        print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
+        return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
     scene = ctx.scene(pos, idx, alb)
     dirs = ctx.fibonacci(NDIRS)
@@ -331,6 +338,7 @@ def main():
                          "kind": "port", "sample": f"first {len(sample)} of {P} probes, {NDIRS} dirs each"},
         "clocks": clk,
         "skybox_c0": skybox_measure(ctx, torch, stream, args.steps, hbm_peak),
+        "projection_c2": projection_measure(ctx, torch, stream, args.steps, hbm_peak),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -379,6 +387,51 @@ def skybox_measure(ctx, torch, stream, steps, hbm_peak):
         "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "algorithmic_bytes_per_launch": bytes_per_launch,
                      "avg_launch_ms": k_avg, "traffic": load_traffic(kname)},
+    }
+
+
+def projection_measure(ctx, torch, stream, steps, hbm_peak, nprobes=262144, S=1024):
+    """Config 2 projection: a [262,144 x 3, 1024] radiance tile resident in
+    HBM, BF16 through the tcgen05 kernel (hi/lo BF16 basis, FP32
+    accumulation) and FP32 through the CUDA-core kernel."""
+    import vlb
+
+    ds = ctx.fibonacci(S)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    t16 = (torch.rand((nprobes * 3, S), generator=g, device="cuda") * 5).to(torch.bfloat16)
+    out = torch.empty((nprobes, vlb.k_of(LMAX), 3), dtype=torch.float32, device="cuda")
+
+    def run(tile, dtype, k):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for a, b in evs:
+            a.record(stream)
+            ctx.project(tile, nprobes, ds, LMAX, dtype=dtype, out=out)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    bits = t16.view(torch.int16)
+    run(bits, vlb.DTYPE_BF16, 3)
+    ms16 = run(bits, vlb.DTYPE_BF16, steps)
+    t32 = t16.float()
+    run(t32, vlb.DTYPE_F32, 3)
+    ms32 = run(t32, vlb.DTYPE_F32, steps)
+    del t32
+    b16 = nprobes * 3 * S * 2 + out.numel() * 4
+    b32 = nprobes * 3 * S * 4 + out.numel() * 4
+    m16 = sorted(ms16)[len(ms16) // 2]
+    m32 = sorted(ms32)[len(ms32) // 2]
+    flops = 2 * nprobes * 3 * S * 32  # the MMA work (N = 32: high and low basis halves)
+    return {
+        "workload": f"SH projection of a [{nprobes}x3, {S}] radiance tile resident in HBM, L{LMAX}",
+        "bf16_tcgen05": {"probes_per_s": nprobes / (m16 / 1e3), "ms": m16,
+                         "roofline": {"kernel": "project_tc", "bound": "hbm", "achieved": b16 / (m16 * 1e-3) / 1e9,
+                                      "peak": hbm_peak, "unit": "GB/s",
+                                      "frac": b16 / (m16 * 1e-3) / 1e9 / hbm_peak,
+                                      "algorithmic_bytes_per_launch": b16, "mma_tflops": flops / (m16 * 1e-3) / 1e12,
+                                      "traffic": load_traffic("project_tc")}},
+        "fp32_cuda_cores": {"probes_per_s": nprobes / (m32 / 1e3), "ms": m32,
+                            "achieved_gbs": b32 / (m32 * 1e-3) / 1e9},
     }
 
 

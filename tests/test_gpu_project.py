@@ -65,6 +65,28 @@ def test_project_bf16_matches_oracle_on_rounded_input(ctx):
     assert rel(got, ref) < 1e-5
 
 
+@pytest.mark.parametrize("lmax", [2, 3])
+@pytest.mark.parametrize("nprobes,S", [(1, 64), (43, 1000), (300, 1024), (5, 104), (7, 100), (100_000, 1024)])
+def test_project_bf16_tensor_core_matches_oracle(ctx, lmax, nprobes, S):
+    """BF16 tiles go through the tcgen05 kernel (S % 8 == 0) or the CUDA-core
+    kernel (S = 100); hi/lo BF16 basis, FP32 accumulation."""
+    torch = pytest.importorskip("torch")
+    ds = ctx.fibonacci(S)
+    d, w = O.dirs_fibonacci(S)
+    B = O.basis_matrix(d.astype(np.float64), w, lmax)
+    g = torch.Generator().manual_seed(nprobes + S + lmax)
+    rad = (torch.rand((nprobes, 3, S), generator=g) * 5).to(torch.bfloat16)
+    dev = rad.cuda().view(torch.int16)
+    out = torch.empty((nprobes, vlb.k_of(lmax), 3), dtype=torch.float32, device="cuda")
+    ctx.project(dev, nprobes, ds, lmax, dtype=vlb.DTYPE_BF16, out=out)
+    ctx.synchronize()
+    got = out.cpu().numpy()
+    m = min(nprobes, 2000)  # the oracle checks a prefix of the large tile
+    ref = O.project(rad[:m].float().numpy(), m, S, B)
+    assert rel(got[:m], ref) < 1e-5
+    assert np.isfinite(got).all()
+
+
 def test_sh_eval_matches_reference_golden(ctx, golden):
     w, h = (int(v) for v in golden["recon_wh"])
     got = ctx.sh_eval_envmap(golden["coeffs"], 3, w, h, 1250.0)

@@ -188,6 +188,20 @@ void sh_basis16(double x, double y, double z, double* o) {
   o[14] = 1.445306 * z * (x * x - y * y); o[15] = -0.590044 * x * (x * x - 3.0 * y * y);
 }
 
+// BF16 with round-to-nearest-even (finite inputs).
+uint16_t bf16_rne(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return uint16_t(u >> 16);
+}
+float bf16_to_float(uint16_t h) {
+  const uint32_t u = uint32_t(h) << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
 // Builds the host + device halves of a direction set.
 vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>& bdirs, const std::vector<double>& w) {
   const uint32_t n = d->n;
@@ -225,6 +239,19 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
   std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return oct(x) < oct(y); });
   VLB_CUDA(ctx, cudaMalloc(&d->d_order, size_t(n) * 4));
   VLB_CUDA(ctx, cudaMemcpy(d->d_order, order.data(), size_t(n) * 4, cudaMemcpyHostToDevice));
+  // BF16 basis for the tensor-core projection, transposed [32][pitch]: row k
+  // the BF16 rounding of w_s Y_k, row 16 + k the BF16 rounding of the rest
+  d->bt_pitch = (n + 7) / 8 * 8;
+  std::vector<uint16_t> bt(size_t(32) * d->bt_pitch, 0);
+  for (uint32_t s = 0; s < n; ++s)
+    for (int k = 0; k < 16; ++k) {
+      const double b = d->h_basis[size_t(s) * 16 + k];
+      const uint16_t hi = bf16_rne(float(b));
+      bt[size_t(k) * d->bt_pitch + s] = hi;
+      bt[size_t(16 + k) * d->bt_pitch + s] = bf16_rne(float(b - double(bf16_to_float(hi))));
+    }
+  VLB_CUDA(ctx, cudaMalloc(&d->d_bt, bt.size() * 2));
+  VLB_CUDA(ctx, cudaMemcpy(d->d_bt, bt.data(), bt.size() * 2, cudaMemcpyHostToDevice));
   return VLB_OK;
 }
 
@@ -614,6 +641,7 @@ void vlb_dirset_destroy(vlb_dirset* d) {
   cudaFree(d->d_dirs);
   cudaFree(d->d_basis16);
   cudaFree(d->d_order);
+  cudaFree(d->d_bt);
   delete d;
 }
 
@@ -757,6 +785,23 @@ void vlb_bake_params_default(vlb_bake_params* p) {
   p->shadow_bias = 0.005f;
 }
 
+// BF16 tile projection: the tcgen05 kernel when the tile meets its alignment
+// (S a multiple of 8, 16-byte aligned), else the CUDA-core kernel.
+static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprobes, const vlb_dirset* dirs,
+                               uint32_t K, float* out) {
+  const uint32_t S = dirs->n;
+  if (vlbk::project_tc_supported(rad, S)) {
+    KScope k(ctx, "project_tc");
+    if (vlbk::launch_project_tc(rad, nprobes, S, dirs->d_bt, dirs->bt_pitch, K, out, ctx->d_err, ctx->num_sms,
+                                ctx->stream) < 0)
+      return fail(ctx, VLB_ERR_CUDA, "tensor map encoding failed for the BF16 projection");
+    return VLB_OK;
+  }
+  KScope k(ctx, "project_bf16");
+  vlbk::launch_project_bf16_simt(rad, nprobes, S, dirs->d_basis16, K, out, ctx->stream);
+  return VLB_OK;
+}
+
 // Common part of a bake launch: validated parameters -> trace arguments,
 // probes staged on the device and sorted into spatially compact packets.
 static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
@@ -859,14 +904,12 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
       KScope k(ctx, "trace_tile");
       vlbk::launch_trace_tile(a, ctx->num_sms, ctx->stream);
     }
-    {
-      KScope k(ctx, bf16 ? "project_bf16" : "project_f32");
-      if (bf16)
-        vlbk::launch_project_bf16_simt(a.radiance_bf16, nprobes, S, p->dirs->d_basis16, K,
-                                       static_cast<float*>(ob.dev), ctx->stream);
-      else
-        vlbk::launch_project_f32(a.radiance, nprobes, S, p->dirs->d_basis16, K, static_cast<float*>(ob.dev),
-                                 ctx->stream);
+    if (bf16) {
+      if ((st = project_bf16(ctx, a.radiance_bf16, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) return st;
+    } else {
+      KScope k(ctx, "project_f32");
+      vlbk::launch_project_f32(a.radiance, nprobes, S, p->dirs->d_basis16, K, static_cast<float*>(ob.dev),
+                               ctx->stream);
     }
   }
   if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) || (st = copy_out(ctx, orad)))
@@ -927,14 +970,13 @@ vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint
   if ((st = stage_in(ctx, radiance, size_t(nprobes) * 3 * S * eb, "proj_in", &drad))) return st;
   OutBuf ob;
   if ((st = stage_out(ctx, out, size_t(nprobes) * K * 12, "proj_out", &ob))) return st;
-  {
-    KScope k(ctx, dtype == VLB_DTYPE_F32 ? "project_f32" : "project_bf16");
-    if (dtype == VLB_DTYPE_F32)
-      vlbk::launch_project_f32(static_cast<const float*>(drad), nprobes, S, dirs->d_basis16, K,
-                               static_cast<float*>(ob.dev), ctx->stream);
-    else
-      vlbk::launch_project_bf16_simt(static_cast<const uint16_t*>(drad), nprobes, S, dirs->d_basis16, K,
-                                     static_cast<float*>(ob.dev), ctx->stream);
+  if (dtype == VLB_DTYPE_F32) {
+    KScope k(ctx, "project_f32");
+    vlbk::launch_project_f32(static_cast<const float*>(drad), nprobes, S, dirs->d_basis16, K,
+                             static_cast<float*>(ob.dev), ctx->stream);
+  } else if ((st = project_bf16(ctx, static_cast<const uint16_t*>(drad), nprobes, dirs, K,
+                                static_cast<float*>(ob.dev)))) {
+    return st;
   }
   if ((st = copy_out(ctx, ob))) return st;
   return finish(ctx, ob.host);

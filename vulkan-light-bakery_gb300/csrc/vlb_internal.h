@@ -54,6 +54,13 @@ void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, con
                         float* out, cudaStream_t s);
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
                               uint32_t K, float* out, cudaStream_t s);
+// tcgen05 projection of a BF16 tile (k_project_tc.cu).  basis_bt: [32][bt_pitch]
+// BF16, rows 0..15 the high and 16..31 the low part of the weighted basis.
+// Needs S % 8 == 0 and a 16-byte aligned tile; returns -1 if the tensor maps
+// cannot be built.
+bool project_tc_supported(const void* radiance, uint32_t S);
+int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const uint16_t* basis_bt,
+                      uint32_t bt_pitch, uint32_t K, float* out, int* err, int num_sms, cudaStream_t s);
 void launch_sh_eval_envmap(const float* coeffs, uint32_t K, uint32_t w, uint32_t h, float scale, const float2* col_tab,
                            const float4* row_tab, float* out, cudaStream_t s);
 
@@ -176,6 +183,8 @@ struct vlb_dirset {
   uint32_t n = 0;
   float4* d_dirs = nullptr;     // n trace directions
   uint32_t* d_order = nullptr;  // n direction indices sorted by ray octant (stable)
+  uint16_t* d_bt = nullptr;     // [32][bt_pitch] BF16 weighted basis, high rows 0..15, low rows 16..31
+  uint32_t bt_pitch = 0;
   float* d_basis16 = nullptr;   // n x 16 weighted basis, FP32
   std::vector<float> h_dirs;    // n*3
   std::vector<double> h_basis;  // n*16 FP64 weighted basis
