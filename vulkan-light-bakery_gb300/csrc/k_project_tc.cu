@@ -74,10 +74,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 // Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, 8-row
 // swizzle atoms 1024 bytes apart (stride byte offset); the leading byte offset
 // is not used by swizzled K-major layouts.

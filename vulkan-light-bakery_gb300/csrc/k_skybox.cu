@@ -4,20 +4,25 @@
 //
 // The reference lets every texel do an unsynchronised read-modify-write of
 // the 48 output floats (skybox_sh.comp:39), so its result depends on
-// scheduling.  Here each CTA owns a contiguous slab of texels, streams it
-// through shared memory with 1-D bulk async copies (cp.async.bulk, completion
-// on an mbarrier, 4 stages), evaluates the basis per texel in FP32, reduces
-// with warp shuffles, writes one partial per slab, and a second kernel sums
-// the slabs of each map in FP64 in a fixed order.  The result is identical
-// run to run and independent of how many maps are batched together.
+// scheduling.  Here a work unit is a fixed slab of kSkySlab texels of a group
+// of G maps.  The CTA streams the group's texels through a 4-stage shared-
+// memory ring filled by 1-D bulk async copies (cp.async.bulk, completion on
+// an mbarrier; one copy per map per stage), computes each texel's direction,
+// solid angle and weighted basis ONCE and applies it to the G maps with
+// packed FP32x2 FMAs (two maps per instruction), reduces each map's sums with
+// warp shuffles into one partial per (map, slab), and a second kernel adds a
+// map's slabs in FP64 in a fixed order.  The slab size does not depend on the
+// batch, so a map's result is bit-identical alone or in any batch.
 #include "vlb_device.cuh"
 #include "vlb_internal.h"
 
 namespace vlbk {
 
-constexpr int kSkyThreads = 256;
-constexpr int kSkyChunk = 1024;  // texels per pipeline stage, 4 per thread
-constexpr int kSkyStages = 4;
+constexpr int kSkyConsumers = 32 * kSkyPartialsPerSlab;  // consumer threads (8 warps)
+constexpr int kSkyThreads = kSkyConsumers + 32;           // + one producer warp
+constexpr int kSkyChunk = 512;  // texels per map per pipeline stage, 2 per consumer thread
+constexpr int kSkyStages = 3;
+constexpr uint32_t kSkySlab = 8192;  // texels per work unit, independent of the batch
 
 // Exact solid angle of cube-face texel (x, y) of an n x n face, in FP64:
 // corner sum of atan2(u v, sqrt(u^2 + v^2 + 1)), the antiderivative of the
@@ -37,207 +42,344 @@ void launch_cube_solid_angle(float* out, uint32_t n, cudaStream_t s) {
   k_cube_solid_angle<<<(total + 255) / 256, 256, 0, s>>>(out, n);
 }
 
-struct SlabIter {
-  uint32_t unit, chunk, seq;
-};
+// Weighted basis per cubemap texel, FP64 throughout, rounded once to FP32.
+// Constants of shaders/sh_common.h:26-116; faces +X,-X,+Y,-Y,+Z,-Z.
+__global__ void k_cube_basis_table(float4* out, uint32_t n, uint32_t lmax) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6 * n * n) return;
+  const uint32_t nn = n * n, face = t / nn, rem = t - face * nn, y = rem / n, x = rem - y * n;
+  const double s = 2.0 / double(n);
+  const double u0 = -1.0 + s * x, u1 = u0 + s, v0 = -1.0 + s * y, v1 = v0 + s;
+  auto A = [](double u, double v) { return atan2(u * v, sqrt(u * u + v * v + 1.0)); };
+  const double w = A(u0, v0) - A(u0, v1) - A(u1, v0) + A(u1, v1);
+  const double u = u0 + 0.5 * s, v = v0 + 0.5 * s;
+  double d[3];
+  switch (face) {
+    case 0: d[0] = 1.0; d[1] = -v; d[2] = -u; break;
+    case 1: d[0] = -1.0; d[1] = -v; d[2] = u; break;
+    case 2: d[0] = u; d[1] = 1.0; d[2] = v; break;
+    case 3: d[0] = u; d[1] = -1.0; d[2] = -v; break;
+    case 4: d[0] = u; d[1] = -v; d[2] = 1.0; break;
+    default: d[0] = -u; d[1] = -v; d[2] = -1.0; break;
+  }
+  const double r = 1.0 / sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double X = d[0] * r, Yy = d[1] * r, Z = d[2] * r;
+  double b[16] = {0.282095, -0.488603 * Yy, 0.488603 * Z, -0.488603 * X, 1.092548 * X * Yy, -1.092548 * Yy * Z,
+                  0.315392 * (-X * X - Yy * Yy + 2.0 * Z * Z), -1.092548 * X * Z, 0.546274 * (X * X - Yy * Yy),
+                  -0.590044 * Yy * (3.0 * X * X - Yy * Yy), 2.890611 * X * Yy * Z,
+                  -0.457046 * Yy * (4.0 * Z * Z - X * X - Yy * Yy),
+                  0.373176 * Z * (2.0 * Z * Z - 3.0 * X * X - 3.0 * Yy * Yy),
+                  -0.457046 * X * (4.0 * Z * Z - X * X - Yy * Yy), 1.445306 * Z * (X * X - Yy * Yy),
+                  -0.590044 * X * (X * X - 3.0 * Yy * Yy)};
+  const uint32_t K = (lmax + 1) * (lmax + 1), NQ = (K + 3) / 4;
+  for (uint32_t q = 0; q < NQ; ++q) {
+    float f[4];
+    for (int e = 0; e < 4; ++e) f[e] = (4 * q + e < K) ? float(w * b[4 * q + e]) : 0.f;
+    out[size_t(t) * NQ + q] = make_float4(f[0], f[1], f[2], f[3]);
+  }
+}
 
-template <int LMAX, int LAYOUT, int FMT, bool TMA>
+void launch_cube_basis_table(float4* out, uint32_t n, uint32_t lmax, cudaStream_t s) {
+  const uint32_t total = 6 * n * n;
+  k_cube_basis_table<<<(total + 255) / 256, 256, 0, s>>>(out, n, lmax);
+}
+
+void skybox_plan(SkyboxArgs& a, uint32_t max_slabs) {
+  uint32_t slab = kSkySlab;
+  if (max_slabs && (a.texels_per_map + slab - 1) / slab > max_slabs)
+    slab = ((a.texels_per_map + max_slabs - 1) / max_slabs + kSkyChunk - 1) / kSkyChunk * kSkyChunk;
+  a.slab_texels = slab;
+  a.slabs_per_map = (a.texels_per_map + slab - 1) / slab;
+  // two maps per unit fill one packed FP32x2 pair and keep ~120 registers,
+  // two CTAs per SM (four maps measured slower: ~190 registers, one CTA)
+  a.group = a.count == 1 ? 1 : 2;
+}
+
+// q = num / d for num < 2^31 (float estimate, then exact integer correction)
+__device__ __forceinline__ uint32_t udiv(uint32_t num, uint32_t d, float inv_d) {
+  uint32_t q = __float2uint_rz(__fmul_rn(float(num) + 0.5f, inv_d));
+  while (q * d > num) --q;
+  while (num - q * d >= d) ++q;
+  return q;
+}
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<uint64_t*>(&a)), "l"(*reinterpret_cast<uint64_t*>(&b)),
+        "l"(*reinterpret_cast<uint64_t*>(&c)));
+  return *reinterpret_cast<float2*>(&d);
+}
+
+template <int FMT>
+__device__ __forceinline__ void texel_rgb(const unsigned char* p, uint32_t i, bool swap, float* c) {
+  if constexpr (FMT == 0) {
+    const float* f = reinterpret_cast<const float*>(p) + 3 * i;
+    c[0] = f[0]; c[1] = f[1]; c[2] = f[2];
+  } else {
+    const uchar4 q = reinterpret_cast<const uchar4*>(p)[i];
+    const float s = 1.0f / 255.0f;
+    c[0] = q.x * s; c[1] = q.y * s; c[2] = q.z * s;
+  }
+  if (swap) { const float t = c[0]; c[0] = c[2]; c[2] = t; }
+}
+
+// Warp-specialised: warps 0..7 consume, warp 8 (TMA path) produces.  The
+// producer refills a stage as soon as all 8 consumer warps have arrived on
+// its `empty` barrier; consumers never wait for each other.  Each consumer
+// warp reduces its own sums with shuffles and writes one partial per (map,
+// slab, warp), so no CTA-wide barrier follows the set-up -- a consumer whose
+// bounded wait gives up simply stops, and nobody is left waiting for it.
+template <int LMAX, int LAYOUT, int FMT, int G, bool TMA, bool BT>
 __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
   constexpr int K = sh_k<LMAX>();
   constexpr int V = 3 * K;
-  constexpr int TB = FMT == 0 ? 12 : 4;  // bytes per texel
+  constexpr int GP = (G + 1) / 2;  // map pairs
+  constexpr int TB = FMT == 0 ? 12 : 4;
+  constexpr uint32_t kMapChunkBytes = kSkyChunk * TB;
+  constexpr int NQ = (K + 3) / 4;  // float4 per basis-table row
+  constexpr uint32_t kTabBytes = BT ? kSkyChunk * NQ * 16 : 0;
+  constexpr uint32_t kStageBytes = G * kMapChunkBytes + kTabBytes;  // G map chunks, then the table chunk
+  constexpr uint32_t kConsumerWarps = kSkyConsumers / 32;
   extern __shared__ __align__(128) unsigned char stage_mem[];
-  __shared__ __align__(8) uint64_t bars[kSkyStages];
-  __shared__ float red[kSkyThreads / 32][V];
+  __shared__ __align__(8) uint64_t full[kSkyStages], empty[kSkyStages];
+  __shared__ volatile int abort_flag;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t units = a.count * a.slabs_per_map;
-  const uint32_t T = a.texels_per_map;
+  const uint32_t T = a.texels_per_map, spm = a.slabs_per_map;
+  const uint32_t groups = (a.count + G - 1) / G;
+  const uint32_t units = groups * spm;
+  const unsigned char* tex = static_cast<const unsigned char*>(a.texels);
 
-  auto unit_range = [&](uint32_t u, uint32_t* t0, uint32_t* nchunks) {
-    const uint32_t j = u % a.slabs_per_map;
-    *t0 = j * a.slab_texels;
-    const uint32_t t1 = min(T, *t0 + a.slab_texels);
-    *nchunks = (t1 - *t0 + kSkyChunk - 1) / kSkyChunk;
+  // (unit, chunk) iteration shared by the producer and the consumers
+  struct It { uint32_t unit, chunk, seq; };
+  auto nchunks = [&](uint32_t u) {
+    const uint32_t t0 = (u % spm) * a.slab_texels, t1 = min(T, t0 + a.slab_texels);
+    return (t1 - t0 + kSkyChunk - 1) / kSkyChunk;
   };
-  auto chunk_texels = [&](uint32_t u, uint32_t c) -> uint32_t {
-    uint32_t t0, nc;
-    unit_range(u, &t0, &nc);
-    const uint32_t t1 = min(T, t0 + a.slab_texels);
-    const uint32_t b = t0 + c * kSkyChunk;
-    return min(uint32_t(kSkyChunk), t1 - b);
-  };
-  auto advance = [&](SlabIter& it) {
-    uint32_t t0, nc;
-    unit_range(it.unit, &t0, &nc);
+  auto advance = [&](It& it) {
     ++it.seq;
-    if (++it.chunk == nc) { it.chunk = 0; it.unit += gridDim.x; }
+    if (++it.chunk == nchunks(it.unit)) { it.chunk = 0; it.unit += gridDim.x; }
+  };
+  auto chunk_span = [&](const It& it, uint32_t* tb, uint32_t* nt, uint32_t* m0, uint32_t* gv) {
+    const uint32_t t0 = (it.unit % spm) * a.slab_texels, t1 = min(T, t0 + a.slab_texels);
+    *tb = t0 + it.chunk * kSkyChunk;
+    *nt = min(uint32_t(kSkyChunk), t1 - *tb);
+    *m0 = (it.unit / spm) * G;
+    *gv = min(uint32_t(G), a.count - *m0);
   };
 
-  SlabIter prod{blockIdx.x, 0, 0};
-  auto issue = [&](SlabIter& it) {
-    const uint32_t st = it.seq % kSkyStages;
-    uint32_t t0, nc;
-    unit_range(it.unit, &t0, &nc);
-    const uint32_t nt = chunk_texels(it.unit, it.chunk);
-    const uint32_t m = it.unit / a.slabs_per_map;
-    const size_t first = size_t(m) * T + t0 + size_t(it.chunk) * kSkyChunk;
-    const unsigned char* src = static_cast<const unsigned char*>(a.texels) + first * TB;
-    mbar_arrive_expect_tx(&bars[st], nt * TB);
-    bulk_g2s(stage_mem + size_t(st) * kSkyChunk * TB, src, nt * TB, &bars[st]);
-    advance(it);
-  };
+  if (tid == 0) {
+    for (int i = 0; i < kSkyStages; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kConsumerWarps); }
+    abort_flag = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
 
-  if constexpr (TMA) {
-    if (tid == 0) {
-      for (int i = 0; i < kSkyStages; ++i) mbar_init(&bars[i], 1);
-      fence_mbar_init();
+  if (warp == kConsumerWarps) {  // producer warp
+    if (TMA && lane == 0) {
+      It it{blockIdx.x, 0, 0};
+      while (it.unit < units && !abort_flag) {
+        const uint32_t st = it.seq % kSkyStages;
+        if (!mbar_wait_bounded(&empty[st], ((it.seq / kSkyStages) & 1u) ^ 1u, a.err)) { abort_flag = 1; break; }
+        uint32_t tb, nt, m0, gv;
+        chunk_span(it, &tb, &nt, &m0, &gv);
+        unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;
+        mbar_arrive_expect_tx(&full[st], gv * nt * TB + (BT ? nt * NQ * 16 : 0));
+        for (uint32_t g = 0; g < gv; ++g)
+          bulk_g2s(sbase + g * kMapChunkBytes, tex + (size_t(m0 + g) * T + tb) * TB, nt * TB, &full[st]);
+        if constexpr (BT)
+          bulk_g2s(sbase + G * kMapChunkBytes, a.basis_table + size_t(tb) * NQ, nt * NQ * 16, &full[st]);
+        advance(it);
+      }
+      // every copy issued lands before the CTA may exit
+      const uint32_t first = it.seq > uint32_t(kSkyStages) ? it.seq - kSkyStages : 0;
+      for (uint32_t q = first; q < it.seq; ++q)
+        mbar_wait_bounded(&full[q % kSkyStages], (q / kSkyStages) & 1u, a.err, 1u << 16);
     }
-    __syncthreads();
-    if (tid == 0)
-      for (int i = 0; i < kSkyStages && prod.unit < units; ++i) issue(prod);
+    return;
   }
 
-  float acc[V];
+  float2 acc[GP][V];
 #pragma unroll
-  for (int v = 0; v < V; ++v) acc[v] = 0.f;
+  for (int p = 0; p < GP; ++p)
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[p][v] = make_float2(0.f, 0.f);
 
   const bool swap_rb = (a.flags & VLB_SKY_REF_BGRA_SWAP) != 0;
-  const float inv255 = 1.0f / 255.0f;
-  bool timed_out = false;
+  const float inv_w = 1.0f / float(a.w);
+  const uint32_t nn = a.w * a.w;
+  const float inv_nn = 1.0f / float(nn);
 
-  SlabIter cons{blockIdx.x, 0, 0};
+  It cons{blockIdx.x, 0, 0};
   while (cons.unit < units) {
-    uint32_t t0, nc;
-    unit_range(cons.unit, &t0, &nc);
-    const uint32_t nt = chunk_texels(cons.unit, cons.chunk);
-    const uint32_t m = cons.unit / a.slabs_per_map;
-    const uint32_t tbase = t0 + cons.chunk * kSkyChunk;  // texel index within the map
+    uint32_t tb, nt, m0, gv;
+    chunk_span(cons, &tb, &nt, &m0, &gv);
     const uint32_t st = cons.seq % kSkyStages;
-    bool ok = true;
-    if constexpr (TMA) ok = mbar_wait_bounded(&bars[st], (cons.seq / kSkyStages) & 1u, a.err);
-    const unsigned char* sbase = TMA ? stage_mem + size_t(st) * kSkyChunk * TB
-                                     : static_cast<const unsigned char*>(a.texels) + (size_t(m) * T + tbase) * TB;
-    if (ok) {
+    if constexpr (TMA) {
+      if (!mbar_wait_bounded(&full[st], (cons.seq / kSkyStages) & 1u, a.err)) abort_flag = 1;
+    }
+    if (abort_flag) break;
+    const unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;
+    // per-chunk pointers: the group's texel chunks and the basis-table chunk
+    const unsigned char* mp[G];
 #pragma unroll
-      for (int r = 0; r < kSkyChunk / kSkyThreads; ++r) {
-        const uint32_t i = tid + r * kSkyThreads;
-        if (i < nt) {
-          float cr, cg, cb;
-          if constexpr (FMT == 0) {
-            const float* p = reinterpret_cast<const float*>(sbase) + 3 * i;
-            cr = p[0]; cg = p[1]; cb = p[2];
-          } else {
-            const uchar4 q = reinterpret_cast<const uchar4*>(sbase)[i];
-            cr = q.x * inv255; cg = q.y * inv255; cb = q.z * inv255;
-          }
-          if (swap_rb) { const float tmp = cr; cr = cb; cb = tmp; }
-          const uint32_t t = tbase + i;
-          float bx, by, bz, w;
-          if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
-            const uint32_t n = a.w, nn = n * n;
-            const uint32_t face = t / nn, rem = t - face * nn, y = rem / n, x = rem - y * n;
-            const float inv_n = 1.0f / float(n);
-            const float u = fmaf(float(x), 2.0f * inv_n, inv_n - 1.0f);
-            const float v = fmaf(float(y), 2.0f * inv_n, inv_n - 1.0f);
-            const float rn = rsqrtf(fmaf(u, u, fmaf(v, v, 1.0f)));
-            switch (face) {
-              case 0: bx = rn; by = -v * rn; bz = -u * rn; break;
-              case 1: bx = -rn; by = -v * rn; bz = u * rn; break;
-              case 2: bx = u * rn; by = rn; bz = v * rn; break;
-              case 3: bx = u * rn; by = -rn; bz = -v * rn; break;
-              case 4: bx = u * rn; by = -v * rn; bz = rn; break;
-              default: bx = -u * rn; by = -v * rn; bz = -rn; break;
-            }
-            w = __ldg(a.solid_angle + rem);
-          } else {
-            const uint32_t y = t / a.w, x = t - y * a.w;
-            const float2 cs = __ldg(a.col_tab + x);
-            const float4 rw = __ldg(a.row_tab + y);
-            const float dx = rw.x * cs.x, dy = rw.x * cs.y, dz = rw.y;
-            if constexpr (LAYOUT == VLB_SKY_PANORAMA) { bx = dx; by = dz; bz = dy; }  // skybox_sh.comp:39 dir.xzy
-            else { bx = dx; by = dy; bz = dz; }
-            w = rw.z;
-          }
-          float Y[K];
-          sh_basis<LMAX>(bx, by, bz, Y);
-          const float wr = w * cr, wg = w * cg, wb = w * cb;
+    for (int g = 0; g < G; ++g)
+      mp[g] = TMA ? sbase + g * kMapChunkBytes : tex + (size_t(m0 + min(uint32_t(g), gv - 1)) * T + tb) * TB;
+    const float4* tab = BT ? (TMA ? reinterpret_cast<const float4*>(sbase + G * kMapChunkBytes)
+                                  : a.basis_table + size_t(tb) * NQ)
+                           : nullptr;
+    // chunk origin: one division per chunk, the texels then step from it
+    uint32_t face0 = 0, rem0 = 0, y0 = 0, x0 = 0;
+    if constexpr (BT) {
+    } else if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
+      face0 = udiv(tb, nn, inv_nn);
+      rem0 = tb - face0 * nn;
+    } else {
+      y0 = udiv(tb, a.w, inv_w);
+      x0 = tb - y0 * a.w;
+    }
+#pragma unroll 1
+    for (uint32_t i = tid; i < nt; i += kSkyConsumers) {
+      float Y[K];
+      if constexpr (BT) {
+        // cached weighted basis of this texel position (shared by every map)
 #pragma unroll
-          for (int k = 0; k < K; ++k) {
-            acc[3 * k] = fmaf(Y[k], wr, acc[3 * k]);
-            acc[3 * k + 1] = fmaf(Y[k], wg, acc[3 * k + 1]);
-            acc[3 * k + 2] = fmaf(Y[k], wb, acc[3 * k + 2]);
+        for (int q = 0; q < NQ; ++q) {
+          const float4 b = tab[size_t(i) * NQ + q];  // shared memory (TMA) or global: a generic load
+          const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (4 * q + e < K) Y[4 * q + e] = bb[e];
+        }
+      } else {
+        float bx, by, bz, w;
+        if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
+          const uint32_t n = a.w;
+          uint32_t rem = rem0 + i, face = face0;
+          while (rem >= nn) { rem -= nn; ++face; }
+          const uint32_t y = udiv(rem, n, inv_w), x = rem - y * n;
+          const float u = fmaf(float(x), 2.0f * inv_w, inv_w - 1.0f);
+          const float v = fmaf(float(y), 2.0f * inv_w, inv_w - 1.0f);
+          const float rn = rsqrtf(fmaf(u, u, fmaf(v, v, 1.0f)));
+          switch (face) {
+            case 0: bx = rn; by = -v * rn; bz = -u * rn; break;
+            case 1: bx = -rn; by = -v * rn; bz = u * rn; break;
+            case 2: bx = u * rn; by = rn; bz = v * rn; break;
+            case 3: bx = u * rn; by = -rn; bz = -v * rn; break;
+            case 4: bx = u * rn; by = -v * rn; bz = rn; break;
+            default: bx = -u * rn; by = -v * rn; bz = -rn; break;
           }
+          w = __ldg(a.solid_angle + rem);
+        } else {
+          const uint32_t xi = x0 + i;
+          const uint32_t dy = udiv(xi, a.w, inv_w);
+          const uint32_t x = xi - dy * a.w, y = y0 + dy;
+          const float2 cs = __ldg(a.col_tab + x);
+          const float4 rw = __ldg(a.row_tab + y);
+          const float dx = rw.x * cs.x, dyy = rw.x * cs.y, dz = rw.y;
+          if constexpr (LAYOUT == VLB_SKY_PANORAMA) { bx = dx; by = dz; bz = dyy; }  // skybox_sh.comp:39 dir.xzy
+          else { bx = dx; by = dyy; bz = dz; }
+          w = rw.z;
+        }
+        sh_basis<LMAX>(bx, by, bz, Y);
+#pragma unroll
+        for (int k = 0; k < K; ++k) Y[k] *= w;
+      }
+#pragma unroll
+      for (int p = 0; p < GP; ++p) {
+        float ca[3], cb[3] = {0.f, 0.f, 0.f};
+        texel_rgb<FMT>(mp[2 * p], i, false, ca);
+        if (2 * p + 1 < G) texel_rgb<FMT>(mp[2 * p + 1], i, false, cb);  // stale or repeated if gv < G: never written
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float2 yk = make_float2(Y[k], Y[k]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[p][3 * k + c] = ffma2(yk, make_float2(ca[c], cb[c]), acc[p][3 * k + c]);
         }
       }
     }
-    const bool last = cons.chunk + 1 == nc;
     if constexpr (TMA) {
-      if (__syncthreads_or(!ok)) { timed_out = true; break; }
-      if (tid == 0 && prod.unit < units) issue(prod);  // refill the stage just drained
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
     }
-    if (last) {
+    if (cons.chunk + 1 == nchunks(cons.unit)) {
+      // the warp's partial for each map of the group: partial[map][slab][warp][v]
+      const uint32_t slab = cons.unit % spm;
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const float s = warp_sum(acc[v]);
-        if (lane == 0) red[warp][v] = s;
-        acc[v] = 0.f;
-      }
-      __syncthreads();
-      if (tid < V) {
-        float s = 0.f;
+      for (int p = 0; p < GP; ++p)
 #pragma unroll
-        for (int w = 0; w < kSkyThreads / 32; ++w) s += red[w][tid];
-        a.partial[size_t(cons.unit) * V + tid] = s;
-      }
-      __syncthreads();
+        for (int v = 0; v < V; ++v) {
+          const float s0 = warp_sum(acc[p][v].x), s1 = warp_sum(acc[p][v].y);
+          acc[p][v] = make_float2(0.f, 0.f);
+          if (lane == 0) {
+            const int k = v / 3, c = v - 3 * k;
+            const int vo = 3 * k + (swap_rb ? 2 - c : c);  // R/B swap applied to the linear result
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const uint32_t g = 2 * p + h;
+              if (g < gv && (h == 0 || 2 * p + 1 < G))
+                a.partial[((size_t(m0 + g) * spm + slab) * kConsumerWarps + warp) * V + vo] = h ? s1 : s0;
+            }
+          }
+        }
     }
     advance(cons);
   }
-  if constexpr (TMA) {
-    // After a timeout, let copies already issued land before the CTA exits.
-    if (timed_out && tid == 0) {
-      for (uint32_t q = cons.seq; q < prod.seq; ++q)
-        mbar_wait_bounded(&bars[q % kSkyStages], (q / kSkyStages) & 1u, a.err, 1u << 16);
-    }
+}
+
+template <int LMAX, int LAYOUT, int FMT, int G, bool BT>
+static void launch4(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
+  const int TB = FMT == 0 ? 12 : 4;
+  const size_t tab = BT ? size_t(kSkyChunk) * ((sh_k<LMAX>() + 3) / 4) * 16 : 0;
+  const size_t smem = tma ? size_t(kSkyStages) * (G * kSkyChunk * TB + tab) : 0;
+  const uint32_t groups = (a.count + G - 1) / G;
+  const uint64_t units = uint64_t(groups) * a.slabs_per_map;
+  auto k = tma ? k_skybox_sh<LMAX, LAYOUT, FMT, G, true, BT> : k_skybox_sh<LMAX, LAYOUT, FMT, G, false, BT>;
+  if (smem) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSkyThreads, smem);
+  if (per_sm < 1) per_sm = 1;
+  const uint64_t cap = uint64_t(num_sms) * per_sm;
+  const int grid = int(units < cap ? units : cap);
+  k<<<grid, kSkyThreads, smem, s>>>(a);
+}
+
+template <int LMAX, int LAYOUT, int FMT, int G>
+static void launch4b(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
+  if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
+    if (a.basis_table) { launch4<LMAX, LAYOUT, FMT, G, true>(a, tma, num_sms, s); return; }
   }
+  launch4<LMAX, LAYOUT, FMT, G, false>(a, tma, num_sms, s);
 }
 
 template <int LMAX, int LAYOUT, int FMT>
-static void launch3(const SkyboxArgs& a, bool tma, int grid, cudaStream_t s) {
-  const int TB = FMT == 0 ? 12 : 4;
-  const size_t smem = tma ? size_t(kSkyStages) * kSkyChunk * TB : 0;
-  if (tma) {
-    auto k = k_skybox_sh<LMAX, LAYOUT, FMT, true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k<<<grid, kSkyThreads, smem, s>>>(a);
-  } else {
-    k_skybox_sh<LMAX, LAYOUT, FMT, false><<<grid, kSkyThreads, 0, s>>>(a);
-  }
+static void launch3(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
+  if (a.group == 1) launch4b<LMAX, LAYOUT, FMT, 1>(a, tma, num_sms, s);
+  else if (LMAX == 2 && a.group == 4) launch4b<LMAX, LAYOUT, FMT, 4>(a, tma, num_sms, s);
+  else launch4b<LMAX, LAYOUT, FMT, 2>(a, tma, num_sms, s);
 }
 
 template <int LMAX, int LAYOUT>
-static void launch2(const SkyboxArgs& a, bool tma, int grid, cudaStream_t s) {
-  if (a.fmt == VLB_TEXEL_RGB32F) launch3<LMAX, LAYOUT, 0>(a, tma, grid, s);
-  else launch3<LMAX, LAYOUT, 1>(a, tma, grid, s);
+static void launch2(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
+  if (a.fmt == VLB_TEXEL_RGB32F) launch3<LMAX, LAYOUT, 0>(a, tma, num_sms, s);
+  else launch3<LMAX, LAYOUT, 1>(a, tma, num_sms, s);
 }
 
 template <int LMAX>
-static void launch1(const SkyboxArgs& a, bool tma, int grid, cudaStream_t s) {
+static void launch1(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
   switch (a.layout) {
-    case VLB_SKY_CUBEMAP: launch2<LMAX, VLB_SKY_CUBEMAP>(a, tma, grid, s); break;
-    case VLB_SKY_PANORAMA: launch2<LMAX, VLB_SKY_PANORAMA>(a, tma, grid, s); break;
-    default: launch2<LMAX, VLB_SKY_ENVMAP>(a, tma, grid, s); break;
+    case VLB_SKY_CUBEMAP: launch2<LMAX, VLB_SKY_CUBEMAP>(a, tma, num_sms, s); break;
+    case VLB_SKY_PANORAMA: launch2<LMAX, VLB_SKY_PANORAMA>(a, tma, num_sms, s); break;
+    default: launch2<LMAX, VLB_SKY_ENVMAP>(a, tma, num_sms, s); break;
   }
 }
 
 int launch_skybox_sh(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
-  const uint32_t units = a.count * a.slabs_per_map;
-  const uint64_t cap = uint64_t(num_sms) * 4;
-  const int grid = int(units < cap ? units : cap);
-  if (a.lmax == 2) launch1<2>(a, tma, grid, s);
-  else launch1<3>(a, tma, grid, s);
-  return grid;
+  if (a.lmax == 2) launch1<2>(a, tma, num_sms, s);
+  else launch1<3>(a, tma, num_sms, s);
+  return 0;
 }
 
 __global__ void k_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, uint32_t nvals, float* out) {

@@ -120,13 +120,12 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
   vlbk::SkyboxArgs a{};
   a.texels = texels; a.fmt = fmt; a.layout = layout; a.w = w; a.h = h; a.count = 1; a.lmax = lmax;
   a.flags = flags; a.texels_per_map = T; a.err = err;
-  // same work split as vlb_skybox_sh for one map
-  const uint32_t chunk = 1024;
-  uint32_t spm = std::min<uint32_t>(std::max<uint32_t>(1, 2u * num_sms), (T + chunk - 1) / chunk);
-  const uint32_t slab = ((T + spm - 1) / spm + chunk - 1) / chunk * chunk;
-  spm = (T + slab - 1) / slab;
-  if (spm > kMaxSlabs) return VLB_ERR_INVALID;
-  a.slab_texels = slab; a.slabs_per_map = spm; a.partial = partial;
+  // the work split of vlb_skybox_sh within kMaxSlabs partials (8 per slab):
+  // maps above 64 x 8192 texels get wider slabs
+  vlbk::skybox_plan(a, kMaxSlabs / vlbk::kSkyPartialsPerSlab);
+  const uint32_t spm = a.slabs_per_map;
+  if (spm * vlbk::kSkyPartialsPerSlab > kMaxSlabs) return VLB_ERR_INVALID;
+  a.partial = partial;
   if (cudaMemsetAsync(err, 0, vlbk::kErrSlots * sizeof(int), s) != cudaSuccess) return VLB_ERR_CUDA;
   if (layout == VLB_SKY_CUBEMAP) {
     vlbk::launch_cube_solid_angle(table, w, s);
@@ -138,7 +137,7 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
   }
   const bool tma = (reinterpret_cast<uintptr_t>(texels) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
   vlbk::launch_skybox_sh(a, tma, num_sms, s);
-  vlbk::launch_sh_finalize(partial, 1, spm, V, out, s);
+  vlbk::launch_sh_finalize(partial, 1, spm * vlbk::kSkyPartialsPerSlab, V, out, s);
   if (cudaGetLastError() != cudaSuccess) return VLB_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return VLB_ERR_CUDA;
   int herr[vlbk::kErrSlots];

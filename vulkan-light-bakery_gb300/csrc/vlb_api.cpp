@@ -371,6 +371,7 @@ void vlb_ctx_destroy(vlb_ctx* ctx) {
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   for (auto& kv : ctx->cube_sa) cudaFree(kv.second);
+  for (auto& kv : ctx->cube_bt) cudaFree(kv.second);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -662,6 +663,22 @@ vlb_status vlb_dirset_export(const vlb_dirset* d, float* trace_dirs, float* basi
 }
 
 // ---- skybox SH ---------------------------------------------------------------------------
+static vlb_status cube_basis_table(vlb_ctx* ctx, uint32_t n, uint32_t lmax, const float4** out) {
+  const uint64_t key = (uint64_t(n) << 8) | lmax;
+  auto it = ctx->cube_bt.find(key);
+  if (it != ctx->cube_bt.end()) { *out = it->second; return VLB_OK; }
+  const size_t nq = (k_of(lmax) + 3) / 4;
+  float4* p = nullptr;
+  VLB_CUDA(ctx, cudaMalloc(&p, size_t(6) * n * n * nq * sizeof(float4)));
+  {
+    KScope k(ctx, "cube_basis_table");
+    vlbk::launch_cube_basis_table(p, n, lmax, ctx->stream);
+  }
+  ctx->cube_bt[key] = p;
+  *out = p;
+  return VLB_OK;
+}
+
 static vlb_status cube_sa_table(vlb_ctx* ctx, uint32_t n, const float** out) {
   auto it = ctx->cube_sa.find(n);
   if (it != ctx->cube_sa.end()) { *out = it->second; return VLB_OK; }
@@ -700,6 +717,8 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
   a.flags = flags; a.texels_per_map = T; a.err = ctx->d_err;
   if (layout == VLB_SKY_CUBEMAP) {
     st = cube_sa_table(ctx, w, &a.solid_angle);
+    // faces up to 512: per-texel weighted basis cached on the device (6n^2 x 48-64 B)
+    if (!st && w <= 512) st = cube_basis_table(ctx, w, lmax, &a.basis_table);
     if (st) return st;
   } else {
     std::vector<float> col, row;
@@ -713,16 +732,10 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
     a.col_tab = static_cast<const float2*>(dc);
     a.row_tab = static_cast<const float4*>(dr);
   }
-  // Work units: enough slabs per map for ~2 CTAs per SM in total.
-  const uint32_t chunk = 1024;
-  const uint32_t max_slabs = (T + chunk - 1) / chunk;
-  uint32_t spm = std::max<uint32_t>(1, uint32_t((2ull * ctx->num_sms + count - 1) / count));
-  spm = std::min(spm, max_slabs);
-  uint32_t slab = ((T + spm - 1) / spm + chunk - 1) / chunk * chunk;
-  spm = (T + slab - 1) / slab;
-  a.slab_texels = slab; a.slabs_per_map = spm;
+  vlbk::skybox_plan(a, 0);
+  const uint32_t spm = a.slabs_per_map;
   void* part;
-  if ((st = scratch(ctx, "sky_partial", size_t(count) * spm * V * 4, &part))) return st;
+  if ((st = scratch(ctx, "sky_partial", size_t(count) * spm * vlbk::kSkyPartialsPerSlab * V * 4, &part))) return st;
   a.partial = static_cast<float*>(part);
   const bool tma = (reinterpret_cast<uintptr_t>(dtex) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
   OutBuf ob;
@@ -733,7 +746,7 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
   }
   {
     KScope k(ctx, "sh_finalize");
-    vlbk::launch_sh_finalize(a.partial, count, spm, V, static_cast<float*>(ob.dev), ctx->stream);
+    vlbk::launch_sh_finalize(a.partial, count, spm * vlbk::kSkyPartialsPerSlab, V, static_cast<float*>(ob.dev), ctx->stream);
   }
   if ((st = copy_out(ctx, ob))) return st;
   return finish(ctx, ob.host);

@@ -36,13 +36,26 @@ struct SkyboxArgs {
   uint32_t texels_per_map;
   uint32_t slab_texels;   // texels per work unit (multiple of the chunk)
   uint32_t slabs_per_map;
+  uint32_t group;         // maps per work unit (1, 2 or 4)
   const float* solid_angle;  // cubemap: w*w table (same for every face)
+  const float4* basis_table; // cubemap, optional: per texel w * Y_k, (lmax+1)^2 padded to a multiple of 4
   const float2* col_tab;     // panorama: w entries (cos phi, sin phi)
   const float4* row_tab;     // panorama: h entries (sin theta, cos theta, weight, 0)
   float* partial;            // count*slabs_per_map*K*3
   int* err;
 };
+// The skybox kernel writes one partial per (map, slab, consumer warp):
+// partial[map][slab][warp][v], kSkyPartialsPerSlab warps.
+constexpr int kSkyPartialsPerSlab = 8;
 void launch_cube_solid_angle(float* out, uint32_t n, cudaStream_t s);
+// Per-texel weighted basis of a 6 x n x n cubemap, computed in FP64 (exact
+// solid angle, normalised direction, basis) and stored in FP32: 3 float4 per
+// texel for lmax 2, 4 for lmax 3.
+void launch_cube_basis_table(float4* out, uint32_t n, uint32_t lmax, cudaStream_t s);
+// Fills slab_texels / slabs_per_map / group from texels_per_map, count and
+// lmax.  The slab is 8192 texels whatever the batch (so a map's sums have one
+// order); max_slabs > 0 caps the slabs per map by widening the slab.
+void skybox_plan(SkyboxArgs& a, uint32_t max_slabs);
 // Returns the number of CTAs launched.
 int launch_skybox_sh(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s);
 // out[m][v] = sum_j partial[m][j][v] in FP64, j in fixed order.
@@ -162,6 +175,7 @@ struct vlb_ctx {
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   std::map<uint32_t, float*> cube_sa;  // solid-angle tables by face size
+  std::map<uint64_t, float4*> cube_bt;  // weighted-basis tables by (face size << 8 | lmax)
 };
 
 struct vlb_scene {
