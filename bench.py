@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
-    ap.add_argument("--only", choices=["skybox", "projection"], default=None,
+    ap.add_argument("--only", choices=["skybox", "projection", "batch"], default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
@@ -205,7 +205,7 @@ def main():
     ctx.set_stream(stream.cuda_stream)
     if args.only:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-        fn = skybox_measure if args.only == "skybox" else projection_measure
+        fn = {"skybox": skybox_measure, "projection": projection_measure, "batch": batch_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
         return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
@@ -339,6 +339,7 @@ def main():
         "clocks": clk,
         "skybox_c0": skybox_measure(ctx, torch, stream, args.steps, hbm_peak),
         "projection_c2": projection_measure(ctx, torch, stream, args.steps, hbm_peak),
+        "batch_c3": batch_measure(ctx, torch, stream, args.steps, hbm_peak),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -432,6 +433,122 @@ def projection_measure(ctx, torch, stream, steps, hbm_peak, nprobes=262144, S=10
                                       "traffic": load_traffic("project_tc")}},
         "fp32_cuda_cores": {"probes_per_s": nprobes / (m32 / 1e3), "ms": m32,
                             "achieved_gbs": b32 / (m32 * 1e-3) / 1e9},
+    }
+
+
+def batch_volumes(seed=SEED, nvol=256):
+    """Uneven batch: per volume a seeded box scene (boxes log-uniform in
+    [16, 16384]), probes log-uniform in [64, 32768] at uniform positions in the
+    scene bounds, rays per probe drawn from {64, 256, 1024}."""
+    import vlb
+
+    rng = np.random.default_rng(seed + 1000)
+    boxes = np.exp(rng.uniform(np.log(16), np.log(16384), nvol)).astype(int)
+    nprobes = np.exp(rng.uniform(np.log(64), np.log(32768), nvol)).astype(int)
+    rays = rng.choice([64, 256, 1024], nvol)
+    vols = []
+    for i in range(nvol):
+        pos, idx, alb = vlb.synth_box_scene(seed * 7919 + i, int(boxes[i]))
+        lo = np.minimum(pos.min(0), 0)
+        hi = np.maximum(pos.max(0), 0)
+        probes = (lo + rng.random((int(nprobes[i]), 3)) * (hi - lo)).astype(np.float32)
+        vols.append((pos, idx, alb, probes, int(rays[i]), vlb.synth_sun(seed * 104729 + i)))
+    return vols
+
+
+def batch_measure(ctx, torch, stream, steps, hbm_peak):
+    """Config 3: 256 uneven bake jobs in one batch (one persistent trace launch
+    over all jobs, one tcgen05 projection per direction set, replayed as a CUDA
+    graph).  BF16 radiance, FP32 accumulation, L2 SH.  Inputs and outputs
+    resident in HBM for `value`; `e2e` passes pinned host probes and outputs."""
+    import vlb
+
+    vols = batch_volumes()
+    sky = ctx.sky(vlb.synth_cubemap(SEED, SKY_N), SKY_N)
+    dsets = {S: ctx.fibonacci(S) for S in (64, 256, 1024)}
+    K = vlb.k_of(LMAX)
+    scenes, plist, jobs, hjobs = [], [], [], []
+    for pos, idx, alb, probes, S, sun in vols:
+        sc = ctx.scene(pos, idx, alb)
+        p = vlb.bake_params(dsets[S], LMAX, vlb.PREC_MIXED, sun, sky=sky)
+        scenes.append(sc)
+        plist.append(p)
+        n = probes.shape[0]
+        jobs.append((sc, torch.from_numpy(probes).cuda(), torch.empty((n, K, 3), device="cuda"), p))
+        hjobs.append((sc, torch.from_numpy(probes).pin_memory(), torch.empty((n, K, 3)).pin_memory(), p))
+    P = sum(v[3].shape[0] for v in vols)
+    rays = sum(v[3].shape[0] * v[4] for v in vols)
+    tris = [int(v[1].shape[0]) for v in vols]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    steps = max(3, min(steps, 10))
+    t0 = time.perf_counter()
+    sched, tune_ms = ctx.batch_autotune(jobs, plist[0], reps=1)
+    tune_s = time.perf_counter() - t0
+
+    def run(js, k, profile=False):
+        ctx.set_profiling(profile)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        l0 = ctx.launch_count
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            ctx.bake_batch(js, plist[0])
+            b.record(stream)
+        torch.cuda.synchronize()
+        ctx.set_profiling(False)
+        return [a.elapsed_time(b) for a, b in evs], ctx.launch_count - l0
+
+    run(jobs, 3)  # direct, capture, replay
+    ms, launches = run(jobs, steps)
+    # per-kernel times (direct launches, library events)
+    ctx.profile_reset()
+    direct = vlb.BatchSchedule(sched.dirs_per_item, sched.cost_order, 0)
+    ctx.set_profiling(True)
+    for _ in range(2):
+        flush.zero_()
+        ctx.bake_batch(jobs, plist[0], direct)
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
+    prof = ctx.profile()
+    # the same jobs as 256 separate vlb_bake calls (device buffers, no sync between)
+    def singles():
+        for sc, pr, o, p in jobs:
+            ctx.bake(sc, pr, p, out=o)
+    singles()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    a.record(stream)
+    singles()
+    b.record(stream)
+    torch.cuda.synchronize()
+    single_ms = a.elapsed_time(b)
+    # e2e: pinned host probes in, host SH out, through the public call
+    run(hjobs, 3)
+    e2e = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.bake_batch(hjobs, plist[0])
+        e2e.append(1e3 * (time.perf_counter() - t))
+    tot = sum(ms)
+    tr = prof.get("trace_batch", (0, 0.0))
+    return {
+        "workload": f"{len(vols)} bake jobs: boxes log-uniform 16-16384 ({min(tris)}-{max(tris)} tris), probes "
+                    f"log-uniform 64-32768 (total {P}), rays per probe in {{64,256,1024}} (total {rays} primary), "
+                    f"L{LMAX} SH, BF16 radiance + tcgen05 projection, CUDA graph replay",
+        "probes_per_s": P * len(ms) / (tot / 1e3), "grays_per_s": rays * len(ms) / (tot / 1e3) / 1e9,
+        "ms_per_batch": tot / len(ms), "p99_ms": sorted(ms)[-1], "gpu_launches_per_batch": launches / len(ms),
+        "schedule": {"dirs_per_item": sched.dirs_per_item, "cost_order": sched.cost_order,
+                     "autotune_s": tune_s, "autotune_best_ms": tune_ms},
+        "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)} for k, v in prof.items()},
+        "trace_batch_grays_per_s": rays / (tr[1] / max(tr[0], 1) * 1e-3) / 1e9 if tr[0] else None,
+        "separate_bakes": {"ms": single_ms, "probes_per_s": P / (single_ms / 1e3),
+                           "note": "the same 256 jobs as separate vlb_bake calls"},
+        "e2e": {"probes_per_s": P * len(e2e) / (sum(e2e) / 1e3), "h2d_bytes_per_step": int(P * 12),
+                "d2h_bytes_per_step": int(P * K * 12)},
+        "l2": "flushed (256 MiB write) before every timed batch",
     }
 
 

@@ -1,0 +1,142 @@
+"""Batched bakes (vlb_bake_batch): many (scene, probes) jobs in one persistent
+trace launch.  Every job's output must be bit-identical to vlb_bake of that
+job alone with the same parameters, whatever the batch composition, the
+schedule (directions per work item, job order), graph replay or output
+residency; one job is also checked against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import parity
+import vlb
+
+pytestmark = pytest.mark.gpu
+
+
+def _uniform_probes(rng, bounds, n):
+    lo, hi = bounds[:3], bounds[3:]
+    return (lo + rng.random((n, 3)) * (hi - lo)).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def batch_world(ctx):
+    """Uneven jobs: scenes of 1..2000 boxes, 0..3000 probes, two direction sets."""
+    rng = np.random.default_rng(7)
+    sky = ctx.sky(vlb.synth_cubemap(5, 32), 32)
+    dsets = {64: ctx.fibonacci(64), 256: ctx.fibonacci(256)}
+    spec = [(1, 37, 64), (2000, 3000, 256), (64, 1, 256), (300, 33, 64), (16, 0, 64), (5, 500, 256),
+            (700, 1029, 64), (64, 31, 256)]
+    jobs = []
+    for i, (nb, n, S) in enumerate(spec):
+        pos, idx, alb = vlb.synth_box_scene(100 + i, nb)
+        scene = ctx.scene(pos, idx, alb)
+        probes = _uniform_probes(rng, scene.bounds(), n)
+        sun = vlb.synth_sun(200 + i)
+        jobs.append(dict(scene=scene, probes=probes, S=S, sun=sun, pos=pos, idx=idx, alb=alb))
+    return dict(jobs=jobs, sky=sky, dsets=dsets)
+
+
+def _job_params(w, j, lmax, precision, intensity=5.0):
+    return vlb.bake_params(w["dsets"][j["S"]], lmax=lmax, precision=precision, sun=j["sun"], sun_intensity=intensity,
+                           sky=w["sky"])
+
+
+def _singles(ctx, w, plist):
+    return [ctx.bake(j["scene"], j["probes"], p) if len(j["probes"]) else np.empty((0, p.lmax ** 2 + 2 * p.lmax + 1, 3),
+                                                                                    np.float32)
+            for j, p in zip(w["jobs"], plist)]
+
+
+@pytest.mark.parametrize("precision,lmax", [(vlb.PREC_MIXED, 2), (vlb.PREC_FP32, 2), (vlb.PREC_MIXED, 3)])
+def test_batch_matches_single_bakes(ctx, batch_world, precision, lmax):
+    w = batch_world
+    plist = [_job_params(w, j, lmax, precision) for j in w["jobs"]]
+    ref = _singles(ctx, w, plist)
+    batch_p = plist[0]
+    jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
+    outs = ctx.bake_batch(jobs, batch_p)
+    for i, (a, b) in enumerate(zip(outs, ref)):
+        assert a.shape == b.shape
+        assert np.array_equal(a, b), (i, np.abs(a - b).max())
+
+
+def test_batch_schedule_and_graph_invariance(ctx, batch_world):
+    import torch
+
+    w = batch_world
+    plist = [_job_params(w, j, 2, vlb.PREC_MIXED) for j in w["jobs"]]
+    ref = _singles(ctx, w, plist)
+    jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
+    for dpw in (1, 8, 64, 4096):
+        for order in (0, 1):
+            outs = ctx.bake_batch(jobs, plist[0], vlb.BatchSchedule(dpw, order, 0))
+            assert all(np.array_equal(a, b) for a, b in zip(outs, ref)), (dpw, order)
+    # same shape three times: direct, capture + replay, replay
+    for _ in range(3):
+        outs = ctx.bake_batch(jobs, plist[0], vlb.BatchSchedule(16, 1, 1))
+        assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
+    # device outputs and device probes (scattered by the kernel), mixed with host ones
+    djobs, douts = [], []
+    for k, (j, p) in enumerate(zip(w["jobs"], plist)):
+        n = len(j["probes"])
+        if k % 2 == 0:
+            o = torch.empty((n, 9, 3), dtype=torch.float32, device="cuda")
+            pr = torch.from_numpy(j["probes"]).cuda() if n else j["probes"]
+        else:
+            o, pr = None, j["probes"]
+        djobs.append((j["scene"], pr, o, p))
+    for _ in range(3):
+        outs = ctx.bake_batch(djobs, plist[0], vlb.BatchSchedule(16, 1, 1))
+        torch.cuda.synchronize()
+        for a, b in zip(outs, ref):
+            a = a.cpu().numpy() if hasattr(a, "cpu") else a
+            assert np.array_equal(a, b)
+
+
+def test_batch_autotune(ctx, batch_world):
+    w = batch_world
+    plist = [_job_params(w, j, 2, vlb.PREC_MIXED) for j in w["jobs"]]
+    ref = _singles(ctx, w, plist)
+    jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
+    sched, ms = ctx.batch_autotune(jobs, plist[0], reps=1)
+    assert sched.dirs_per_item in (8, 16, 32, 64, 128) and sched.cost_order in (0, 1) and ms > 0
+    for _ in range(3):  # the tuned schedule, graph on
+        outs = ctx.bake_batch(jobs, plist[0])
+        assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
+
+
+def test_batch_job_vs_oracle(ctx, batch_world):
+    """One batched job (300 boxes, 33 probes) against the FP64 oracle, FP32 path."""
+    w = batch_world
+    plist = [_job_params(w, j, 2, vlb.PREC_FP32) for j in w["jobs"]]
+    jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
+    outs = ctx.bake_batch(jobs, plist[0])
+    j = w["jobs"][3]
+    d32, wt = O.dirs_fibonacci(j["S"])
+    B = O.basis_matrix(d32.astype(np.float64), wt, 2)
+    orc = O.Scene(j["pos"], j["idx"], j["alb"])
+    sky = vlb.synth_cubemap(5, 32)
+    sh, hit, vis, rad = ctx.bake(j["scene"], j["probes"], plist[3], debug=True)
+    assert np.array_equal(outs[3], sh)
+    rep = orc.bake(j["probes"], d32, B, j["sun"], sky=sky, sky_n=32, force_hit=hit, force_vis=vis)
+    assert parity.per_probe_rel(outs[3], rep).max() < parity.SH_TOL
+
+
+def test_batch_invalid(ctx, batch_world):
+    w = batch_world
+    j = w["jobs"][0]
+    p2 = _job_params(w, j, 2, vlb.PREC_MIXED)
+    p3 = _job_params(w, j, 3, vlb.PREC_MIXED)
+    with pytest.raises(vlb.VlbError) as e:
+        ctx.bake_batch([(j["scene"], j["probes"], None, p3)], p2)
+    assert e.value.status == vlb.ERR_INVALID
+    pf = _job_params(w, j, 2, vlb.PREC_FP32)
+    with pytest.raises(vlb.VlbError):
+        ctx.bake_batch([(j["scene"], j["probes"], None, pf)], p2)
+    assert ctx.bake_batch([], p2) == []
+    # FUSED bakes as FP32 in a batch
+    pu = _job_params(w, j, 2, vlb.PREC_FUSED)
+    a = ctx.bake_batch([(j["scene"], j["probes"], None)], pu)[0]
+    b = ctx.bake(j["scene"], j["probes"], _job_params(w, j, 2, vlb.PREC_FP32))
+    assert np.array_equal(a, b)

@@ -233,10 +233,11 @@ __global__ void k_probe_codes(const float* __restrict__ probes, uint32_t n, floa
 // instead of ten for the probe counts of a typical bake request.
 constexpr uint32_t kSmallSort = 16384;
 
-__global__ void __launch_bounds__(1024) k_probe_order_small(const float* __restrict__ probes, uint32_t n, float lox,
-                                                            float loy, float loz, float sx, float sy, float sz,
-                                                            uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
-                                                            uint32_t* order) {
+// The whole sort by one CTA of 1024 threads (any n; one launch for up to
+// kSmallSort probes, one CTA per job in the batched bake).
+__device__ __forceinline__ void probe_sort_cta(const float* __restrict__ probes, uint32_t n, float lox, float loy,
+                                               float loz, float sx, float sy, float sz, uint32_t* ka, uint32_t* va,
+                                               uint32_t* kb, uint32_t* vb, uint32_t* order) {
   constexpr int W = 32;
   __shared__ uint32_t base[256];
   __shared__ uint32_t wcnt[W][256];
@@ -310,6 +311,30 @@ __global__ void __launch_bounds__(1024) k_probe_order_small(const float* __restr
       __syncthreads();
     }
   }
+}
+
+__global__ void __launch_bounds__(1024) k_probe_order_small(const float* __restrict__ probes, uint32_t n, float lox,
+                                                            float loy, float loz, float sx, float sy, float sz,
+                                                            uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
+                                                            uint32_t* order) {
+  probe_sort_cta(probes, n, lox, loy, loz, sx, sy, sz, ka, va, kb, vb, order);
+}
+
+__global__ void __launch_bounds__(1024) k_probe_order_batch(const BakeJobDev* __restrict__ jobs) {
+  const BakeJobDev& j = jobs[blockIdx.x];
+  const uint32_t n = j.nprobes;
+  float s[3];
+  for (int i = 0; i < 3; ++i) {
+    const float e = j.bounds[3 + i] - j.bounds[i];
+    s[i] = e > 0.f ? 256.0f / e : 0.f;
+  }
+  uint32_t* sc = j.sort_scratch;  // 4 arrays of n
+  probe_sort_cta(j.probes, n, j.bounds[0], j.bounds[1], j.bounds[2], s[0], s[1], s[2], sc, sc + n, sc + 2 * size_t(n),
+                 sc + 3 * size_t(n), j.order);
+}
+
+void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s) {
+  if (njobs) k_probe_order_batch<<<njobs, 1024, 0, s>>>(jobs);
 }
 
 size_t probe_order_scratch_bytes(uint32_t n) {

@@ -238,9 +238,11 @@ struct Shaded {
 };
 
 // One sample for the whole warp: primary packet, shading, shadow packet.
-template <bool COUNT>
-__device__ __forceinline__ Shaded trace_sample(const TraceArgs& a, bool valid, float ox, float oy, float oz,
-                                               const float4 d, Work& w) {
+// A: any type with the scene and shading fields of TraceArgs (nodes, tris,
+// albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
+template <bool COUNT, class A>
+__device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox, float oy, float oz, const float4 d,
+                                               Work& w) {
   RayCtx ray;
   make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
   bool act = valid;
@@ -428,6 +430,81 @@ static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
 void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
   if (a.counters) launch<0, 1, true>(a, num_sms, s);
   else launch<0, 1, false>(a, num_sms, s);
+}
+
+// Batched bake: the same packet tracing, with work items numbered across all
+// jobs (job j owns items [item_begin, item_begin + packets * chunks)); a warp
+// finds its job by binary search over the item ranges and traces that job's
+// scene.  Radiance goes to the job's rows of its direction set's tile.
+__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobDev* __restrict__ jobs, uint32_t njobs,
+                                                               uint32_t total, uint32_t* counter) {
+  const uint32_t lane = threadIdx.x & 31;
+  Work w;
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1u);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= total) break;
+    uint32_t lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (__ldg(&jobs[mid].item_begin) <= item) lo = mid; else hi = mid - 1;
+    }
+    const BakeJobDev& j = jobs[lo];
+    const uint32_t npg = (j.nprobes + 31) / 32;
+    const uint32_t li = item - j.item_begin;
+    const uint32_t chunk = li / npg, pg = li - chunk * npg;
+    const uint32_t slot = pg * 32 + lane;
+    const bool valid = slot < j.nprobes;
+    const uint32_t p = valid ? j.order[slot] : 0;
+    const float ox = valid ? j.probes[3 * size_t(p)] : 0.f, oy = valid ? j.probes[3 * size_t(p) + 1] : 0.f,
+                oz = valid ? j.probes[3 * size_t(p) + 2] : 0.f;
+    const uint32_t s0 = min(j.S, chunk * j.dpw), s1 = min(j.S, s0 + j.dpw);
+    for (uint32_t t = s0; t < s1; ++t) {
+      const uint32_t s = __ldg(j.dir_order + t);
+      const Shaded o = trace_sample<false>(j, valid, ox, oy, oz, __ldg(j.dirs + s), w);
+      if (!valid) continue;
+      const size_t row = size_t(p) * 3;
+      if (j.radiance) {
+        j.radiance[row * j.S + s] = o.r;
+        j.radiance[(row + 1) * j.S + s] = o.g;
+        j.radiance[(row + 2) * j.S + s] = o.b;
+      } else {
+        j.radiance_bf16[row * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
+        j.radiance_bf16[(row + 1) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
+        j.radiance_bf16[(row + 2) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
+      }
+    }
+  }
+}
+
+void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_items, uint32_t* counter,
+                        int num_sms, cudaStream_t s) {
+  if (!total_items || !njobs) return;
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch, kTraceThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t ctas = std::min<uint64_t>((uint64_t(total_items) + kTraceWarps - 1) / kTraceWarps,
+                                           uint64_t(num_sms) * per_sm);
+  k_trace_batch<<<uint32_t(ctas), kTraceThreads, 0, s>>>(jobs, njobs, total_items, counter);
+}
+
+__global__ void k_scatter_rows(const float* __restrict__ src, float* const* __restrict__ dst,
+                               const uint32_t* __restrict__ src_probe0, const uint32_t* __restrict__ nprobes,
+                               uint32_t K) {
+  const uint32_t jb = blockIdx.y;
+  const size_t n = size_t(nprobes[jb]) * K * 3;
+  const float* sp = src + size_t(src_probe0[jb]) * K * 3;
+  float* dp = dst[jb];
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    dp[i] = sp[i];
+}
+
+void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
+                         uint32_t njobs, uint32_t K, cudaStream_t s) {
+  if (njobs) k_scatter_rows<<<dim3(16, njobs), 256, 0, s>>>(src, dst, src_probe0, nprobes, K);
 }
 
 void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s) {

@@ -369,6 +369,7 @@ void vlb_ctx_destroy(vlb_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   drain_profile(ctx);
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   for (auto& kv : ctx->cube_sa) cudaFree(kv.second);
   for (auto& kv : ctx->cube_bt) cudaFree(kv.second);
@@ -817,19 +818,27 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
 
 // Common part of a bake launch: validated parameters -> trace arguments,
 // probes staged on the device and sorted into spatially compact packets.
-static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
-                                const vlb_bake_params* p, vlbk::TraceArgs* out) {
+// Checks the parameters of one bake; *sun_len gets |sun_dir| (FP64).
+static vlb_status check_params(vlb_ctx* ctx, const vlb_scene* scene, const vlb_bake_params* p, double* sun_len) {
   if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
   if (scene->ctx != ctx || p->dirs->ctx != ctx || (p->sky && p->sky->ctx != ctx))
     return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
   if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
   if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
-  if (!probe_xyz) return fail(ctx, VLB_ERR_INVALID, "null probes");
   const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
                               double(p->sun_dir[2]) * p->sun_dir[2]);
   if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
   if (!(p->tmax > p->tmin) || p->tmin < 0.f) return fail(ctx, VLB_ERR_INVALID, "bad ray interval");
-  vlb_status st;
+  *sun_len = sl;
+  return VLB_OK;
+}
+
+static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                                const vlb_bake_params* p, vlbk::TraceArgs* out) {
+  double sl = 0.0;
+  vlb_status st = check_params(ctx, scene, p, &sl);
+  if (st) return st;
+  if (!probe_xyz) return fail(ctx, VLB_ERR_INVALID, "null probes");
   const void* dprobes;
   if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
   void *order, *oscr;
@@ -964,6 +973,327 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
   out[4] = h[3];
   out[5] = 0;
   return VLB_OK;
+}
+
+// ---- batched bakes ---------------------------------------------------------------------------
+namespace {
+
+struct BatchJob {
+  uint32_t idx;               // caller's job index
+  const vlb_bake_params* p;   // effective parameters
+  double sun_len;
+  uint32_t nprobes, S, group;
+  uint64_t row0;              // first row of the concatenated output (direction sets contiguous)
+  double cost;
+};
+
+struct BatchGroup {
+  const vlb_dirset* dirs;
+  uint64_t row0, rows;
+  size_t tile_off;            // bytes into the batch tile (256-byte aligned)
+};
+
+struct BatchPlan {
+  std::vector<BatchJob> jobs;     // non-empty jobs, caller order
+  std::vector<BatchGroup> groups;
+  uint64_t rows = 0;
+  size_t tile_bytes = 0, host_probe_bytes = 0;
+  uint32_t K = 0;
+  bool bf16 = false;
+};
+
+uint32_t batch_prec(uint32_t p) { return p == VLB_PREC_MIXED ? VLB_PREC_MIXED : VLB_PREC_FP32; }
+
+// Device buffers of one batch (context scratch, allocated before any launch
+// so that the launch sequence can be captured).
+struct BatchBufs {
+  float* probes;       // packed host-side probes
+  uint32_t* order;     // rows
+  uint32_t* sort;      // 4 x rows
+  uint8_t* tile;
+  float* out;          // rows x V
+  uint8_t* meta;       // job table + scatter arrays
+  uint32_t* counter;
+  size_t table_bytes, dst_off, p0_off, np_off;
+  uint32_t ndev_out;   // jobs whose output is device memory (scattered by a kernel)
+};
+
+}  // namespace
+
+static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
+                             BatchPlan* pl) {
+  if (!params) return fail(ctx, VLB_ERR_INVALID, "null batch params");
+  if (!jobs && njobs) return fail(ctx, VLB_ERR_INVALID, "null job array");
+  if (params->lmax != 2 && params->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", params->lmax);
+  if (params->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", params->precision);
+  pl->K = k_of(params->lmax);
+  pl->bf16 = batch_prec(params->precision) == VLB_PREC_MIXED;
+  for (uint32_t i = 0; i < njobs; ++i) {
+    const vlb_bake_job& j = jobs[i];
+    const vlb_bake_params* p = j.params ? j.params : params;
+    BatchJob b{};
+    vlb_status st = check_params(ctx, j.scene, p, &b.sun_len);
+    if (st) return fail(ctx, st, "job %u: %s", i, ctx->err.c_str());
+    if (p->lmax != params->lmax || batch_prec(p->precision) != batch_prec(params->precision))
+      return fail(ctx, VLB_ERR_INVALID, "job %u: lmax and precision must equal the batch's", i);
+    if (j.nprobes == 0) continue;
+    if (!j.probe_xyz || !j.out) return fail(ctx, VLB_ERR_INVALID, "job %u: null probes or output", i);
+    b.idx = i; b.p = p; b.nprobes = j.nprobes; b.S = p->dirs->n;
+    b.cost = double(j.nprobes) * b.S * std::log2(double(j.scene->ntris) + 2.0);
+    uint32_t g = 0;
+    while (g < pl->groups.size() && pl->groups[g].dirs != p->dirs) ++g;
+    if (g == pl->groups.size()) pl->groups.push_back({p->dirs, 0, 0, 0});
+    b.group = g;
+    pl->groups[g].rows += j.nprobes;
+    if (!is_device_ptr(j.probe_xyz)) pl->host_probe_bytes += (size_t(j.nprobes) * 12 + 15) / 16 * 16;
+    pl->jobs.push_back(b);
+  }
+  const size_t esz = pl->bf16 ? 2 : 4;
+  for (auto& g : pl->groups) {
+    g.row0 = pl->rows;
+    pl->rows += g.rows;
+    g.tile_off = pl->tile_bytes;
+    pl->tile_bytes += (size_t(g.rows) * 3 * g.dirs->n * esz + 255) / 256 * 256;
+    g.rows = 0;  // reused below as the running row
+  }
+  for (auto& b : pl->jobs) {
+    auto& g = pl->groups[b.group];
+    b.row0 = g.row0 + g.rows;
+    g.rows += b.nprobes;
+  }
+  if (pl->rows > 0xFFFFFFFFull / 16) return fail(ctx, VLB_ERR_INVALID, "batch too large (%llu probes)",
+                                                   (unsigned long long)pl->rows);
+  return VLB_OK;
+}
+
+// The device work of a batch on ctx->stream (capturable: no allocation, no
+// synchronisation).
+static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBufs& bb, uint32_t ntable,
+                                uint32_t total_items) {
+  const uint32_t V = 3 * pl.K;
+  const auto* table = reinterpret_cast<const vlbk::BakeJobDev*>(bb.meta);
+  VLB_CUDA(ctx, cudaMemsetAsync(bb.counter, 0, 4, ctx->stream));
+  {
+    KScope k(ctx, "probe_order_batch");
+    vlbk::launch_probe_order_batch(table, ntable, ctx->stream);
+  }
+  {
+    KScope k(ctx, "trace_batch");
+    vlbk::launch_trace_batch(table, ntable, total_items, bb.counter, ctx->num_sms, ctx->stream);
+  }
+  for (const auto& g : pl.groups) {
+    float* out = bb.out + g.row0 * V;
+    const uint32_t n = uint32_t(g.rows);
+    if (pl.bf16) {
+      vlb_status st = project_bf16(ctx, reinterpret_cast<const uint16_t*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out);
+      if (st) return st;
+    } else {
+      KScope k(ctx, "project_f32");
+      vlbk::launch_project_f32(reinterpret_cast<const float*>(bb.tile + g.tile_off), n, g.dirs->n,
+                               g.dirs->d_basis16, pl.K, out, ctx->stream);
+    }
+  }
+  if (bb.ndev_out) {
+    KScope k(ctx, "scatter_rows");
+    vlbk::launch_scatter_rows(bb.out, reinterpret_cast<float* const*>(bb.meta + bb.dst_off),
+                              reinterpret_cast<const uint32_t*>(bb.meta + bb.p0_off),
+                              reinterpret_cast<const uint32_t*>(bb.meta + bb.np_off), bb.ndev_out, pl.K, ctx->stream);
+  }
+  return VLB_OK;
+}
+
+static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
+                            const vlb_batch_schedule& sc) {
+  BatchPlan pl;
+  vlb_status st = batch_plan(ctx, jobs, njobs, params, &pl);
+  if (st) return st;
+  if (pl.jobs.empty()) return VLB_OK;
+  const uint32_t K = pl.K, V = 3 * K;
+  const uint32_t ntable = uint32_t(pl.jobs.size());
+  // job table order: costliest first (or caller order)
+  std::vector<uint32_t> ord(ntable);
+  for (uint32_t i = 0; i < ntable; ++i) ord[i] = i;
+  if (sc.cost_order)
+    std::stable_sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return pl.jobs[a].cost > pl.jobs[b].cost; });
+  uint32_t ndev_out = 0;
+  for (const auto& b : pl.jobs) ndev_out += is_device_ptr(jobs[b.idx].out) ? 1 : 0;
+  BatchBufs bb{};
+  bb.table_bytes = (size_t(ntable) * sizeof(vlbk::BakeJobDev) + 255) / 256 * 256;
+  bb.dst_off = bb.table_bytes;
+  bb.p0_off = bb.dst_off + size_t(ndev_out) * 8;
+  bb.np_off = bb.p0_off + size_t(ndev_out) * 4;
+  bb.ndev_out = ndev_out;
+  const size_t meta_bytes = bb.np_off + size_t(ndev_out) * 4;
+  void *probes = nullptr, *order, *sort, *tile, *out, *meta, *counter;
+  if ((pl.host_probe_bytes && (st = scratch(ctx, "batch_probes", pl.host_probe_bytes, &probes))) ||
+      (st = scratch(ctx, "batch_order", pl.rows * 4, &order)) ||
+      (st = scratch(ctx, "batch_sort", pl.rows * 16, &sort)) ||
+      (st = scratch(ctx, "batch_tile", pl.tile_bytes, &tile)) ||
+      (st = scratch(ctx, "batch_out", pl.rows * V * 4, &out)) ||
+      (st = scratch(ctx, "batch_meta", meta_bytes, &meta)) ||
+      (st = scratch(ctx, "batch_counter", 256, &counter)))
+    return st;
+  bb.probes = static_cast<float*>(probes); bb.order = static_cast<uint32_t*>(order);
+  bb.sort = static_cast<uint32_t*>(sort); bb.tile = static_cast<uint8_t*>(tile); bb.out = static_cast<float*>(out);
+  bb.meta = static_cast<uint8_t*>(meta); bb.counter = static_cast<uint32_t*>(counter);
+
+  // stage host probes, build the job table
+  const size_t esz = pl.bf16 ? 2 : 4;
+  uint64_t warp_rays = 0;
+  for (const auto& b : pl.jobs) warp_rays += (uint64_t(b.nprobes) + 31) / 32 * b.S;
+  uint32_t dpw = sc.dirs_per_item;
+  if (!dpw) {
+    const uint64_t target = 8ull * 32 * uint64_t(ctx->num_sms);
+    dpw = uint32_t(std::min<uint64_t>(32, std::max<uint64_t>(1, warp_rays / target)));
+  }
+  auto& table = ctx->batch_table;
+  table.assign(ntable, vlbk::BakeJobDev{});
+  size_t poff = 0;
+  uint64_t items = 0;
+  for (uint32_t t = 0; t < ntable; ++t) {
+    const BatchJob& b = pl.jobs[ord[t]];
+    const vlb_bake_job& j = jobs[b.idx];
+    const vlb_bake_params* p = b.p;
+    const BatchGroup& g = pl.groups[b.group];
+    vlbk::BakeJobDev& d = table[t];
+    d.nodes = j.scene->nodes; d.tris = j.scene->tris; d.albedo = j.scene->albedo; d.ntris = j.scene->ntris;
+    d.tmin = p->tmin; d.tmax = p->tmax; d.bias = p->shadow_bias;
+    d.sun = make_float3(float(p->sun_dir[0] / b.sun_len), float(p->sun_dir[1] / b.sun_len),
+                        float(p->sun_dir[2] / b.sun_len));
+    d.sun_scale = float(double(p->sun_intensity) / kPi);
+    d.sky = p->sky ? p->sky->d_texels : nullptr; d.sky_n = p->sky ? p->sky->n : 0;
+    d.err = ctx->d_err;
+    if (is_device_ptr(j.probe_xyz)) {
+      d.probes = j.probe_xyz;
+    } else {
+      float* dst = reinterpret_cast<float*>(static_cast<uint8_t*>(probes) + poff);
+      VLB_CUDA(ctx, cudaMemcpyAsync(dst, j.probe_xyz, size_t(b.nprobes) * 12, cudaMemcpyHostToDevice, ctx->stream));
+      ctx->host_inputs_pending = true;
+      d.probes = dst;
+      poff += (size_t(b.nprobes) * 12 + 15) / 16 * 16;
+    }
+    d.order = bb.order + b.row0;
+    d.nprobes = b.nprobes;
+    d.dirs = p->dirs->d_dirs; d.dir_order = p->dirs->d_order; d.S = b.S;
+    uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
+    if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
+    else d.radiance = reinterpret_cast<float*>(rad);
+    d.dpw = std::min(dpw, b.S);
+    d.chunks = (b.S + d.dpw - 1) / d.dpw;
+    d.item_begin = uint32_t(items);
+    items += (uint64_t(b.nprobes) + 31) / 32 * d.chunks;
+    for (int a = 0; a < 6; ++a) d.bounds[a] = j.scene->bounds[a];
+    d.sort_scratch = bb.sort + 4 * b.row0;
+  }
+  if (items > 0xFFFFFFFFull) return fail(ctx, VLB_ERR_INVALID, "batch has too many work items");
+  auto& meta_h = ctx->batch_meta;
+  meta_h.assign(meta_bytes, 0);
+  std::memcpy(meta_h.data(), table.data(), table.size() * sizeof(vlbk::BakeJobDev));
+  {
+    uint32_t k = 0;
+    for (const auto& b : pl.jobs) {
+      float* o = jobs[b.idx].out;
+      if (!is_device_ptr(o)) continue;
+      const uint32_t p0 = uint32_t(b.row0), np = b.nprobes;
+      std::memcpy(meta_h.data() + bb.dst_off + 8 * k, &o, 8);
+      std::memcpy(meta_h.data() + bb.p0_off + 4 * k, &p0, 4);
+      std::memcpy(meta_h.data() + bb.np_off + 4 * k, &np, 4);
+      ++k;
+    }
+  }
+  VLB_CUDA(ctx, cudaMemcpyAsync(meta, meta_h.data(), meta_bytes, cudaMemcpyHostToDevice, ctx->stream));
+
+  // shape key: everything the captured launches bake in as parameters
+  std::vector<uint64_t> key = {ntable, uint64_t(items), dpw, pl.bf16, K, ndev_out, uint64_t(uintptr_t(tile)),
+                               uint64_t(uintptr_t(out)), uint64_t(uintptr_t(meta)), uint64_t(uintptr_t(counter)),
+                               uint64_t(ctx->num_sms)};
+  for (const auto& g : pl.groups) {
+    key.push_back(uint64_t(uintptr_t(g.dirs)));
+    key.push_back(g.row0); key.push_back(g.rows); key.push_back(g.tile_off);
+  }
+  const bool same = ctx->batch_key == key;
+  if (!same) {
+    if (ctx->batch_exec) { cudaGraphExecDestroy(ctx->batch_exec); ctx->batch_exec = nullptr; }
+    ctx->batch_key = key;
+  }
+  if (sc.graph && same) {
+    if (!ctx->batch_exec) {
+      const bool prof = ctx->profiling;
+      const uint64_t l0 = ctx->launches;
+      ctx->profiling = false;
+      cudaGraph_t g = nullptr;
+      VLB_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items));
+      const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      ctx->profiling = prof;
+      ctx->batch_graph_kernels = uint32_t(ctx->launches - l0);
+      ctx->launches = l0;
+      if (st) { if (g) cudaGraphDestroy(g); return st; }
+      if (e != cudaSuccess) { cudaGetLastError(); return cuda_fail(ctx, e, "batch graph capture"); }
+      const cudaError_t ei = cudaGraphInstantiate(&ctx->batch_exec, g, 0ull);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) { ctx->batch_exec = nullptr; return cuda_fail(ctx, ei, "batch graph instantiate"); }
+    }
+    KScope k(ctx, "bake_batch_graph", int(ctx->batch_graph_kernels));
+    VLB_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, ctx->stream));
+  } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items)))) {
+    return st;
+  }
+  bool host_out = false;
+  for (const auto& b : pl.jobs) {
+    float* o = jobs[b.idx].out;
+    if (is_device_ptr(o)) continue;
+    host_out = true;
+    VLB_CUDA(ctx, cudaMemcpyAsync(o, bb.out + b.row0 * V, size_t(b.nprobes) * V * 4, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+  }
+  return finish(ctx, host_out);
+}
+
+vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
+                          const vlb_batch_schedule* sched) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  vlb_batch_schedule sc = sched ? *sched : ctx->batch_sched;
+  if (sc.dirs_per_item > 4096) return fail(ctx, VLB_ERR_INVALID, "dirs_per_item %u > 4096", sc.dirs_per_item);
+  return batch_run(ctx, jobs, njobs, params, sc);
+}
+
+vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
+                              uint32_t reps, vlb_batch_schedule* best, float* best_ms) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (reps == 0) reps = 1;
+  const uint32_t dpws[] = {8, 16, 32, 64, 128};
+  cudaEvent_t e0, e1;
+  VLB_CUDA(ctx, cudaEventCreate(&e0));
+  VLB_CUDA(ctx, cudaEventCreate(&e1));
+  vlb_batch_schedule win{0, 1, 1};
+  float win_ms = -1.f;
+  vlb_status st = VLB_OK;
+  for (uint32_t order = 0; order < 2 && !st; ++order) {
+    for (uint32_t dpw : dpws) {
+      const vlb_batch_schedule sc{dpw, order, 0};
+      if ((st = batch_run(ctx, jobs, njobs, params, sc))) break;  // warm-up
+      cudaEventRecord(e0, ctx->stream);
+      for (uint32_t r = 0; r < reps && !st; ++r) st = batch_run(ctx, jobs, njobs, params, sc);
+      cudaEventRecord(e1, ctx->stream);
+      if (st) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) { st = cuda_fail(ctx, cudaGetLastError(), "autotune timing"); break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= float(reps);
+      if (win_ms < 0.f || ms < win_ms) { win_ms = ms; win = {dpw, order, 1}; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  ctx->batch_sched = win;
+  ctx->batch_tuned = true;
+  if (best) *best = win;
+  if (best_ms) *best_ms = win_ms;
+  return finish(ctx, true);
 }
 
 // ---- projection / reconstruction --------------------------------------------------------

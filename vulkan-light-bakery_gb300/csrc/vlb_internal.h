@@ -154,6 +154,45 @@ void plan_trace(TraceArgs& a, int num_sms, bool fused);
 void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s);
 void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s);
 
+// ---- batched bakes: many jobs (scene, probes, direction set) in one launch -------
+struct BakeJobDev {
+  // scene and shading (the fields trace_sample reads)
+  const float4* nodes;
+  const float4* tris;
+  const float4* albedo;
+  uint32_t ntris;
+  float tmin, tmax, bias;
+  float3 sun;
+  float sun_scale;
+  const float* sky;
+  uint32_t sky_n;
+  int* err;
+  // probes and directions
+  const float* probes;    // device nprobes*3
+  uint32_t* order;        // device nprobes: packet slot -> probe (written by the batched sort)
+  uint32_t nprobes;
+  const float4* dirs;
+  const uint32_t* dir_order;
+  uint32_t S;
+  // this job's rows of its direction set's radiance tile
+  float* radiance;
+  uint16_t* radiance_bf16;
+  // work items [item_begin, item_begin + packets * chunks), chunk-major
+  uint32_t item_begin, chunks, dpw;
+  // probe sort: bounds for the Morton codes, 4 scratch arrays of nprobes
+  float bounds[6];
+  uint32_t* sort_scratch;
+};
+// One CTA per job: Morton order of each job's probes into job.order.
+void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s);
+// Persistent trace over all jobs' items (tile mode), counter zeroed before.
+void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_items, uint32_t* counter,
+                        int num_sms, cudaStream_t s);
+// Copies job j's rows of a projected group output to its own output:
+// dst[j] <- src + src_row0[j]*K*3 floats, nprobes[j]*K*3 floats.
+void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
+                         uint32_t njobs, uint32_t K, cudaStream_t s);
+
 }  // namespace vlbk
 
 // ---- host objects behind the opaque handles ------------------------------------
@@ -176,6 +215,15 @@ struct vlb_ctx {
   std::map<std::string, Buf> scratch;
   std::map<uint32_t, float*> cube_sa;  // solid-angle tables by face size
   std::map<uint64_t, float4*> cube_bt;  // weighted-basis tables by (face size << 8 | lmax)
+  // batched bakes: the shape key of the last batch, its captured graph (made
+  // on the second call with that key) and the tuned schedule
+  std::vector<uint64_t> batch_key;
+  cudaGraphExec_t batch_exec = nullptr;
+  uint32_t batch_graph_kernels = 0;
+  std::vector<vlbk::BakeJobDev> batch_table;  // host copy of the job table
+  std::vector<uint8_t> batch_meta;             // job table + scatter arrays, uploaded each call
+  bool batch_tuned = false;
+  vlb_batch_schedule batch_sched{0, 1, 1};
 };
 
 struct vlb_scene {

@@ -51,6 +51,15 @@ class BakeDebug(C.Structure):
     _fields_ = [("hit_tri", C.c_void_p), ("shadow", C.c_void_p), ("radiance", C.c_void_p)]
 
 
+class BakeJob(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("probe_xyz", C.c_void_p), ("nprobes", C.c_uint32),
+                ("params", C.c_void_p), ("out", C.c_void_p)]
+
+
+class BatchSchedule(C.Structure):
+    _fields_ = [("dirs_per_item", C.c_uint32), ("cost_order", C.c_uint32), ("graph", C.c_uint32)]
+
+
 def _load() -> C.CDLL:
     if not LIB_PATH.exists():
         raise ImportError(f"libvlb.so not found at {LIB_PATH}; run __graft_entry__.build() first")
@@ -91,6 +100,8 @@ def _load() -> C.CDLL:
         "vlb_bake": (I32, [P, P, P, U32, P, P]),
         "vlb_bake_ex": (I32, [P, P, P, U32, P, P, P]),
         "vlb_bake_trace_stats": (I32, [P, P, P, U32, P, P]),
+        "vlb_bake_batch": (I32, [P, P, U32, P, P]),
+        "vlb_batch_autotune": (I32, [P, P, U32, P, U32, P, P]),
         "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
         "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
         "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
@@ -241,6 +252,23 @@ class Context:
         self.check(lib.vlb_bake_ex(self.h, scene.h, _ptr(probes), n, C.byref(params), _ptr(ret), C.byref(dbg)))
         return ret, hit.reshape(n, S), vis.reshape(n, S), (None if rad is None else rad.reshape(n, S, 3))
 
+    def bake_batch(self, jobs, params: BakeParams, schedule: "BatchSchedule | None" = None):
+        """jobs: list of (scene, probes, out-or-None[, job params]); returns the outputs."""
+        arr, keep, outs = _job_array(jobs, params)
+        self.check(lib.vlb_bake_batch(self.h, arr, len(jobs), C.byref(params),
+                                      None if schedule is None else C.byref(schedule)))
+        del keep
+        return outs
+
+    def batch_autotune(self, jobs, params: BakeParams, reps: int = 2):
+        """Times the candidate schedules; returns (BatchSchedule, ms per batch)."""
+        arr, keep, _ = _job_array(jobs, params)
+        best = BatchSchedule()
+        ms = C.c_float()
+        self.check(lib.vlb_batch_autotune(self.h, arr, len(jobs), C.byref(params), reps, C.byref(best), C.byref(ms)))
+        del keep
+        return best, float(ms.value)
+
     def project(self, radiance, nprobes: int, dirs: "DirSet", lmax: int, dtype: int = DTYPE_F32, out=None):
         K = k_of(lmax)
         ret = out if out is not None else np.empty((nprobes, K, 3), np.float32)
@@ -252,6 +280,25 @@ class Context:
         out = np.empty((h, w, 3), np.float32)
         self.check(lib.vlb_sh_eval_envmap(self.h, _ptr(c), lmax, w, h, scale, _ptr(out)))
         return out
+
+
+def _job_array(jobs, params: BakeParams):
+    """vlb_bake_job[] for (scene, probes, out[, params]) tuples; outputs made when None."""
+    arr = (BakeJob * max(1, len(jobs)))()
+    keep, outs = [], []
+    for i, j in enumerate(jobs):
+        scene, probes, out = j[0], j[1], j[2]
+        jp = j[3] if len(j) > 3 else None
+        if not hasattr(probes, "data_ptr"):
+            probes = _f32(probes).reshape(-1, 3)
+        n = int(probes.shape[0])
+        K = k_of((jp or params).lmax)
+        if out is None:
+            out = np.empty((n, K, 3), np.float32)
+        keep += [probes, out, jp]
+        outs.append(out)
+        arr[i] = BakeJob(getattr(scene.h, "value", scene.h), _ptr(probes), n, None if jp is None else C.addressof(jp), _ptr(out))
+    return arr, keep, outs
 
 
 def params_dirs_count(p: BakeParams) -> int:
