@@ -89,6 +89,43 @@ def test_lmax3_reference_layout_and_radiance(ctx):
     assert parity.per_probe_rel(sh, rep).max() < parity.SH_TOL
 
 
+@pytest.mark.parametrize("nboxes,counts", [(64, (8, 8, 8)), (3000, (3, 3, 3))])
+def test_traversal_modes_agree(ctx, nboxes, counts):
+    """Packet and lane traversal give the same per-ray decisions and radiance,
+    bit for bit (dense probes in a small scene; sparse probes in a large one)."""
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=11, nboxes=nboxes, counts=counts)
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(S)
+    skyh = ctx.sky(sky, 128)
+    res = []
+    for flag in (vlb.BAKE_TRAVERSAL_PACKET, vlb.BAKE_TRAVERSAL_LANE):
+        p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun, sky=skyh)
+        p.flags = flag
+        res.append(ctx.bake(scene, probes, p, debug=True))
+    (sa, ha, va, ra), (sb, hb, vb, rb) = res
+    diff = np.argwhere((ha != hb) | (va != vb))
+    if len(diff):
+        d32, w = O.dirs_fibonacci(S)
+        B = O.basis_matrix(d32.astype(np.float64), w, 2)
+        orc = O.Scene(pos, idx, alb)
+        sel = np.unique(diff[:, 0])[:8]
+        o_sh, o_hit, o_vis, o_edge, o_rad = orc.bake(probes[sel], d32, B, sun, sky=sky, sky_n=128, per_ray=True)
+        for p_, s_ in diff[:12]:
+            if p_ in sel:
+                k = int(np.where(sel == p_)[0][0])
+                print(f"probe {p_} {probes[p_]} dir {s_} {d32[s_]}: packet {ha[p_, s_]}/{va[p_, s_]} lane "
+                      f"{hb[p_, s_]}/{vb[p_, s_]} oracle {o_hit[k, s_]}/{o_vis[k, s_]} edge {o_edge[k, s_]:.3e}")
+    assert len(diff) == 0, f"{len(diff)} of {ha.size} rays differ"
+    assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+    if nboxes > 1000:  # the sparse case against the oracle too
+        d32, w = O.dirs_fibonacci(S)
+        B = O.basis_matrix(d32.astype(np.float64), w, 2)
+        orc = O.Scene(pos, idx, alb)
+        o_sh, o_hit, o_vis, o_edge, o_rad = orc.bake(probes, d32, B, sun, sky=sky, sky_n=128, per_ray=True)
+        cls = parity.classify(orc, probes, d32, sun, hb, vb, o_hit, o_vis, o_edge)
+        assert not cls["unexplained"], cls["unexplained"][:10]
+
+
 def test_empty_scene_sees_sky(ctx):
     sky = vlb.synth_cubemap(4, 32)
     pos = np.zeros((3, 3), np.float32)

@@ -13,7 +13,8 @@
 //   6. bottom-up refit with one atomic counter per internal node (min/max
 //      unions are order independent);
 //   7. packing into the traversal layout: internal node = 4 float4 holding
-//      both children's boxes and references; triangle = 3 float4 (v0 | id,
+//      both children's boxes (widened by a relative 2^-20 so that the box
+//      tests are conservative) and references; triangle = 3 float4 (v0 | id,
 //      e1, e2) in leaf order.
 #include <algorithm>
 
@@ -442,14 +443,34 @@ __global__ void k_refit(const int32_t* __restrict__ parent, const int32_t* __res
   }
 }
 
+// Traversal boxes are the exact boxes widened by (|x| + scene scale) * 2^-20
+// per bound, so that the box tests are conservative: a ray lying in a box's
+// face plane (a zero direction component) or grazing its boundary still
+// enters it, and only the triangle test decides.  The exact boxes stay in
+// `box` (exported and compared with the oracle).
+__device__ __forceinline__ float widen_lo(float x, float scale) {
+  return __fsub_rn(x, __fmul_rn(__fadd_rn(fabsf(x), scale), 0x1p-20f));
+}
+__device__ __forceinline__ float widen_hi(float x, float scale) {
+  return __fadd_rn(x, __fmul_rn(__fadd_rn(fabsf(x), scale), 0x1p-20f));
+}
+
 __global__ void k_pack_nodes(const int32_t* __restrict__ child, const float* __restrict__ box, uint32_t n,
                              float4* __restrict__ nodes) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i + 1 >= n) return;
   const int leaf0 = int(n) - 1;
   const int32_t c0 = child[2 * i], c1 = child[2 * i + 1];
-  const float* b0 = box + 6 * size_t(c0 >= 0 ? c0 : leaf0 + ~c0);
-  const float* b1 = box + 6 * size_t(c1 >= 0 ? c1 : leaf0 + ~c1);
+  const float* r = box;  // root (internal node 0)
+  const float scale = fmaxf(fmaxf(fmaxf(fabsf(r[0]), fabsf(r[1])), fmaxf(fabsf(r[2]), fabsf(r[3]))),
+                            fmaxf(fabsf(r[4]), fabsf(r[5])));
+  const float* p0 = box + 6 * size_t(c0 >= 0 ? c0 : leaf0 + ~c0);
+  const float* p1 = box + 6 * size_t(c1 >= 0 ? c1 : leaf0 + ~c1);
+  float b0[6], b1[6];
+  for (int a = 0; a < 3; ++a) {
+    b0[a] = widen_lo(p0[a], scale); b0[3 + a] = widen_hi(p0[3 + a], scale);
+    b1[a] = widen_lo(p1[a], scale); b1[3 + a] = widen_hi(p1[3 + a], scale);
+  }
   nodes[4 * size_t(i) + 0] = make_float4(b0[0], b0[1], b0[2], b0[3]);
   nodes[4 * size_t(i) + 1] = make_float4(b0[4], b0[5], b1[0], b1[1]);
   nodes[4 * size_t(i) + 2] = make_float4(b1[2], b1[3], b1[4], b1[5]);

@@ -10,10 +10,10 @@
 // address, broadcast to the lanes), every lane tests its own ray, and warp
 // ballots decide which children to visit.  All control flow is warp-uniform.
 // The stack is warp-uniform too, so it lives in registers spread over the
-// lanes (entry i in lane i % 32) and a pop is one shuffle.  A lane's result is
-// exactly its own closest hit -- the warp visits a superset of the nodes the
-// lane needs -- and equal distances resolve to the lower triangle index, so
-// results do not depend on which probes share the packet.
+// lanes (entry i in lane i % 32) and a pop is one shuffle.  A lane tests only
+// the nodes its own box tests admit (one private bit per stack entry), and
+// equal distances resolve to the lower triangle index, so results do not
+// depend on which probes share the packet.
 //
 // Per ray:
 //   closest hit in (tmin, tmax)                    [env_map.rgen:22-26]
@@ -23,6 +23,16 @@
 //   miss: nearest texel of the cubemap sky, or 0   [main.rmiss:37-41]
 // BVH2 nodes hold both children's boxes (4 x float4 = 64 B); triangles are
 // 3 x float4 in leaf order.
+//
+// Lane mode.  When a packet's probes are far apart relative to the
+// geometry (few probes in a large scene) the union of their paths is much
+// longer than any one path, so each lane walks its own path instead (a
+// per-lane stack in local memory, the warp's direction -- and octant -- still
+// shared).  Both modes prune a subtree only when its box entry exceeds the
+// lane's best distance by a relative margin of 2^-12, so a triangle whose
+// computed distance ties or beats the best is never pruned by a rounding of
+// the box test: a lane's result does not depend on the visiting order, hence
+// on the mode or the packet.
 //
 // Scheduling: persistent, independent warps take work items (packet,
 // direction chunk) from an atomic counter -- no CTA-wide barrier, so a warp
@@ -111,11 +121,17 @@ __device__ __forceinline__ float tri_hit(const RayCtx& r, const float4 v0, const
   return (e2.x * qx + e2.y * qy + e2.z * qz) * inv;
 }
 
+// Far limit of the box tests: the best distance so far plus a relative 2^-12.
+__device__ __forceinline__ float prune_limit(float tbest) { return fmaf(tbest, 0x1p-12f, tbest); }
+
 // Warp-uniform stack of up to kTraceStack (64) node references held in two
-// registers per lane: entry i sits in lane i % 32, register i / 32.
+// registers per lane: entry i sits in lane i % 32, register i / 32.  Each
+// lane also keeps one private bit per entry: whether its own box test
+// accepted that subtree.
 struct WarpStack {
   int r0 = 0, r1 = 0, sp = 0;
-  __device__ __forceinline__ void push(int v, uint32_t lane, int* err) {
+  uint64_t want = 0;
+  __device__ __forceinline__ void push(int v, bool mine, uint32_t lane, int* err) {
     if (sp >= kTraceStack) {
       if (lane == 0) atomicAdd(err + kErrStackOverflow, 1);
       return;
@@ -123,10 +139,12 @@ struct WarpStack {
     if (lane == uint32_t(sp & 31)) {
       if (sp < 32) r0 = v; else r1 = v;
     }
+    want = (want & ~(1ull << sp)) | (uint64_t(mine) << sp);
     ++sp;
   }
-  __device__ __forceinline__ int pop() {
+  __device__ __forceinline__ int pop(bool& mine) {
     --sp;
+    mine = (want >> sp) & 1ull;
     return __shfl_sync(kFull, sp < 32 ? r0 : r1, sp & 31);
   }
 };
@@ -135,7 +153,10 @@ struct WarpStack {
 // with ties to the lower triangle id; ANY = true: a lane stops (active =
 // false, best_slot >= 0) at its first hit in (tmin, tbest).  Must be called
 // by all 32 lanes; lanes with active == false only vote "no".  OCT is the
-// packet's (warp-uniform) ray octant.
+// packet's (warp-uniform) ray octant.  A lane tests a node or triangle only
+// inside subtrees its own box tests accepted (`in`), so it visits exactly the
+// nodes its own walk would, in the warp's order: its result does not depend
+// on the other rays of the packet.
 template <int OCT, bool ANY, bool COUNT>
 __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, const float4* __restrict__ nodes,
                                                 const float4* __restrict__ tris, uint32_t ntris, float tmin,
@@ -144,16 +165,19 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
   const uint32_t lane = threadIdx.x & 31;
   WarpStack st;
   int cur = ntris > 1 ? 0 : ~0;
+  bool in = true;
   for (;;) {
+    const bool test = active && in;
     if (cur >= 0) {
-      if constexpr (COUNT) { w.wnodes += lane == 0; w.lnodes += active; }
+      if constexpr (COUNT) { w.wnodes += lane == 0; w.lnodes += test; }
       const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
                    n3 = __ldg(nodes + 4 * cur + 3);
       bool h0 = false, h1 = false;
       float tn0 = 0.f, tn1 = 0.f;
-      if (active) {
-        h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, tbest, &tn0);
-        h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, tbest, &tn1);
+      if (test) {
+        const float lim = prune_limit(tbest);
+        h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
+        h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
       }
       const unsigned b0 = __ballot_sync(kFull, h0), b1 = __ballot_sync(kFull, h1);
       const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
@@ -164,17 +188,18 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
           const unsigned pref0 = __ballot_sync(kFull, h0 && (!h1 || tn0 <= tn1));
           first0 = 2 * __popc(pref0) >= __popc(b0 | b1);
         }
-        st.push(first0 ? c1 : c0, lane, err);
+        st.push(first0 ? c1 : c0, first0 ? h1 : h0, lane, err);
         cur = first0 ? c0 : c1;
+        in = first0 ? h0 : h1;
         continue;
       }
-      if (b0) { cur = c0; continue; }
-      if (b1) { cur = c1; continue; }
+      if (b0) { cur = c0; in = h0; continue; }
+      if (b1) { cur = c1; in = h1; continue; }
     } else {
       if constexpr (COUNT) w.wtris += lane == 0;
       const int slot = ~cur;
       const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
-      if (active) {
+      if (test) {
         const float t = tri_hit(r, v0, e1, e2);
         if (t > tmin) {
           if constexpr (ANY) {
@@ -190,17 +215,70 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
       }
     }
     if (st.sp == 0) break;
-    cur = st.pop();
+    cur = st.pop(in);
   }
 }
 
-// Dispatch on the packet's octant (a warp-uniform branch).
-template <bool ANY, bool COUNT>
+// Per-lane traversal (lane mode): the same tests and tie rule as the packet
+// walk, the lane's own stack (local memory), nearer child first.  Lanes with
+// active == false return at once; no warp collectives.
+template <int OCT, bool ANY, bool COUNT>
+__device__ __forceinline__ void lane_traverse(const RayCtx& r, bool& active, const float4* __restrict__ nodes,
+                                              const float4* __restrict__ tris, uint32_t ntris, float tmin,
+                                              float& tbest, int& best_slot, int& best_id, int* err, Work& w) {
+  if (ntris == 0 || !active) return;
+  int stack[kTraceStack];
+  int sp = 0;
+  int cur = ntris > 1 ? 0 : ~0;
+  for (;;) {
+    if (cur >= 0) {
+      if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+      const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
+                   n3 = __ldg(nodes + 4 * cur + 3);
+      float tn0, tn1;
+      const float lim = prune_limit(tbest);
+      const bool h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
+      const bool h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (h0 && h1) {
+        const bool first0 = tn0 <= tn1;
+        if (sp < kTraceStack) stack[sp++] = first0 ? c1 : c0;
+        else atomicAdd(err + kErrStackOverflow, 1);
+        cur = first0 ? c0 : c1;
+        continue;
+      }
+      if (h0) { cur = c0; continue; }
+      if (h1) { cur = c1; continue; }
+    } else {
+      if constexpr (COUNT) ++w.wtris;
+      const int slot = ~cur;
+      const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
+      const float t = tri_hit(r, v0, e1, e2);
+      if (t > tmin) {
+        if constexpr (ANY) {
+          if (t < tbest) { best_slot = slot; active = false; return; }
+        } else {
+          const int id = __float_as_int(v0.w);
+          if (t < tbest || (t == tbest && best_slot >= 0 && id < best_id)) { tbest = t; best_slot = slot; best_id = id; }
+        }
+      }
+    }
+    if (sp == 0) break;
+    cur = stack[--sp];
+  }
+}
+
+// Dispatch on the packet's octant (a warp-uniform branch) and the mode.
+template <bool ANY, bool COUNT, bool LANE>
 __device__ __forceinline__ void traverse(int oct, const RayCtx& r, bool& active, const float4* __restrict__ nodes,
                                          const float4* __restrict__ tris, uint32_t ntris, float tmin, float& tbest,
                                          int& best_slot, int& best_id, int* err, Work& w) {
-#define VLB_OCT(o) \
-  case o: packet_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot, best_id, err, w); break;
+#define VLB_OCT(o)                                                                                                \
+  case o:                                                                                                         \
+    if constexpr (LANE) lane_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot,       \
+                                                     best_id, err, w);                                            \
+    else packet_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot, best_id, err, w); \
+    break;
   switch (oct) {
     VLB_OCT(0) VLB_OCT(1) VLB_OCT(2) VLB_OCT(3) VLB_OCT(4) VLB_OCT(5) VLB_OCT(6) VLB_OCT(7)
   }
@@ -240,7 +318,7 @@ struct Shaded {
 // One sample for the whole warp: primary packet, shading, shadow packet.
 // A: any type with the scene and shading fields of TraceArgs (nodes, tris,
 // albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
-template <bool COUNT, class A>
+template <bool COUNT, bool LANE, class A>
 __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox, float oy, float oz, const float4 d,
                                                Work& w) {
   RayCtx ray;
@@ -248,7 +326,7 @@ __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox,
   bool act = valid;
   float tb = a.tmax;
   int slot = -1, id = -1;
-  traverse<false, COUNT>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id, a.err,
+  traverse<false, COUNT, LANE>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id, a.err,
                          w);
   Shaded o{0.f, 0.f, 0.f, -1, 2};
   RayCtx sh = ray;
@@ -280,7 +358,7 @@ __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox,
   float stb = a.tmax;
   int sslot = -1, sid = -1;
   // inactive lanes keep their primary ray: the octant comes from the sun, uniform
-  traverse<true, COUNT>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb, sslot,
+  traverse<true, COUNT, LANE>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb, sslot,
                         sid, a.err, w);
   if (need) {
     const bool occ = sslot >= 0;
@@ -326,7 +404,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs a) {
     }
     for (uint32_t t = s0; t < s1; ++t) {
       const uint32_t s = __ldg(a.dir_order + t);  // direction index (caller order)
-      const Shaded o = trace_sample<COUNT>(a, valid, ox, oy, oz, __ldg(a.dirs + s), w);
+      const float4 dv = __ldg(a.dirs + s);
+      const Shaded o = a.lane ? trace_sample<COUNT, true>(a, valid, ox, oy, oz, dv, w)
+                              : trace_sample<COUNT, false>(a, valid, ox, oy, oz, dv, w);
       if constexpr (MODE == 1) {
         const float4* b4 = reinterpret_cast<const float4*>(a.basis16 + size_t(s) * 16);
 #pragma unroll
@@ -462,7 +542,9 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
     const uint32_t s0 = min(j.S, chunk * j.dpw), s1 = min(j.S, s0 + j.dpw);
     for (uint32_t t = s0; t < s1; ++t) {
       const uint32_t s = __ldg(j.dir_order + t);
-      const Shaded o = trace_sample<false>(j, valid, ox, oy, oz, __ldg(j.dirs + s), w);
+      const float4 dv = __ldg(j.dirs + s);
+      const Shaded o = j.lane ? trace_sample<false, true>(j, valid, ox, oy, oz, dv, w)
+                              : trace_sample<false, false>(j, valid, ox, oy, oz, dv, w);
       if (!valid) continue;
       const size_t row = size_t(p) * 3;
       if (j.radiance) {

@@ -23,6 +23,9 @@ namespace {
 
 constexpr double kPiRef = 3.1415926538;  // shaders/sh_common.h:1
 constexpr double kPi = 3.141592653589793;
+// Triangles per probe above which a bake traces in lane mode (measured
+// crossover of the two modes on box scenes: 0.1 to 6 triangles per probe).
+constexpr uint32_t kLaneTrisPerProbe = 1;
 
 vlb_status fail(vlb_ctx* ctx, vlb_status s, const char* fmt, ...) {
   if (ctx) {
@@ -818,6 +821,15 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
 
 // Common part of a bake launch: validated parameters -> trace arguments,
 // probes staged on the device and sorted into spatially compact packets.
+// Traversal mode of one bake: forced by the flags, else lane mode when the
+// scene has many triangles per probe (packets of sparse probes walk long
+// union paths).
+static uint32_t lane_mode(const vlb_scene* scene, uint32_t nprobes, uint32_t flags) {
+  if (flags & VLB_BAKE_TRAVERSAL_LANE) return 1;
+  if (flags & VLB_BAKE_TRAVERSAL_PACKET) return 0;
+  return uint64_t(scene->ntris) > uint64_t(kLaneTrisPerProbe) * nprobes ? 1 : 0;
+}
+
 // Checks the parameters of one bake; *sun_len gets |sun_dir| (FP64).
 static vlb_status check_params(vlb_ctx* ctx, const vlb_scene* scene, const vlb_bake_params* p, double* sun_len) {
   if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
@@ -863,6 +875,7 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
   a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
   a.basis16 = p->dirs->d_basis16; a.K = k_of(p->lmax); a.err = ctx->d_err;
+  a.lane = lane_mode(scene, nprobes, p->flags);
   vlbk::plan_trace(a, ctx->num_sms, p->precision == VLB_PREC_FUSED);
   void* wc;
   if ((st = scratch(ctx, "trace_work", 256, &wc))) return st;
@@ -1178,6 +1191,7 @@ static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njo
     uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
     if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
     else d.radiance = reinterpret_cast<float*>(rad);
+    d.lane = lane_mode(j.scene, b.nprobes, p->flags);
     d.dpw = std::min(dpw, b.S);
     d.chunks = (b.S + d.dpw - 1) / d.dpw;
     d.item_begin = uint32_t(items);

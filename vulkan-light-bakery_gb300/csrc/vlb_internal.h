@@ -141,6 +141,7 @@ struct TraceArgs {
   // dirs_per_warp consecutive directions; persistent warps pull items
   uint32_t dirs_per_warp;
   uint32_t chunks;        // direction chunks per packet
+  uint32_t lane;          // 1: per-lane traversal, 0: packet traversal
   unsigned long long* counters;  // null, or [warp node fetches, warp triangle fetches, shadow rays, lane node tests]
   int* err;
 };
@@ -179,6 +180,7 @@ struct BakeJobDev {
   uint16_t* radiance_bf16;
   // work items [item_begin, item_begin + packets * chunks), chunk-major
   uint32_t item_begin, chunks, dpw;
+  uint32_t lane;          // 1: per-lane traversal, 0: packet traversal
   // probe sort: bounds for the Morton codes, 4 scratch arrays of nprobes
   float bounds[6];
   uint32_t* sort_scratch;
