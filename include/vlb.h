@@ -271,6 +271,70 @@ vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                               uint32_t reps, vlb_batch_schedule* best, float* best_ms);
 
+/* ---- bake service ------------------------------------------------------------
+ * No reference counterpart (the reference bakes once per process,
+ * baker/main.cpp:22-24).  A resident service over the scenes, direction sets
+ * and skies of one context: requests are submitted from any thread, admitted
+ * against a device-memory budget and baked by a worker thread in continuous
+ * batches -- while one batch runs on the GPU the next is assembled from the
+ * requests that arrived meanwhile and queued behind it (vlb_bake_batch
+ * machinery on the service's own stream).  A bake may keep its primary hits
+ * (triangle and distance per ray, 8 bytes); a relight of that bake re-shades
+ * the kept hits with new sun and sky and re-traces only the shadow rays.
+ * Every result is bit-identical to vlb_bake of the same request (a relight:
+ * to vlb_bake of the original probes with the relight's parameters).
+ * While a service runs, its context's objects may be used by other calls on
+ * that context; they must outlive the requests that name them. */
+typedef struct vlb_service vlb_service;
+typedef struct vlb_service_config {
+  uint64_t hbm_budget_bytes; /* device bytes for batches in flight plus kept hits (0: 64 GiB) */
+  uint32_t lmax;             /* 2 or 3, every request */
+  uint32_t precision;        /* VLB_PREC_FP32 or VLB_PREC_MIXED (VLB_PREC_FUSED bakes as FP32) */
+  uint32_t max_batch_probes; /* probes per batch (0: 1,048,576) */
+  uint32_t max_inflight;     /* batches queued on the GPU at once (0: 2) */
+} vlb_service_config;
+typedef struct vlb_request {
+  const vlb_scene* scene;         /* ignored by a relight (the original's) */
+  const float* probe_xyz;         /* nprobes*3 host, copied at submit; ignored by a relight */
+  uint32_t nprobes;               /* ignored by a relight */
+  const vlb_bake_params* params;  /* lmax and precision come from the service; a relight keeps the
+                                     original's direction set, tmin and tmax */
+  uint64_t relight_of;            /* 0: bake; else the ticket of a bake submitted with keep_hits */
+  uint32_t keep_hits;             /* 1: keep this bake's primary hits for relights */
+} vlb_request;
+/* The service's own state lives on ctx's device; ctx must outlive it. */
+vlb_status vlb_service_create(vlb_ctx* ctx, const vlb_service_config* cfg, vlb_service** out);
+/* Finishes the requests already submitted, then stops. */
+void vlb_service_destroy(vlb_service* svc);
+/* VLB_ERR_OOM: the request alone exceeds the budget.  *ticket > 0. */
+vlb_status vlb_service_submit(vlb_service* svc, const vlb_request* req, uint64_t* ticket);
+/* Waits up to timeout_ms (0: only look) for a ticket.  On VLB_OK, out (host,
+ * nprobes x K x 3, may be NULL) gets the result, *latency_ms (may be NULL)
+ * the time from submit to completion, and the ticket's result is released
+ * (its kept hits stay until vlb_service_release or eviction).  VLB_ERR_TIMEOUT:
+ * not done yet.  A failed request returns its error once. */
+vlb_status vlb_service_wait(vlb_service* svc, uint64_t ticket, uint32_t timeout_ms, float* out, double* latency_ms);
+/* Drops the kept hits of a bake (a later relight of it bakes in full). */
+vlb_status vlb_service_release(vlb_service* svc, uint64_t ticket);
+typedef struct vlb_service_stats {
+  uint64_t submitted, completed, failed, batches;
+  uint64_t relights, relights_rebaked; /* relights, and those whose kept hits were gone (baked in full) */
+  uint64_t evictions;                  /* kept-hit sets dropped to admit work */
+  uint64_t probes, rays;               /* completed work */
+  uint64_t bytes_in_use, bytes_peak;   /* budget accounting: batches in flight + kept hits */
+} vlb_service_stats;
+vlb_status vlb_service_stats_read(vlb_service* svc, vlb_service_stats* out);
+/* Message of the calling thread's last failed vlb_service_* call (never NULL). */
+const char* vlb_service_last_error(void);
+/* The admission rule of the service, as a pure host function (no GPU):
+ * requests in queue order with their probe counts and device bytes are cut
+ * into batches, each at most max_batch_probes probes (a larger request goes
+ * alone) and at most budget_bytes (a request over the budget is refused,
+ * batch size 0).  out_batch[i] = index of request i's batch (or UINT32_MAX
+ * if refused); returns the number of batches in *nbatches. */
+vlb_status vlb_service_plan(const uint64_t* probes, const uint64_t* bytes, uint32_t n, uint64_t max_batch_probes,
+                            uint64_t budget_bytes, uint32_t* out_batch, uint32_t* nbatches);
+
 /* ---- projection and reconstruction ----------------------------------------
  * Replaces dispatchBakingKernel / shaders/sh.comp:23-42 for a radiance tile
  * laid out [nprobes][3][S] (S = the direction set's count): out nprobes x K x

@@ -105,3 +105,26 @@ def test_context_creation_fails_cleanly_without_gpu():
         pytest.skip("a GPU is present")
     with pytest.raises(vlb.VlbError):
         vlb.Context(0)
+
+
+def test_service_admission_plan():
+    """The service's batch cut rule (pure host code): FIFO, probe cap, budget,
+    oversize requests refused, a request larger than the cap goes alone."""
+    b, n = vlb.service_plan([10, 20, 30, 5, 100], [1, 2, 3, 1, 50], 40, 10)
+    assert list(b) == [0, 0, 1, 1, -1] and n == 2
+    b, n = vlb.service_plan([100, 1, 1], [1, 1, 1], 40, 10)
+    assert list(b) == [0, 1, 1] and n == 2
+    b, n = vlb.service_plan([1, 1, 1, 1], [4, 4, 4, 4], 1000, 10)
+    assert list(b) == [0, 0, 1, 1] and n == 2
+    b, n = vlb.service_plan([1], [11], 1000, 10)
+    assert list(b) == [-1] and n == 0
+    b, n = vlb.service_plan([], [], 1, 1)
+    assert len(b) == 0 and n == 0
+    rng = np.random.default_rng(4)
+    p = rng.integers(1, 5000, 500)
+    by = rng.integers(1, 1 << 20, 500)
+    b, n = vlb.service_plan(p, by, 16384, 1 << 22)
+    assert np.all(np.diff(b[b >= 0]) >= 0) and b.max() == n - 1  # batches in queue order
+    for k in range(n):  # each batch within the caps, and no batch could take the next request
+        sel = b == k
+        assert by[sel].sum() <= 1 << 22 and (p[sel].sum() <= 16384 or sel.sum() == 1)

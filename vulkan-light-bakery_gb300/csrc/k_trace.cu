@@ -125,27 +125,28 @@ __device__ __forceinline__ float tri_hit(const RayCtx& r, const float4 v0, const
 __device__ __forceinline__ float prune_limit(float tbest) { return fmaf(tbest, 0x1p-12f, tbest); }
 
 // Warp-uniform stack of up to kTraceStack (64) node references held in two
-// registers per lane: entry i sits in lane i % 32, register i / 32.  Each
-// lane also keeps one private bit per entry: whether its own box test
-// accepted that subtree.
+// registers per lane: entry i sits in lane i % 32, register i / 32, together
+// with the ballot of the lanes whose own box test accepted that subtree.
 struct WarpStack {
   int r0 = 0, r1 = 0, sp = 0;
-  uint64_t want = 0;
-  __device__ __forceinline__ void push(int v, bool mine, uint32_t lane, int* err) {
+  unsigned m0 = 0, m1 = 0;
+  __device__ __forceinline__ void push(int v, unsigned lanes, uint32_t lane, int* err) {
     if (sp >= kTraceStack) {
       if (lane == 0) atomicAdd(err + kErrStackOverflow, 1);
       return;
     }
     if (lane == uint32_t(sp & 31)) {
-      if (sp < 32) r0 = v; else r1 = v;
+      if (sp < 32) { r0 = v; m0 = lanes; } else { r1 = v; m1 = lanes; }
     }
-    want = (want & ~(1ull << sp)) | (uint64_t(mine) << sp);
     ++sp;
   }
-  __device__ __forceinline__ int pop(bool& mine) {
+  __device__ __forceinline__ int pop(bool& mine, uint32_t lane) {
     --sp;
-    mine = (want >> sp) & 1ull;
-    return __shfl_sync(kFull, sp < 32 ? r0 : r1, sp & 31);
+    const bool lo = sp < 32;
+    const int v = __shfl_sync(kFull, lo ? r0 : r1, sp & 31);
+    const unsigned m = __shfl_sync(kFull, lo ? m0 : m1, sp & 31);
+    mine = (m >> lane) & 1u;
+    return v;
   }
 };
 
@@ -188,7 +189,7 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
           const unsigned pref0 = __ballot_sync(kFull, h0 && (!h1 || tn0 <= tn1));
           first0 = 2 * __popc(pref0) >= __popc(b0 | b1);
         }
-        st.push(first0 ? c1 : c0, first0 ? h1 : h0, lane, err);
+        st.push(first0 ? c1 : c0, first0 ? b1 : b0, lane, err);
         cur = first0 ? c0 : c1;
         in = first0 ? h0 : h1;
         continue;
@@ -215,7 +216,7 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
       }
     }
     if (st.sp == 0) break;
-    cur = st.pop(in);
+    cur = st.pop(in, lane);
   }
 }
 
@@ -318,16 +319,24 @@ struct Shaded {
 // One sample for the whole warp: primary packet, shading, shadow packet.
 // A: any type with the scene and shading fields of TraceArgs (nodes, tris,
 // albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
+// Primary ray: closest hit -> (slot, id, t); slot -1 on a miss.
 template <bool COUNT, bool LANE, class A>
-__device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox, float oy, float oz, const float4 d,
-                                               Work& w) {
-  RayCtx ray;
-  make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
+__device__ __forceinline__ void primary_hit(const A& a, bool valid, const RayCtx& ray, const float4 d, int& slot,
+                                            int& id, float& tb, Work& w) {
   bool act = valid;
-  float tb = a.tmax;
-  int slot = -1, id = -1;
-  traverse<false, COUNT, LANE>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id, a.err,
-                         w);
+  tb = a.tmax;
+  slot = -1;
+  id = -1;
+  traverse<false, COUNT, LANE>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id,
+                               a.err, w);
+}
+
+// Shading of a primary result: sky on a miss; at a hit the sun shadow ray
+// (any hit) and Lambert.  Called by all 32 lanes (the shadow walk may be a
+// packet walk).
+template <bool COUNT, bool LANE, class A>
+__device__ __forceinline__ Shaded shade_hit(const A& a, bool valid, const RayCtx& ray, float ox, float oy, float oz,
+                                            const float4 d, int slot, int id, float tb, Work& w) {
   Shaded o{0.f, 0.f, 0.f, -1, 2};
   RayCtx sh = ray;
   bool need = false;
@@ -358,8 +367,8 @@ __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox,
   float stb = a.tmax;
   int sslot = -1, sid = -1;
   // inactive lanes keep their primary ray: the octant comes from the sun, uniform
-  traverse<true, COUNT, LANE>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb, sslot,
-                        sid, a.err, w);
+  traverse<true, COUNT, LANE>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb,
+                              sslot, sid, a.err, w);
   if (need) {
     const bool occ = sslot >= 0;
     o.vis = occ ? 0 : 1;
@@ -370,6 +379,20 @@ __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox,
     }
   }
   return o;
+}
+
+// One sample for the whole warp: primary walk, shading, shadow walk.
+// A: any type with the scene and shading fields of TraceArgs (nodes, tris,
+// albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
+template <bool COUNT, bool LANE, class A>
+__device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox, float oy, float oz, const float4 d,
+                                               Work& w) {
+  RayCtx ray;
+  make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
+  int slot, id;
+  float tb;
+  primary_hit<COUNT, LANE>(a, valid, ray, d, slot, id, tb, w);
+  return shade_hit<COUNT, LANE>(a, valid, ray, ox, oy, oz, d, slot, id, tb, w);
 }
 
 // MODE 0: radiance tile (+ optional per-ray debug arrays); MODE 1: fused projection.
@@ -543,8 +566,26 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
     for (uint32_t t = s0; t < s1; ++t) {
       const uint32_t s = __ldg(j.dir_order + t);
       const float4 dv = __ldg(j.dirs + s);
-      const Shaded o = j.lane ? trace_sample<false, true>(j, valid, ox, oy, oz, dv, w)
-                              : trace_sample<false, false>(j, valid, ox, oy, oz, dv, w);
+      const size_t ray_i = size_t(p) * j.S + s;
+      RayCtx ray;
+      make_ray(ray, ox, oy, oz, dv.x, dv.y, dv.z);
+      int slot = -1, id = -1;
+      float tb = j.tmax;
+      if (j.hits_in) {  // relight: the kept primary hit, only the shadow ray is traced
+        if (valid) {
+          const int2 h = __ldg(j.hits_in + ray_i);
+          slot = h.x;
+          tb = __int_as_float(h.y);
+          if (slot >= 0) id = __float_as_int(__ldg(j.tris + 3 * slot).w);
+        }
+      } else if (j.lane) {
+        primary_hit<false, true>(j, valid, ray, dv, slot, id, tb, w);
+      } else {
+        primary_hit<false, false>(j, valid, ray, dv, slot, id, tb, w);
+      }
+      if (j.hits_out && valid) j.hits_out[ray_i] = make_int2(slot, __float_as_int(tb));
+      const Shaded o = j.lane ? shade_hit<false, true>(j, valid, ray, ox, oy, oz, dv, slot, id, tb, w)
+                              : shade_hit<false, false>(j, valid, ray, ox, oy, oz, dv, slot, id, tb, w);
       if (!valid) continue;
       const size_t row = size_t(p) * 3;
       if (j.radiance) {

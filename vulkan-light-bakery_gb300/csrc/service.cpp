@@ -1,0 +1,587 @@
+// service.cpp -- the resident bake service of include/vlb.h (vlb_service_*).
+//
+// No reference counterpart: the reference bakes one scene per process
+// (baker/main.cpp:22-24, LightBaker::bake light_baker.cpp:166-230).  This is
+// the serving loop around the batched bake:
+//
+//   submit (any thread)  -> queue (FIFO, mutex)
+//   worker thread        -> cuts the queue head into a batch (probe cap,
+//                           device-memory budget), launches it with the
+//                           vlb_bake_batch machinery on a private stream
+//                           without waiting, records an event, and retires
+//                           batches whose event has fired (copies each
+//                           request's rows out of pinned staging);
+//                           up to max_inflight batches are queued on the GPU,
+//                           so the next batch is assembled while one runs.
+//   wait (any thread)    -> condition variable on the ticket.
+//
+// Kept hits: a bake submitted with keep_hits stores (triangle slot, distance)
+// per ray in stream-ordered device memory; a relight of it skips the primary
+// walk (the trace kernel reads the kept hit) and re-traces only the shadow
+// ray.  Kept sets count against the budget and are evicted least recently
+// used when a batch needs room; the host copy of the probes stays, so a
+// relight of an evicted set bakes in full with the same result.
+//
+// Budget accounting: device bytes of the batches in flight (radiance tile,
+// outputs, probe and sort scratch) plus the resident kept sets.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "vlb_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr uint64_t kDefaultBudget = 64ull << 30;
+constexpr uint32_t kDefaultMaxProbes = 1u << 20;
+constexpr uint32_t kDefaultInflight = 2;
+
+uint32_t svc_k(uint32_t lmax) { return (lmax + 1) * (lmax + 1); }
+
+// Message of the calling thread's last failed service call.
+thread_local std::string t_err;
+vlb_status sfail(vlb_status st, const std::string& msg) {
+  t_err = msg;
+  return st;
+}
+
+// Device bytes a batch holds for one request while it runs.
+uint64_t transient_bytes(uint64_t n, uint64_t S, uint32_t K, bool bf16) {
+  return n * S * 3 * (bf16 ? 2 : 4) + n * (12 + 4 + 16 + uint64_t(K) * 12);
+}
+// Device bytes of a kept-hit set.
+uint64_t hitset_bytes(uint64_t n, uint64_t S) { return n * S * 8 + n * 12; }
+
+// The cut rule shared by the worker and vlb_service_plan: does a request of
+// (probes, bytes) still join the batch being formed?
+bool joins(bool empty, uint64_t cur_probes, uint64_t cur_bytes, uint64_t probes, uint64_t bytes, uint64_t max_probes,
+           uint64_t room) {
+  if (empty) return bytes <= room;
+  return cur_probes + probes <= max_probes && cur_bytes + bytes <= room;
+}
+
+struct Request {
+  uint64_t ticket = 0;
+  const vlb_scene* scene = nullptr;
+  std::vector<float> probes;  // host copy (bakes)
+  uint32_t n = 0;
+  vlb_bake_params params{};
+  uint64_t relight_of = 0;
+  bool keep = false;
+  Clock::time_point t_submit;
+  enum State { kQueued, kRunning, kDone, kFailed } state = kQueued;
+  vlb_status status = VLB_OK;
+  std::string err;
+  std::vector<float> result;
+  double latency_ms = 0.0;
+};
+
+struct HitSet {
+  const vlb_scene* scene = nullptr;
+  const vlb_dirset* dirs = nullptr;
+  float tmin = 0.f, tmax = 0.f;
+  uint32_t n = 0;
+  std::vector<float> h_probes;
+  float* d_probes = nullptr;
+  int2* d_hits = nullptr;
+  uint64_t bytes = 0;
+  uint64_t last_use = 0;
+  bool resident = false;   // device copies exist (allocated when the keeping bake launched)
+  bool dropped = false;    // released by the user: freed by the worker
+};
+
+struct Batch {
+  std::vector<Request*> reqs;
+  std::vector<size_t> offs;  // float offset of each request's rows in the staging buffer
+  cudaEvent_t done = nullptr;
+  float* h_out = nullptr;    // pinned staging
+  size_t h_cap = 0;
+  int* h_err = nullptr;      // pinned copy of the device error counters
+  uint64_t bytes = 0;
+  uint64_t rays = 0;
+};
+
+}  // namespace
+
+struct vlb_service {
+  vlb_ctx* user = nullptr;
+  vlb_ctx* ctx = nullptr;  // private context: own stream, accepts the user's objects
+  vlb_service_config cfg{};
+  bool bf16 = false;
+  uint32_t K = 9;
+
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  uint64_t next_ticket = 1;
+  std::deque<uint64_t> queue;
+  std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+  std::unordered_map<uint64_t, std::unique_ptr<HitSet>> sets;  // by the keeping bake's ticket
+  uint64_t use_clock = 0;
+  vlb_service_stats stats{};
+  uint64_t set_bytes = 0, flight_bytes = 0;
+
+  // worker-only state
+  std::deque<Batch> inflight;
+  std::vector<std::pair<float*, size_t>> pinned_pool;
+  std::vector<int*> err_pool;
+  std::vector<cudaEvent_t> event_pool;
+  std::thread worker;
+
+  void run();
+  bool launch_next(std::unique_lock<std::mutex>& lk);
+  void retire(Batch& b, std::unique_lock<std::mutex>& lk);
+  void free_set(HitSet& s);
+  void fail_batch(std::vector<Request*>& rs, vlb_status st, const std::string& msg);
+  void note_bytes() {
+    stats.bytes_in_use = set_bytes + flight_bytes;
+    stats.bytes_peak = std::max(stats.bytes_peak, stats.bytes_in_use);
+  }
+};
+
+void vlb_service::free_set(HitSet& s) {
+  if (!s.resident) return;
+  cudaFreeAsync(s.d_hits, ctx->stream);
+  cudaFreeAsync(s.d_probes, ctx->stream);
+  s.d_hits = nullptr;
+  s.d_probes = nullptr;
+  s.resident = false;
+  set_bytes -= s.bytes;
+}
+
+void vlb_service::fail_batch(std::vector<Request*>& rs, vlb_status st, const std::string& msg) {
+  for (Request* r : rs) {
+    r->state = Request::kFailed;
+    r->status = st;
+    r->err = msg;
+    ++stats.failed;
+  }
+  cv_done.notify_all();
+}
+
+// Forms and launches the next batch from the queue head.  Called with the
+// lock held; returns false when nothing could be launched now.
+bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
+  const uint64_t budget = cfg.hbm_budget_bytes;
+  std::vector<Request*> take;
+  uint64_t probes = 0, bytes = 0;
+  std::vector<uint64_t> in_batch;  // tickets of the bakes in this batch
+  while (!queue.empty()) {
+    Request* r = reqs[queue.front()].get();
+    HitSet* src = nullptr;
+    if (r->relight_of) {
+      auto it = sets.find(r->relight_of);
+      src = it == sets.end() ? nullptr : it->second.get();
+      // the keeping bake's hits are written by its own trace launch: never in the same batch
+      if (std::find(in_batch.begin(), in_batch.end(), r->relight_of) != in_batch.end()) break;
+    }
+    const uint32_t n = src ? src->n : r->n;
+    const uint32_t S = src ? src->dirs->n : r->params.dirs->n;
+    uint64_t b = transient_bytes(n, S, K, bf16);
+    if (r->keep && !r->relight_of) b += hitset_bytes(n, S);
+    // room: budget minus what is held; evict unused kept sets (LRU) if the head does not fit
+    auto room = [&]() { return budget > set_bytes + flight_bytes ? budget - set_bytes - flight_bytes : 0; };
+    if (!joins(take.empty(), probes, bytes, n, b, cfg.max_batch_probes, room())) {
+      if (!take.empty()) break;
+      while (b > room()) {
+        HitSet* lru = nullptr;
+        for (auto& kv : sets)
+          if (kv.second->resident && kv.second.get() != src &&
+              (!lru || kv.second->last_use < lru->last_use))
+            lru = kv.second.get();
+        if (!lru) break;
+        free_set(*lru);
+        ++stats.evictions;
+      }
+      note_bytes();
+      if (b > room()) {
+        if (!inflight.empty()) return false;  // wait for the batches in flight to free their room
+        std::vector<Request*> one{r};
+        queue.pop_front();
+        fail_batch(one, VLB_ERR_OOM, "request exceeds the free device-memory budget");
+        continue;
+      }
+    }
+    queue.pop_front();
+    take.push_back(r);
+    in_batch.push_back(r->ticket);
+    probes += n;
+    bytes += b;
+    if (src) src->last_use = ++use_clock;
+  }
+  if (take.empty()) return false;
+
+  // jobs (the lock stays held: the worker is the only user of ctx and of the
+  // sets' device state; submitters only append to the queue)
+  const size_t nj = take.size();
+  std::vector<vlb_bake_job> jobs(nj);
+  std::vector<vlbh::JobExt> ext(nj);
+  std::vector<vlb_bake_params> jp(nj);
+  Batch bt;
+  bt.reqs = take;
+  bt.offs.resize(nj);
+  size_t rows = 0;
+  for (size_t i = 0; i < nj; ++i) {
+    Request* r = take[i];
+    jp[i] = r->params;
+    jp[i].lmax = cfg.lmax;
+    jp[i].precision = cfg.precision;
+    vlb_bake_job& j = jobs[i];
+    j.params = &jp[i];
+    if (r->relight_of) {
+      ++stats.relights;
+      HitSet* s = sets[r->relight_of].get();
+      jp[i].dirs = s->dirs;
+      jp[i].tmin = s->tmin;
+      jp[i].tmax = s->tmax;
+      j.scene = s->scene;
+      j.nprobes = s->n;
+      if (s->resident && !s->dropped) {
+        j.probe_xyz = s->d_probes;
+        ext[i].hits_in = s->d_hits;
+      } else {
+        ++stats.relights_rebaked;
+        j.probe_xyz = s->h_probes.data();
+      }
+    } else {
+      j.scene = r->scene;
+      j.nprobes = r->n;
+      j.probe_xyz = r->probes.data();
+      if (r->keep) {
+        HitSet* s = sets[r->ticket].get();
+        const size_t rays = size_t(r->n) * r->params.dirs->n;
+        if (cudaMallocAsync(reinterpret_cast<void**>(&s->d_hits), rays * 8, ctx->stream) != cudaSuccess ||
+            cudaMallocAsync(reinterpret_cast<void**>(&s->d_probes), size_t(r->n) * 12, ctx->stream) != cudaSuccess ||
+            cudaMemcpyAsync(s->d_probes, r->probes.data(), size_t(r->n) * 12, cudaMemcpyHostToDevice, ctx->stream) !=
+                cudaSuccess) {
+          cudaGetLastError();
+          if (s->d_hits) cudaFreeAsync(s->d_hits, ctx->stream);
+          if (s->d_probes) cudaFreeAsync(s->d_probes, ctx->stream);
+          s->d_hits = nullptr;
+          s->d_probes = nullptr;
+        } else {
+          s->resident = true;  // a set released before its bake launched is freed right after
+          s->bytes = hitset_bytes(r->n, r->params.dirs->n);
+          set_bytes += s->bytes;
+          s->last_use = ++use_clock;
+          ext[i].hits_out = s->d_hits;
+          j.probe_xyz = s->d_probes;
+        }
+      }
+    }
+    bt.offs[i] = rows * 3 * K;
+    rows += j.nprobes;
+    bt.rays += uint64_t(j.nprobes) * jp[i].dirs->n;
+  }
+  // pinned staging for the outputs and the error counters
+  const size_t need = std::max<size_t>(rows * 3 * K, 1);
+  for (size_t i = 0; i < pinned_pool.size(); ++i)
+    if (pinned_pool[i].second >= need) {
+      bt.h_out = pinned_pool[i].first;
+      bt.h_cap = pinned_pool[i].second;
+      pinned_pool.erase(pinned_pool.begin() + long(i));
+      break;
+    }
+  if (!bt.h_out) {
+    if (cudaMallocHost(reinterpret_cast<void**>(&bt.h_out), need * 4) != cudaSuccess) {
+      cudaGetLastError();
+      fail_batch(take, VLB_ERR_OOM, "pinned staging allocation failed");
+      return true;
+    }
+    bt.h_cap = need;
+  }
+  if (!err_pool.empty()) { bt.h_err = err_pool.back(); err_pool.pop_back(); }
+  else if (cudaMallocHost(reinterpret_cast<void**>(&bt.h_err), vlbk::kErrSlots * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    pinned_pool.push_back({bt.h_out, bt.h_cap});
+    fail_batch(take, VLB_ERR_OOM, "pinned staging allocation failed");
+    return true;
+  }
+  for (size_t i = 0; i < nj; ++i) jobs[i].out = bt.h_out + bt.offs[i];
+  if (!event_pool.empty()) { bt.done = event_pool.back(); event_pool.pop_back(); }
+  else cudaEventCreateWithFlags(&bt.done, cudaEventDisableTiming);
+
+  vlb_bake_params bp = jp[0];
+  const vlb_batch_schedule sc{0, 1, 0};
+  bool host_out = false;
+  vlb_status st = vlbh::batch_launch(ctx, jobs.data(), ext.data(), uint32_t(nj), &bp, sc, &host_out);
+  ctx->host_inputs_pending = false;  // pageable inputs were staged before the copies returned
+  if (st == VLB_OK) {
+    const cudaError_t e1 = cudaMemcpyAsync(bt.h_err, ctx->d_err, vlbk::kErrSlots * sizeof(int), cudaMemcpyDeviceToHost,
+                                           ctx->stream);
+    const cudaError_t e2 = cudaMemsetAsync(ctx->d_err, 0, vlbk::kErrSlots * sizeof(int), ctx->stream);
+    const cudaError_t e3 = cudaEventRecord(bt.done, ctx->stream);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+      cudaGetLastError();
+      st = VLB_ERR_CUDA;
+      ctx->err = "service: enqueue failed";
+    }
+  }
+  if (st != VLB_OK) {
+    pinned_pool.push_back({bt.h_out, bt.h_cap});
+    err_pool.push_back(bt.h_err);
+    event_pool.push_back(bt.done);
+    fail_batch(take, st, ctx->err);
+    return true;
+  }
+  for (Request* r : take) r->state = Request::kRunning;
+  bt.bytes = bytes;
+  for (size_t i = 0; i < nj; ++i)
+    if (take[i]->keep && !take[i]->relight_of) bt.bytes -= hitset_bytes(take[i]->n, take[i]->params.dirs->n);
+  flight_bytes += bt.bytes;
+  ++stats.batches;
+  note_bytes();
+  inflight.push_back(std::move(bt));
+  (void)lk;
+  return true;
+}
+
+void vlb_service::retire(Batch& b, std::unique_lock<std::mutex>&) {
+  const auto now = Clock::now();
+  bool bad = false;
+  for (int i = 0; i < vlbk::kErrSlots; ++i) bad |= b.h_err[i] != 0;
+  if (bad) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "device check failed in the batch (stack overflow %d, timeout %d, input %d)",
+                  b.h_err[vlbk::kErrStackOverflow], b.h_err[vlbk::kErrTimeout], b.h_err[vlbk::kErrBadInput]);
+    fail_batch(b.reqs, VLB_ERR_INTERNAL, msg);
+  } else {
+    for (size_t i = 0; i < b.reqs.size(); ++i) {
+      Request* r = b.reqs[i];
+      const uint32_t n = r->relight_of ? sets[r->relight_of]->n : r->n;
+      r->result.assign(b.h_out + b.offs[i], b.h_out + b.offs[i] + size_t(n) * 3 * K);
+      r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
+      r->state = Request::kDone;
+      ++stats.completed;
+      stats.probes += n;
+    }
+    stats.rays += b.rays;
+  }
+  flight_bytes -= b.bytes;
+  note_bytes();
+  pinned_pool.push_back({b.h_out, b.h_cap});
+  err_pool.push_back(b.h_err);
+  event_pool.push_back(b.done);
+  cv_done.notify_all();
+}
+
+void vlb_service::run() {
+  cudaSetDevice(ctx->device);
+  std::unique_lock<std::mutex> lk(mu);
+  for (;;) {
+    // retire in stream order
+    while (!inflight.empty()) {
+      const cudaError_t q = cudaEventQuery(inflight.front().done);
+      if (q == cudaErrorNotReady) break;
+      if (q != cudaSuccess) {
+        cudaGetLastError();
+        fail_batch(inflight.front().reqs, VLB_ERR_CUDA, cudaGetErrorString(q));
+        flight_bytes -= inflight.front().bytes;
+        note_bytes();
+      } else {
+        retire(inflight.front(), lk);
+      }
+      inflight.pop_front();
+    }
+    // user-released sets: device copies go, the entry (host probes) stays
+    for (auto& kv : sets)
+      if (kv.second->dropped && kv.second->resident) free_set(*kv.second);
+    note_bytes();
+    if (!queue.empty() && inflight.size() < cfg.max_inflight && launch_next(lk)) continue;
+    if (stop && queue.empty() && inflight.empty()) break;
+    // wait for a submit or for the oldest batch (polled: new requests may arrive meanwhile)
+    cv_work.wait_for(lk, std::chrono::microseconds(inflight.empty() ? 20000 : 50));
+  }
+  cudaStreamSynchronize(ctx->stream);
+}
+
+// ---- C ABI ---------------------------------------------------------------------------------
+extern "C" {
+
+vlb_status vlb_service_plan(const uint64_t* probes, const uint64_t* bytes, uint32_t n, uint64_t max_batch_probes,
+                            uint64_t budget_bytes, uint32_t* out_batch, uint32_t* nbatches) {
+  if ((!probes || !bytes || !out_batch) && n) return VLB_ERR_INVALID;
+  if (!nbatches) return VLB_ERR_INVALID;
+  uint32_t batch = 0;
+  bool open = false;
+  uint64_t cp = 0, cb = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (bytes[i] > budget_bytes) { out_batch[i] = UINT32_MAX; continue; }
+    if (open && !joins(false, cp, cb, probes[i], bytes[i], max_batch_probes, budget_bytes)) {
+      ++batch;
+      cp = cb = 0;
+    }
+    out_batch[i] = batch;
+    cp += probes[i];
+    cb += bytes[i];
+    open = true;
+  }
+  *nbatches = open ? batch + 1 : 0;
+  return VLB_OK;
+}
+
+vlb_status vlb_service_create(vlb_ctx* ctx, const vlb_service_config* cfg, vlb_service** out) {
+  if (!ctx || !out) return VLB_ERR_INVALID;
+  *out = nullptr;
+  vlb_service_config c = cfg ? *cfg : vlb_service_config{};
+  if (c.lmax == 0) c.lmax = 2;
+  if (c.lmax != 2 && c.lmax != 3) return sfail(VLB_ERR_INVALID, "service lmax must be 2 or 3");
+  if (c.precision > VLB_PREC_MIXED) return sfail(VLB_ERR_INVALID, "service precision must be FP32, FUSED or MIXED");
+  if (c.precision == VLB_PREC_FUSED) c.precision = VLB_PREC_FP32;
+  if (!c.hbm_budget_bytes) c.hbm_budget_bytes = kDefaultBudget;
+  if (!c.max_batch_probes) c.max_batch_probes = kDefaultMaxProbes;
+  if (!c.max_inflight) c.max_inflight = kDefaultInflight;
+  vlb_ctx* priv = nullptr;
+  vlb_status st = vlb_ctx_create(ctx->device, &priv);
+  if (st) return sfail(st, "service: private context creation failed");
+  priv->parent = ctx;
+  auto* s = new (std::nothrow) vlb_service();
+  if (!s) { vlb_ctx_destroy(priv); return VLB_ERR_OOM; }
+  s->user = ctx;
+  s->ctx = priv;
+  s->cfg = c;
+  s->bf16 = c.precision == VLB_PREC_MIXED;
+  s->K = svc_k(c.lmax);
+  s->worker = std::thread([s] { s->run(); });
+  *out = s;
+  return VLB_OK;
+}
+
+void vlb_service_destroy(vlb_service* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  cudaSetDevice(s->ctx->device);
+  for (auto& kv : s->sets) s->free_set(*kv.second);
+  cudaStreamSynchronize(s->ctx->stream);
+  for (auto& p : s->pinned_pool) cudaFreeHost(p.first);
+  for (int* p : s->err_pool) cudaFreeHost(p);
+  for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+  vlb_ctx_destroy(s->ctx);
+  delete s;
+}
+
+vlb_status vlb_service_submit(vlb_service* s, const vlb_request* q, uint64_t* ticket) {
+  if (!s || !q || !ticket) return VLB_ERR_INVALID;
+  *ticket = 0;
+  auto r = std::make_unique<Request>();
+  if (!q->params || !q->params->dirs) return sfail(VLB_ERR_INVALID, "request params and dirs required");
+  r->params = *q->params;
+  r->relight_of = q->relight_of;
+  r->keep = q->keep_hits != 0 && q->relight_of == 0;
+  std::unique_lock<std::mutex> lk(s->mu);
+  uint32_t n, S;
+  if (q->relight_of) {
+    auto it = s->sets.find(q->relight_of);
+    if (it == s->sets.end()) return sfail(VLB_ERR_INVALID, "relight_of names no bake that keeps its hits");
+    n = it->second->n;
+    S = it->second->dirs->n;
+  } else {
+    if (!q->scene || (q->nprobes && !q->probe_xyz))
+      return sfail(VLB_ERR_INVALID, "request needs a scene and probes");
+    r->scene = q->scene;
+    r->n = q->nprobes;
+    r->probes.assign(q->probe_xyz, q->probe_xyz + size_t(q->nprobes) * 3);
+    n = q->nprobes;
+    S = q->params->dirs->n;
+  }
+  // parameter checks that the batch would otherwise report for the whole batch
+  if (r->params.dirs->ctx != s->user || (r->params.sky && r->params.sky->ctx != s->user) ||
+      (r->scene && r->scene->ctx != s->user))
+    return sfail(VLB_ERR_INVALID, "request handles belong to another context");
+  if (!(r->params.tmax > r->params.tmin) || r->params.tmin < 0.f)
+    return sfail(VLB_ERR_INVALID, "bad ray interval");
+  const double sl = double(r->params.sun_dir[0]) * r->params.sun_dir[0] +
+                    double(r->params.sun_dir[1]) * r->params.sun_dir[1] + double(r->params.sun_dir[2]) * r->params.sun_dir[2];
+  if (!(sl > 0.0)) return sfail(VLB_ERR_INVALID, "sun direction must be non-zero");
+  uint64_t need = transient_bytes(n, S, s->K, s->bf16) + (r->keep ? hitset_bytes(n, S) : 0);
+  if (need > s->cfg.hbm_budget_bytes) {
+    return sfail(VLB_ERR_OOM, "request exceeds the service's device-memory budget");
+  }
+  r->ticket = s->next_ticket++;
+  r->t_submit = Clock::now();
+  if (n == 0) {  // nothing to bake
+    r->state = Request::kDone;
+    ++s->stats.completed;
+  }
+  if (r->keep) {
+    auto hs = std::make_unique<HitSet>();
+    hs->scene = r->scene;
+    hs->dirs = r->params.dirs;
+    hs->tmin = r->params.tmin;
+    hs->tmax = r->params.tmax;
+    hs->n = n;
+    hs->h_probes = r->probes;
+    s->sets[r->ticket] = std::move(hs);
+  }
+  *ticket = r->ticket;
+  ++s->stats.submitted;
+  const bool queued = r->state == Request::kQueued;
+  s->reqs[r->ticket] = std::move(r);
+  if (queued) s->queue.push_back(*ticket);
+  lk.unlock();
+  s->cv_work.notify_one();
+  return VLB_OK;
+}
+
+vlb_status vlb_service_wait(vlb_service* s, uint64_t ticket, uint32_t timeout_ms, float* out, double* latency_ms) {
+  if (!s) return VLB_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return sfail(VLB_ERR_INVALID, "unknown or already collected ticket");
+  Request* r = it->second.get();
+  auto finished = [r] { return r->state == Request::kDone || r->state == Request::kFailed; };
+  if (!finished()) {
+    if (timeout_ms == 0 || !s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), finished))
+      return VLB_ERR_TIMEOUT;
+  }
+  if (r->state == Request::kFailed) {
+    const vlb_status st = r->status;
+    const std::string msg = r->err;
+    s->reqs.erase(it);
+    return sfail(st, msg);
+  }
+  if (out && !r->result.empty()) std::memcpy(out, r->result.data(), r->result.size() * 4);
+  if (latency_ms) *latency_ms = r->latency_ms;
+  s->reqs.erase(it);
+  return VLB_OK;
+}
+
+vlb_status vlb_service_release(vlb_service* s, uint64_t ticket) {
+  if (!s) return VLB_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->sets.find(ticket);
+    if (it == s->sets.end()) return sfail(VLB_ERR_INVALID, "ticket keeps no hits");
+    it->second->dropped = true;
+  }
+  s->cv_work.notify_one();
+  return VLB_OK;
+}
+
+const char* vlb_service_last_error(void) { return t_err.c_str(); }
+
+vlb_status vlb_service_stats_read(vlb_service* s, vlb_service_stats* out) {
+  if (!s || !out) return VLB_ERR_INVALID;
+  std::lock_guard<std::mutex> g(s->mu);
+  *out = s->stats;
+  return VLB_OK;
+}
+
+}  // extern "C"

@@ -23,9 +23,11 @@ namespace {
 
 constexpr double kPiRef = 3.1415926538;  // shaders/sh_common.h:1
 constexpr double kPi = 3.141592653589793;
-// Triangles per probe above which a bake traces in lane mode (measured
-// crossover of the two modes on box scenes: 0.1 to 6 triangles per probe).
-constexpr uint32_t kLaneTrisPerProbe = 1;
+// Packet traversal pays off only for dense probe sets: at least this many
+// probes and at most one triangle per probe (measured on box scenes of
+// 200 to 200k triangles with 64 to 32k probes; elsewhere lane mode is up to
+// 6.5x faster, here packets are up to 1.7x faster).
+constexpr uint32_t kPacketMinProbes = 16384;
 
 vlb_status fail(vlb_ctx* ctx, vlb_status s, const char* fmt, ...) {
   if (ctx) {
@@ -821,19 +823,20 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
 
 // Common part of a bake launch: validated parameters -> trace arguments,
 // probes staged on the device and sorted into spatially compact packets.
-// Traversal mode of one bake: forced by the flags, else lane mode when the
-// scene has many triangles per probe (packets of sparse probes walk long
-// union paths).
+// Traversal mode of one bake: forced by the flags, else packets for dense
+// probe sets (neighbouring probes share most of their paths) and lane mode
+// otherwise (packets of sparse probes walk long union paths).
 static uint32_t lane_mode(const vlb_scene* scene, uint32_t nprobes, uint32_t flags) {
   if (flags & VLB_BAKE_TRAVERSAL_LANE) return 1;
   if (flags & VLB_BAKE_TRAVERSAL_PACKET) return 0;
-  return uint64_t(scene->ntris) > uint64_t(kLaneTrisPerProbe) * nprobes ? 1 : 0;
+  return nprobes >= kPacketMinProbes && scene->ntris <= nprobes ? 0 : 1;
 }
 
 // Checks the parameters of one bake; *sun_len gets |sun_dir| (FP64).
 static vlb_status check_params(vlb_ctx* ctx, const vlb_scene* scene, const vlb_bake_params* p, double* sun_len) {
   if (!scene || !p || !p->dirs) return fail(ctx, VLB_ERR_INVALID, "scene, params and params->dirs are required");
-  if (scene->ctx != ctx || p->dirs->ctx != ctx || (p->sky && p->sky->ctx != ctx))
+  auto mine = [ctx](const vlb_ctx* c) { return c == ctx || (ctx->parent && c == ctx->parent); };
+  if (!mine(scene->ctx) || !mine(p->dirs->ctx) || (p->sky && !mine(p->sky->ctx)))
     return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
   if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
   if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
@@ -1115,8 +1118,15 @@ static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBu
   return VLB_OK;
 }
 
-static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
-                            const vlb_batch_schedule& sc) {
+}  // extern "C"
+
+// Enqueues a batch on ctx->stream and returns without waiting.  Host
+// outputs are copied with cudaMemcpyAsync (asynchronous only for pinned
+// memory); *host_out tells whether there were any.  ext (optional, njobs
+// entries) adds kept-hit outputs and relight inputs per job.
+vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh::JobExt* ext, uint32_t njobs,
+                              const vlb_bake_params* params, const vlb_batch_schedule& sc, bool* host_out_any) {
+  *host_out_any = false;
   BatchPlan pl;
   vlb_status st = batch_plan(ctx, jobs, njobs, params, &pl);
   if (st) return st;
@@ -1198,6 +1208,7 @@ static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njo
     items += (uint64_t(b.nprobes) + 31) / 32 * d.chunks;
     for (int a = 0; a < 6; ++a) d.bounds[a] = j.scene->bounds[a];
     d.sort_scratch = bb.sort + 4 * b.row0;
+    if (ext) { d.hits_out = ext[b.idx].hits_out; d.hits_in = ext[b.idx].hits_in; }
   }
   if (items > 0xFFFFFFFFull) return fail(ctx, VLB_ERR_INVALID, "batch has too many work items");
   auto& meta_h = ctx->batch_meta;
@@ -1253,16 +1264,33 @@ static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njo
   } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items)))) {
     return st;
   }
-  bool host_out = false;
   for (const auto& b : pl.jobs) {
     float* o = jobs[b.idx].out;
     if (is_device_ptr(o)) continue;
-    host_out = true;
+    *host_out_any = true;
     VLB_CUDA(ctx, cudaMemcpyAsync(o, bb.out + b.row0 * V, size_t(b.nprobes) * V * 4, cudaMemcpyDeviceToHost,
                                   ctx->stream));
   }
+  return VLB_OK;
+}
+
+extern "C" {
+
+static vlb_status batch_run(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
+                            const vlb_batch_schedule& sc) {
+  bool host_out = false;
+  const vlb_status st = vlbh::batch_launch(ctx, jobs, nullptr, njobs, params, sc, &host_out);
+  if (st) return st;
   return finish(ctx, host_out);
 }
+
+}  // extern "C"
+
+vlb_status vlbh::ctx_finish(vlb_ctx* ctx, bool sync) { return finish(ctx, sync); }
+
+vlb_status vlbh::ctx_fail(vlb_ctx* ctx, vlb_status s, const char* msg) { return fail(ctx, s, "%s", msg); }
+
+extern "C" {
 
 vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                           const vlb_batch_schedule* sched) {

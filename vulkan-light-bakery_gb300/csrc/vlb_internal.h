@@ -184,6 +184,11 @@ struct BakeJobDev {
   // probe sort: bounds for the Morton codes, 4 scratch arrays of nprobes
   float bounds[6];
   uint32_t* sort_scratch;
+  // kept primary hits, [nprobes][S] (triangle slot or -1, distance bits):
+  // written when hits_out is set; when hits_in is set the primary walk is
+  // skipped and the kept hit shaded (relight)
+  int2* hits_out;
+  const int2* hits_in;
 };
 // One CTA per job: Morton order of each job's probes into job.order.
 void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s);
@@ -197,9 +202,24 @@ void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* sr
 
 }  // namespace vlbk
 
+// ---- host internals shared by the C ABI translation units ----------------------
+namespace vlbh {
+// Per-job extras of a batch: kept primary hits out, or kept hits in (relight).
+struct JobExt {
+  int2* hits_out = nullptr;
+  const int2* hits_in = nullptr;
+};
+vlb_status batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const JobExt* ext, uint32_t njobs,
+                        const vlb_bake_params* params, const vlb_batch_schedule& sc, bool* host_out_any);
+// Launch-error check, and (sync) stream synchronisation + device error counters.
+vlb_status ctx_finish(vlb_ctx* ctx, bool sync);
+vlb_status ctx_fail(vlb_ctx* ctx, vlb_status s, const char* msg);
+}  // namespace vlbh
+
 // ---- host objects behind the opaque handles ------------------------------------
 struct vlb_ctx {
   int device = 0;
+  vlb_ctx* parent = nullptr;  // a service's private context accepts its parent's objects
   int num_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;

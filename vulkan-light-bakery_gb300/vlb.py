@@ -61,6 +61,22 @@ class BatchSchedule(C.Structure):
     _fields_ = [("dirs_per_item", C.c_uint32), ("cost_order", C.c_uint32), ("graph", C.c_uint32)]
 
 
+class ServiceConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("lmax", C.c_uint32), ("precision", C.c_uint32),
+                ("max_batch_probes", C.c_uint32), ("max_inflight", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("probe_xyz", C.c_void_p), ("nprobes", C.c_uint32), ("params", C.c_void_p),
+                ("relight_of", C.c_uint64), ("keep_hits", C.c_uint32)]
+
+
+class ServiceStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "batches", "relights",
+                                          "relights_rebaked", "evictions", "probes", "rays", "bytes_in_use",
+                                          "bytes_peak")]
+
+
 def _load() -> C.CDLL:
     if not LIB_PATH.exists():
         raise ImportError(f"libvlb.so not found at {LIB_PATH}; run __graft_entry__.build() first")
@@ -103,6 +119,14 @@ def _load() -> C.CDLL:
         "vlb_bake_trace_stats": (I32, [P, P, P, U32, P, P]),
         "vlb_bake_batch": (I32, [P, P, U32, P, P]),
         "vlb_batch_autotune": (I32, [P, P, U32, P, U32, P, P]),
+        "vlb_service_create": (I32, [P, P, C.POINTER(P)]),
+        "vlb_service_destroy": (None, [P]),
+        "vlb_service_submit": (I32, [P, P, C.POINTER(U64)]),
+        "vlb_service_wait": (I32, [P, U64, U32, P, C.POINTER(C.c_double)]),
+        "vlb_service_release": (I32, [P, U64]),
+        "vlb_service_stats_read": (I32, [P, P]),
+        "vlb_service_last_error": (C.c_char_p, []),
+        "vlb_service_plan": (I32, [P, P, U32, U64, U64, P, C.POINTER(U32)]),
         "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
         "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
         "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
@@ -281,6 +305,84 @@ class Context:
         out = np.empty((h, w, 3), np.float32)
         self.check(lib.vlb_sh_eval_envmap(self.h, _ptr(c), lmax, w, h, scale, _ptr(out)))
         return out
+
+
+class Service:
+    """Resident bake service (vlb_service_*): submit from any thread, wait by ticket."""
+
+    def __init__(self, ctx: Context, budget_bytes: int = 0, lmax: int = 2, precision: int = PREC_MIXED,
+                 max_batch_probes: int = 0, max_inflight: int = 0):
+        cfg = ServiceConfig(budget_bytes, lmax, precision, max_batch_probes, max_inflight)
+        h = C.c_void_p()
+        self.ctx = ctx
+        self.lmax = lmax
+        self._check(lib.vlb_service_create(ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}  # ticket -> objects the request names (kept alive until collected)
+        self._n = {}
+
+    @staticmethod
+    def _check(st: int) -> None:
+        if st != OK:
+            raise VlbError(st, lib.vlb_service_last_error().decode())
+
+    def submit(self, scene, probes, params: BakeParams, keep_hits: bool = False, relight_of: int = 0) -> int:
+        if relight_of:
+            pr, n = None, self._n.get(relight_of, 0)
+        else:
+            pr = _f32(probes).reshape(-1, 3)
+            n = pr.shape[0]
+        req = Request(None if scene is None else getattr(scene.h, "value", scene.h), _ptr(pr), 0 if relight_of else n,
+                      C.addressof(params), relight_of, 1 if keep_hits else 0)
+        t = C.c_uint64()
+        self._check(lib.vlb_service_submit(self.h, C.byref(req), C.byref(t)))
+        self._keep[t.value] = (scene, params)
+        self._n[t.value] = n
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        """Returns (sh [n, K, 3], latency_ms); raises VlbError (ERR_TIMEOUT if not done)."""
+        n = self._n[ticket]
+        out = np.empty((n, k_of(self.lmax), 3), np.float32)
+        lat = C.c_double()
+        st = lib.vlb_service_wait(self.h, ticket, timeout_ms, _ptr(out) if n else None, C.byref(lat))
+        if st == ERR_TIMEOUT:
+            raise VlbError(st, "not done")
+        self._keep.pop(ticket, None)
+        self._check(st)
+        return out, lat.value
+
+    def release(self, ticket: int) -> None:
+        self._check(lib.vlb_service_release(self.h, ticket))
+
+    def stats(self) -> dict:
+        s = ServiceStats()
+        self._check(lib.vlb_service_stats_read(self.h, C.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in ServiceStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib.vlb_service_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def service_plan(probes, nbytes, max_batch_probes: int, budget_bytes: int):
+    """The service's admission rule on the host: batch index per request (-1 refused)."""
+    p = np.ascontiguousarray(probes, dtype=np.uint64)
+    b = np.ascontiguousarray(nbytes, dtype=np.uint64)
+    out = np.zeros(len(p), np.uint32)
+    nb = C.c_uint32()
+    st = lib.vlb_service_plan(_ptr(p) if len(p) else None, _ptr(b) if len(b) else None, len(p), max_batch_probes,
+                              budget_bytes, _ptr(out) if len(p) else None, C.byref(nb))
+    if st != OK:
+        raise VlbError(st, "vlb_service_plan")
+    return np.where(out == 0xFFFFFFFF, -1, out.astype(np.int64)), nb.value
 
 
 def _job_array(jobs, params: BakeParams):
