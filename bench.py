@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
-    ap.add_argument("--only", choices=["skybox", "projection", "batch"], default=None,
+    ap.add_argument("--only", choices=["skybox", "projection", "batch", "service"], default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
@@ -205,7 +205,8 @@ def main():
     ctx.set_stream(stream.cuda_stream)
     if args.only:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-        fn = {"skybox": skybox_measure, "projection": projection_measure, "batch": batch_measure}[args.only]
+        fn = {"skybox": skybox_measure, "projection": projection_measure, "batch": batch_measure,
+              "service": service_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
         return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
@@ -340,6 +341,7 @@ def main():
         "skybox_c0": skybox_measure(ctx, torch, stream, args.steps, hbm_peak),
         "projection_c2": projection_measure(ctx, torch, stream, args.steps, hbm_peak),
         "batch_c3": batch_measure(ctx, torch, stream, args.steps, hbm_peak),
+        "service_c4": service_measure(ctx, torch, stream, args.steps, hbm_peak),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -550,6 +552,125 @@ def batch_measure(ctx, torch, stream, steps, hbm_peak):
                 "d2h_bytes_per_step": int(P * K * 12)},
         "l2": "flushed (256 MiB write) before every timed batch",
     }
+
+
+SERVICE_BOXES = (64, 512, 4096, 16384, 32768, 65536, 131072, 170000)
+
+
+def service_requests(nreq, rate, seed, scenes_bounds):
+    """Seeded request stream: Poisson arrivals at `rate` per second; bakes of
+    log-uniform 16-16384 probes at uniform positions in a uniformly chosen
+    resident scene with 256 or 1024 rays; 20% relights of an earlier bake
+    with a new seeded sun direction and intensity."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    reqs = []
+    for i in range(nreq):
+        if i >= 4 and rng.random() < 0.2:
+            reqs.append(dict(t=t[i], relight=int(rng.integers(0, i)), sun_seed=int(rng.integers(1 << 30)),
+                             intensity=float(rng.uniform(1, 10))))
+            continue
+        sc = int(rng.integers(0, len(scenes_bounds)))
+        lo, hi = scenes_bounds[sc]
+        n = int(np.exp(rng.uniform(np.log(16), np.log(16384))))
+        reqs.append(dict(t=t[i], relight=None, scene=sc, S=int(rng.choice([256, 1024])),
+                         probes=(lo + rng.random((n, 3)) * (hi - lo)).astype(np.float32),
+                         sun_seed=int(rng.integers(1 << 30)), intensity=5.0))
+    return reqs
+
+
+def service_run(ctx, svc, scenes, dsets, sky, reqs, lmax, prec):
+    """Open-loop run: a submitter thread issues the requests at their arrival
+    times; the caller collects them.  Returns latencies (ms) and wall time."""
+    import vlb
+
+    tickets = [None] * len(reqs)
+    params = [None] * len(reqs)
+    base = [None] * len(reqs)  # bake index each request resolves to
+    t0 = time.perf_counter()
+
+    def submit_all():
+        for i, r in enumerate(reqs):
+            dt = r["t"] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            if r["relight"] is None:
+                base[i] = i
+                p = vlb.bake_params(dsets[r["S"]], lmax, prec, vlb.synth_sun(r["sun_seed"]),
+                                    sun_intensity=r["intensity"], sky=sky)
+                params[i] = p
+                tickets[i] = svc.submit(scenes[r["scene"]], r["probes"], p, keep_hits=True)
+            else:
+                j = r["relight"]
+                while base[j] is None or tickets[base[j]] is None:
+                    time.sleep(0.0001)
+                b = base[j]
+                base[i] = b
+                p = vlb.bake_params(dsets[reqs[b]["S"]], lmax, prec, vlb.synth_sun(r["sun_seed"]),
+                                    sun_intensity=r["intensity"], sky=sky)
+                params[i] = p
+                tickets[i] = svc.submit(None, None, p, relight_of=tickets[b])
+
+    th = threading.Thread(target=submit_all)
+    th.start()
+    lat = []
+    for i in range(len(reqs)):
+        while tickets[i] is None:
+            time.sleep(0.0001)
+        _, ms = svc.wait(tickets[i], timeout_ms=600000)
+        lat.append(ms)
+    th.join()
+    wall = time.perf_counter() - t0
+    return lat, wall, base
+
+
+def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
+    """Config 4: the bake service over 8 resident box scenes (64 ... 170,000
+    boxes, 778 ... 2,040,010 triangles), Poisson arrivals swept over rates
+    relative to the measured capacity, 20% relights, 64 GiB budget."""
+    import vlb
+
+    t0 = time.perf_counter()
+    scenes, bounds, tris = [], [], []
+    for i, nb in enumerate(SERVICE_BOXES):
+        pos, idx, alb = vlb.synth_box_scene(SEED * 31 + i, nb)
+        scenes.append(ctx.scene(pos, idx, alb))
+        bounds.append((np.minimum(pos.min(0), 0), np.maximum(pos.max(0), 0)))
+        tris.append(int(idx.shape[0]))
+    build_s = time.perf_counter() - t0
+    dsets = {S: ctx.fibonacci(S) for S in (256, 1024)}
+    sky = ctx.sky(vlb.synth_cubemap(SEED, SKY_N), SKY_N)
+    out = {"workload": f"bake service: {len(scenes)} resident box scenes ({min(tris)}-{max(tris)} tris), requests "
+                       "of log-uniform 16-16384 probes x {256,1024} rays, 20% relights (kept hits, new sun), "
+                       "Poisson arrivals, 64 GiB budget, L2 SH",
+           "scene_build_s": build_s}
+
+    def run(prec, rate, n, seed):
+        svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=prec)
+        reqs = service_requests(n, rate, seed, bounds)
+        lat, wall, base = service_run(ctx, svc, scenes, dsets, sky, reqs, LMAX, prec)
+        st = svc.stats()
+        svc.close()
+        lat = np.array(lat)
+        return {"rate_offered": rate, "requests": n, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "probes_per_s": st["probes"] / wall,
+                "grays_per_s": st["rays"] / wall / 1e9, "batches": st["batches"], "relights": st["relights"],
+                "relights_rebaked": st["relights_rebaked"], "evictions": st["evictions"],
+                "bytes_peak": st["bytes_peak"], "wall_s": wall}
+
+    # capacity: every request at t = 0 (closed burst)
+    cap = run(vlb.PREC_MIXED, 1e9, nreq // 2, SEED + 7)
+    capacity = cap["requests"] / cap["wall_s"]
+    out["capacity_req_per_s"] = capacity
+    out["burst"] = cap
+    # open-loop runs of about 5 s each (20 to nreq requests)
+    def nfor(rate):
+        return int(min(nreq, max(20, rate * 5.0)))
+
+    out["mixed_bf16"] = [run(vlb.PREC_MIXED, f * capacity, nfor(f * capacity), SEED + 11 + k)
+                         for k, f in enumerate((0.3, 0.6, 0.9))]
+    out["fp32"] = [run(vlb.PREC_FP32, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
+    return out
 
 
 def ctx_trace_stats(ctx, scene, probes, params):
