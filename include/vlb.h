@@ -348,6 +348,28 @@ vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint
 vlb_status vlb_sh_eval_envmap(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, uint32_t w, uint32_t h, float scale,
                               float* out);
 
+/* ---- baked-light glTF files ----------------------------------------------------
+ * Host only (no GPU).  Replaces LightBaker::serialize
+ * (src/baker/light_baker.cpp:372-401): the input glTF document plus one
+ * buffer holding the coefficients as a base64 data URI, one bufferView over
+ * it and the top-level "light" object {bufferView, gridStep {x, y, z},
+ * lmax: coeff_count}, printed the way the reference's JSON library prints it
+ * (every object's keys sorted, 4-space indentation) with a final newline --
+ * the text the reference writes to baked_<name>.gltf.  coeffs: nprobes x
+ * coeff_count x 3 FP32 (coeff_count 16 is the reference's layout and value).
+ * out NULL: only *out_len (bytes including the terminating NUL). */
+vlb_status vlb_gltf_write_light(const char* gltf_json, size_t json_len, const float* coeffs, uint32_t nprobes,
+                                uint32_t coeff_count, const float grid_step[3], char* out, size_t out_cap,
+                                size_t* out_len);
+/* Replaces Scene_t::loadBakedLight (src/scene_manager.cpp:614-648): reads
+ * gridStep, lmax (the coefficient count) and the coefficient bytes
+ * (byteLength of the light's buffer) back.  A document without "light"
+ * gives zeros and *coeffs_bytes = 0.  coeffs NULL: only the sizes. */
+vlb_status vlb_gltf_read_light(const char* gltf_json, size_t json_len, float grid_step[3], uint32_t* coeff_count,
+                               void* coeffs, size_t coeffs_cap, size_t* coeffs_bytes);
+/* Message of the calling thread's last failed vlb_gltf_* call (never NULL). */
+const char* vlb_gltf_last_error(void);
+
 /* ---- synthetic inputs (bench and tests) -------------------------------------
  * Seeded SplitMix64 generators for the benchmark workloads.  The room is the
  * unit box [0,1]^3 open at +Y (10 triangles, albedo 0.5); each box has its

@@ -127,6 +127,11 @@ def _load() -> C.CDLL:
         "vlb_service_stats_read": (I32, [P, P]),
         "vlb_service_last_error": (C.c_char_p, []),
         "vlb_service_plan": (I32, [P, P, U32, U64, U64, P, C.POINTER(U32)]),
+        "vlb_gltf_write_light": (I32, [C.c_char_p, C.c_size_t, P, U32, U32, P, P, C.c_size_t,
+                                       C.POINTER(C.c_size_t)]),
+        "vlb_gltf_read_light": (I32, [C.c_char_p, C.c_size_t, P, C.POINTER(U32), P, C.c_size_t,
+                                      C.POINTER(C.c_size_t)]),
+        "vlb_gltf_last_error": (C.c_char_p, []),
         "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
         "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
         "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
@@ -383,6 +388,41 @@ def service_plan(probes, nbytes, max_batch_probes: int, budget_bytes: int):
     if st != OK:
         raise VlbError(st, "vlb_service_plan")
     return np.where(out == 0xFFFFFFFF, -1, out.astype(np.int64)), nb.value
+
+
+def gltf_write_light(gltf_text: str, coeffs, grid_step) -> str:
+    """The reference's baked_<name>.gltf text for coefficients [n, K, 3] (host only)."""
+    src = gltf_text.encode()
+    c = _f32(coeffs)
+    n, K = (c.shape[0], c.shape[1]) if c.ndim == 3 else (0, 16)
+    g = _f32(grid_step).reshape(3)
+    size = C.c_size_t()
+    args = (src, len(src), _ptr(c) if c.size else None, n, K, _ptr(g))
+    st = lib.vlb_gltf_write_light(*args, None, 0, C.byref(size))
+    if st != OK:
+        raise VlbError(st, lib.vlb_gltf_last_error().decode())
+    buf = C.create_string_buffer(size.value)
+    st = lib.vlb_gltf_write_light(*args, buf, size.value, C.byref(size))
+    if st != OK:
+        raise VlbError(st, lib.vlb_gltf_last_error().decode())
+    return buf.value.decode()
+
+
+def gltf_read_light(gltf_text: str):
+    """(grid_step[3], coeff_count, coefficient bytes) of a baked glTF (host only)."""
+    src = gltf_text.encode()
+    g = np.zeros(3, np.float32)
+    k = C.c_uint32()
+    nb = C.c_size_t()
+    st = lib.vlb_gltf_read_light(src, len(src), _ptr(g), C.byref(k), None, 0, C.byref(nb))
+    if st != OK:
+        raise VlbError(st, lib.vlb_gltf_last_error().decode())
+    data = np.zeros(nb.value, np.uint8)
+    if nb.value:
+        st = lib.vlb_gltf_read_light(src, len(src), _ptr(g), C.byref(k), _ptr(data), nb.value, C.byref(nb))
+        if st != OK:
+            raise VlbError(st, lib.vlb_gltf_last_error().decode())
+    return g, int(k.value), data.tobytes()
 
 
 def _job_array(jobs, params: BakeParams):
