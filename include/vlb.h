@@ -370,6 +370,35 @@ vlb_status vlb_gltf_read_light(const char* gltf_json, size_t json_len, float gri
 /* Message of the calling thread's last failed vlb_gltf_* call (never NULL). */
 const char* vlb_gltf_last_error(void);
 
+/* ---- evaluating a baked grid (the consumer side) --------------------------------
+ * Replaces the probe lighting of shaders/main.rchit:124-168 with
+ * shaders/sh.rmiss:23-39.  For each shading point x with normal n: the grid
+ * cell holding x, its 8 corner probes, a visibility ray from x + bias*n toward
+ * each probe (any hit in (0, |p - x|); scene NULL: all visible), weight
+ * |step| - |p - x|, and out = sum(w E_p(n)) / sum(w) over the visible corners
+ * with E_p(n) = sum_k c_pk Y_k(n).  The reference's faults are not reproduced:
+ * its cell index assumes the grid starts at the origin and 7 x 7 x 7
+ * probes in x-major order (the bake writes them breadth-first,
+ * light_baker.cpp:138-159), it strides by (16+1)^2 coefficients and sums 16
+ * bands of a 16-coefficient probe, and it divides 0 by 0 when no probe is
+ * visible (here: 0).  coeffs: the bake's output for the grid, nprobes x K x 3
+ * in the reference's breadth-first order (vlb_probe_grid_ref_order).
+ * vis_mask (may be NULL): bit c set when corner c (bit 2: +x, bit 1: +y,
+ * bit 0: +z) was visible. */
+typedef struct vlb_probe_grid {
+  float origin[3];    /* position of probe (0,0,0): the bake bounds' minimum */
+  float step[3];      /* grid step (light.gridStep) */
+  uint32_t counts[3]; /* probes per axis */
+} vlb_probe_grid;
+vlb_status vlb_probe_eval(vlb_ctx* ctx, const vlb_scene* scene, const float* coeffs, uint32_t lmax,
+                          const vlb_probe_grid* grid, const float* points, const float* normals, uint32_t n,
+                          float shadow_bias, float* out_rgb, uint8_t* vis_mask);
+/* Replaces shaders/skybox_sh.rmiss:14-25: out[i] = sum_k c_k Y_k(normalize(dirs[i]))
+ * over K = (lmax+1)^2 coefficients (the reference sums 16 bands over a
+ * 16-coefficient buffer). coeffs: K x 3. */
+vlb_status vlb_sh_eval_dirs(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n,
+                            float* out_rgb);
+
 /* ---- synthetic inputs (bench and tests) -------------------------------------
  * Seeded SplitMix64 generators for the benchmark workloads.  The room is the
  * unit box [0,1]^3 open at +Y (10 triangles, albedo 0.5); each box has its

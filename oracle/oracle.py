@@ -43,6 +43,7 @@ def _load():
         "orc_ray_tri": (I32, [P, P, P, I32, P, P, P, P]),
         "orc_shadow_margin": (D, [P, P, P, D, D]),
         "orc_closest_hit": (None, [P, P, P, D, D, P, P]),
+        "orc_probe_eval": (None, [P, P, I32, P, P, P, P, P, U32, F, I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -225,6 +226,26 @@ class Scene:
         tri, t = C.c_int(), C.c_double()
         lib.orc_closest_hit(self.h, _p(o), _p(d), tmin, tmax, C.byref(tri), C.byref(t))
         return tri.value, t.value
+
+
+def probe_eval(scene, coeffs, lmax, origin, step, counts, points, normals, bias=5e-3, margins=False,
+               nthreads=None):
+    """FP64 probe evaluation (main.rchit:124-168 / sh.rmiss:23-39, intended math).
+    scene: Scene or None (every probe visible).  Returns (rgb [n,3] f64,
+    visibility mask [n] u8 (bit c = corner c), shadow margins [n,8] or None)."""
+    c = _c(coeffs, np.float32)
+    o = _c(origin, np.float32)
+    st = _c(step, np.float32)
+    cn = _c(counts, np.uint32)
+    pt = _c(points, np.float32).reshape(-1, 3)
+    nm = _c(normals, np.float32).reshape(-1, 3)
+    n = pt.shape[0]
+    out = np.empty((n, 3), np.float64)
+    vis = np.empty(n, np.uint8)
+    mg = np.empty((n, 8), np.float64) if margins else None
+    lib.orc_probe_eval(None if scene is None else scene.h, _p(c), lmax, _p(o), _p(st), _p(cn), _p(pt), _p(nm), n,
+                       bias, nthreads or NTHREADS, _p(out), _p(vis), _p(mg))
+    return out, vis, mg
 
 
 def load_ref():

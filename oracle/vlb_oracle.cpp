@@ -744,6 +744,79 @@ void orc_bake(const void* scene, const float* probes, uint32_t np, const float* 
   });
 }
 
+// ---- probe evaluation (consumer side) ------------------------------------------
+// shaders/main.rchit:124-168 with shaders/sh.rmiss:23-39, intended math: the
+// grid starts at `origin` (the reference assumes 0), probes are indexed in the
+// bake's breadth-first order (light_baker.cpp:138-159; the reference indexes
+// x + 7y + 49z), each probe holds K = (lmax+1)^2 coefficients (the reference
+// strides by (16+1)^2 and sums 16 bands), and a point that sees no probe gets
+// 0 (the reference divides 0 by 0).  Per corner c (bits z, y, x of c as in
+// gridVertices): probe p = origin + step * ijk (FP32 product and sum),
+// d = p - x, t = |d|, visibility = no hit in (0, t) from x + bias * n along
+// d / t, weight = |step| - t; out = sum(w E_p(n)) / sum(w) over visible
+// corners, E_p(n) = sum_k c_pk Y_k(n).
+uint32_t ref_grid_index(const uint32_t* cnt, uint32_t i, uint32_t j, uint32_t k) {
+  const uint32_t q = j == 0 ? i : cnt[0] + i * (cnt[1] - 1) + (j - 1);
+  return k == 0 ? q : cnt[0] * cnt[1] + q * (cnt[2] - 1) + (k - 1);
+}
+
+void orc_probe_eval(const void* scene, const float* coeffs, int lmax, const float* origin, const float* step,
+                    const uint32_t* counts, const float* points, const float* normals, uint32_t n, float bias,
+                    int nthreads, double* out, uint8_t* vis, double* margin) {
+  const Scene* sc = static_cast<const Scene*>(scene);
+  const int K = sh_count(lmax);
+  parallel_for(n, nthreads, [&](uint32_t i) {
+    const double x[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+    double nv[3] = {normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]};
+    const double nl = std::sqrt(dot3(nv, nv));
+    for (double& c : nv) c /= nl;
+    double Y[25];
+    sh_basis(lmax, nv[0], nv[1], nv[2], Y);
+    const double o[3] = {x[0] + double(bias) * nv[0], x[1] + double(bias) * nv[1], x[2] + double(bias) * nv[2]};
+    int cell[3];
+    for (int a = 0; a < 3; ++a) {
+      const float q = std::floor((points[3 * i + a] - origin[a]) / step[a]);
+      cell[a] = std::min(std::max(int(q), 0), std::max(int(counts[a]) - 2, 0));
+    }
+    const double wmax = std::sqrt(double(step[0]) * step[0] + double(step[1]) * step[1] + double(step[2]) * step[2]);
+    double sum[3] = {0, 0, 0}, ws = 0.0;
+    uint8_t mask = 0;
+    for (int c = 0; c < 8; ++c) {
+      const uint32_t bit[3] = {uint32_t(c >> 2) & 1u, uint32_t(c >> 1) & 1u, uint32_t(c) & 1u};
+      uint32_t ijk[3];
+      double d[3], p[3];
+      for (int a = 0; a < 3; ++a) {
+        ijk[a] = std::min(uint32_t(cell[a]) + bit[a], counts[a] - 1);
+        volatile float pr = step[a] * float(ijk[a]);
+        volatile float ps = origin[a] + pr;
+        p[a] = ps;
+        d[a] = p[a] - x[a];
+      }
+      const double t = std::sqrt(dot3(d, d));
+      bool visible = true;
+      double mg = -INFINITY;
+      if (t > 0.0 && sc) {
+        const double dn[3] = {d[0] / t, d[1] / t, d[2] / t};
+        visible = !any_hit(*sc, o, dn, 0.0, t);
+        if (margin) mg = shadow_margin(*sc, o, dn, 0.0, t);
+      }
+      if (margin) margin[size_t(i) * 8 + c] = mg;
+      if (!visible) continue;
+      mask |= uint8_t(1u << c);
+      const double w = wmax - t;
+      const float* cp = coeffs + size_t(ref_grid_index(counts, ijk[0], ijk[1], ijk[2])) * K * 3;
+      for (int ch = 0; ch < 3; ++ch) {
+        double e = 0.0;
+        for (int k = 0; k < K; ++k) e += double(cp[3 * k + ch]) * Y[k];
+        sum[ch] += w * e;
+      }
+      ws += w;
+    }
+    for (int ch = 0; ch < 3; ++ch) out[3 * size_t(i) + ch] = ws > 0.0 ? sum[ch] / ws : 0.0;
+    if (vis) vis[i] = mask;
+  });
+}
+
 // FP64 facts about one ray and one triangle, for classifying decision
 // mismatches: t, barycentrics, signed edge distance (world units).
 int orc_ray_tri(const void* scene, const double* o, const double* d, int32_t tri, double* t, double* b1, double* b2,

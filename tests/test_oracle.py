@@ -208,3 +208,40 @@ def test_bake_probe_inside_closed_box_is_dark():
     B = O.basis_matrix(d.astype(np.float64), w, 3)
     sh = sc.bake(c[None].astype(np.float32), d, B, vlb.synth_sun(1))
     assert np.max(np.abs(sh)) == 0.0
+
+
+def test_probe_eval_oracle_indexes_the_bake_grid_order():
+    """With no occluders the oracle's probe evaluation is a weighted mean of the
+    8 corner probes, looked up in the bake's breadth-first order: give every
+    probe a DC coefficient equal to its x (resp. y, z) position and the
+    evaluation at a cell's centre returns the centre's coordinate."""
+    import vlb
+
+    bounds = np.float32([-1.0, 0.0, 2.0, 3.0, 1.5, 4.0])
+    counts = np.uint32([5, 3, 4])
+    pos, step = vlb.probe_grid_ref_order(bounds, counts)
+    K = 9
+    y00 = 0.282095
+    rng = np.random.default_rng(1)
+    pts = (bounds[:3] + rng.random((64, 3)) * (bounds[3:] - bounds[:3])).astype(np.float32)
+    cell = np.clip(np.floor((pts - bounds[:3]) / step), 0, counts - 2)
+    nrm = rng.standard_normal((64, 3)).astype(np.float32)
+    for axis in range(3):
+        coeffs = np.zeros((pos.shape[0], K, 3), np.float32)
+        coeffs[:, 0, :] = (pos[:, axis] / y00)[:, None]
+        out, vis, _ = O.probe_eval(None, coeffs, 2, bounds[:3], step, counts, pts, nrm)
+        assert np.all(vis == 255)
+        # expected: the distance-weighted mean of the 8 corner positions along the axis
+        wmax = np.linalg.norm(step.astype(np.float64))
+        exp = np.zeros(len(pts))
+        for i, (p, c) in enumerate(zip(pts, cell)):
+            num = den = 0.0
+            for corner in range(8):
+                bits = np.array([(corner >> 2) & 1, (corner >> 1) & 1, corner & 1])
+                ijk = np.minimum(c + bits, counts - 1)
+                q = (bounds[:3] + step * ijk.astype(np.float32)).astype(np.float64)
+                w = wmax - np.linalg.norm(q - p)
+                num += w * q[axis]
+                den += w
+            exp[i] = num / den
+        assert np.allclose(out[:, 0], exp, rtol=0, atol=1e-5)

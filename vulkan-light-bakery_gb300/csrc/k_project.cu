@@ -135,4 +135,41 @@ void launch_sh_eval_envmap(const float* coeffs, uint32_t K, uint32_t w, uint32_t
   else k_sh_eval_envmap<16><<<grid, 256, 0, s>>>(coeffs, w, h, scale, col_tab, row_tab, out);
 }
 
+// Sky SH evaluated along directions: shaders/skybox_sh.rmiss:14-25 with the
+// coefficient count fixed to K (the reference sums 16 bands, 256 terms, over a
+// 16-coefficient buffer).
+template <int LMAX>
+__global__ void k_sh_eval_dirs(const float* __restrict__ coeffs, const float* __restrict__ dirs, uint32_t n,
+                               float* __restrict__ out) {
+  constexpr int K = sh_k<LMAX>();
+  __shared__ float c[3 * K];
+  if (threadIdx.x < 3 * K) c[threadIdx.x] = coeffs[threadIdx.x];
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x = dirs[3 * size_t(i)], y = dirs[3 * size_t(i) + 1], z = dirs[3 * size_t(i) + 2];
+  const float rn = rsqrtf(x * x + y * y + z * z);
+  x *= rn; y *= rn; z *= rn;
+  float Y[16];
+  sh_basis<LMAX>(x, y, z, Y);
+  float r = 0.f, g = 0.f, b = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    r = fmaf(c[3 * k], Y[k], r);
+    g = fmaf(c[3 * k + 1], Y[k], g);
+    b = fmaf(c[3 * k + 2], Y[k], b);
+  }
+  out[3 * size_t(i)] = r;
+  out[3 * size_t(i) + 1] = g;
+  out[3 * size_t(i) + 2] = b;
+}
+
+void launch_sh_eval_dirs(const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n, float* out,
+                         cudaStream_t s) {
+  if (n == 0) return;
+  const uint32_t grid = (n + 255) / 256;
+  if (lmax == 3) k_sh_eval_dirs<3><<<grid, 256, 0, s>>>(coeffs, dirs, n, out);
+  else k_sh_eval_dirs<2><<<grid, 256, 0, s>>>(coeffs, dirs, n, out);
+}
+
 }  // namespace vlbk

@@ -630,6 +630,91 @@ void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* sr
   if (njobs) k_scatter_rows<<<dim3(16, njobs), 256, 0, s>>>(src, dst, src_probe0, nprobes, K);
 }
 
+// ---- probe evaluation: the consumer side of a baked grid -------------------------
+// Restates shaders/main.rchit:124-168 with shaders/sh.rmiss:23-39 (intended
+// math; the reference's grid-origin, probe-index, coefficient-stride and 0/0
+// faults are not reproduced).  One thread per shading point: the cell of
+// the grid holding the point, its 8 corner probes (gridVertices order: bit 2
+// x, bit 1 y, bit 0 z), a visibility ray from point + bias * n toward each
+// probe (any hit in (0, |d|), per-lane walk: the rays of a warp share
+// nothing), and the distance-weighted mean of the visible probes' SH
+// evaluated at the normal.
+__device__ __forceinline__ uint32_t ref_grid_index(const uint32_t* cnt, uint32_t i, uint32_t j, uint32_t k) {
+  // breadth-first grid order of LightBaker::probePositionsFromBoudingBox
+  const uint32_t q = j == 0 ? i : cnt[0] + i * (cnt[1] - 1) + (j - 1);
+  return k == 0 ? q : cnt[0] * cnt[1] + q * (cnt[2] - 1) + (k - 1);
+}
+
+template <int LMAX>
+__global__ void __launch_bounds__(128) k_probe_eval(const ProbeEvalArgs a) {
+  constexpr int K = sh_k<LMAX>();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  float x[3], nv[3];
+  for (int c = 0; c < 3; ++c) {
+    x[c] = a.points[3 * size_t(i) + c];
+    nv[c] = a.normals[3 * size_t(i) + c];
+  }
+  const float rn = rsqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+  for (float& c : nv) c *= rn;
+  float Y[16];
+  sh_basis<LMAX>(nv[0], nv[1], nv[2], Y);
+  const float o[3] = {fmaf(a.bias, nv[0], x[0]), fmaf(a.bias, nv[1], x[1]), fmaf(a.bias, nv[2], x[2])};
+  int cell[3];
+  for (int c = 0; c < 3; ++c) {
+    const int hi = max(int(a.counts[c]) - 2, 0);
+    cell[c] = hi == 0 ? 0 : min(max(int(floorf(__fdiv_rn(__fsub_rn(x[c], a.org[c]), a.step[c]))), 0), hi);
+  }
+  const float wmax = sqrtf(a.step[0] * a.step[0] + a.step[1] * a.step[1] + a.step[2] * a.step[2]);
+  float sum[3] = {0.f, 0.f, 0.f}, ws = 0.f;
+  uint32_t mask = 0;
+  Work w;
+  for (int c = 0; c < 8; ++c) {
+    uint32_t ijk[3];
+    float d[3];
+    for (int e = 0; e < 3; ++e) {
+      ijk[e] = min(uint32_t(cell[e]) + ((uint32_t(c) >> (2 - e)) & 1u), a.counts[e] - 1);
+      const float p = __fadd_rn(a.org[e], __fmul_rn(a.step[e], float(ijk[e])));
+      d[e] = p - x[e];
+    }
+    const float t = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    bool visible = true;
+    if (t > 0.f && a.ntris) {
+      const float it = 1.0f / t;
+      const float dx = d[0] * it, dy = d[1] * it, dz = d[2] * it;
+      RayCtx ray;
+      make_ray(ray, o[0], o[1], o[2], dx, dy, dz);
+      bool act = true;
+      float tb = t;
+      int slot = -1, id = -1;
+      traverse<true, false, true>(octant_of(dx, dy, dz), ray, act, a.nodes, a.tris, a.ntris, 0.0f, tb, slot, id,
+                                  a.err, w);
+      visible = slot < 0;
+    }
+    if (!visible) continue;
+    mask |= 1u << c;
+    const float wc = wmax - t;
+    const float* cp = a.coeffs + size_t(ref_grid_index(a.counts, ijk[0], ijk[1], ijk[2])) * K * 3;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      float e = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k) e = fmaf(__ldg(cp + 3 * k + ch), Y[k], e);
+      sum[ch] = fmaf(wc, e, sum[ch]);
+    }
+    ws += wc;
+  }
+  for (int ch = 0; ch < 3; ++ch) a.out[3 * size_t(i) + ch] = ws > 0.f ? sum[ch] / ws : 0.f;
+  if (a.vis) a.vis[i] = uint8_t(mask);
+}
+
+void launch_probe_eval(const ProbeEvalArgs& a, uint32_t lmax, cudaStream_t s) {
+  if (!a.n) return;
+  const uint32_t g = (a.n + 127) / 128;
+  if (lmax == 3) k_probe_eval<3><<<g, 128, 0, s>>>(a);
+  else k_probe_eval<2><<<g, 128, 0, s>>>(a);
+}
+
 void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s) {
   if (a.K == 9) launch<1, 9, false>(a, num_sms, s);
   else launch<1, 16, false>(a, num_sms, s);

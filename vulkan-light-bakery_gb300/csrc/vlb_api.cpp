@@ -1338,6 +1338,77 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
   return finish(ctx, true);
 }
 
+// ---- evaluating a baked grid ------------------------------------------------------------------
+vlb_status vlb_probe_eval(vlb_ctx* ctx, const vlb_scene* scene, const float* coeffs, uint32_t lmax,
+                          const vlb_probe_grid* g, const float* points, const float* normals, uint32_t n,
+                          float shadow_bias, float* out_rgb, uint8_t* vis_mask) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
+  if (!g) return fail(ctx, VLB_ERR_INVALID, "null grid");
+  if (scene && scene->ctx != ctx) return fail(ctx, VLB_ERR_INVALID, "scene belongs to another context");
+  uint64_t nprobes = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (g->counts[a] == 0) return fail(ctx, VLB_ERR_INVALID, "grid counts must be positive");
+    if (g->counts[a] > 1 && !(g->step[a] > 0.f && std::isfinite(g->step[a])))
+      return fail(ctx, VLB_ERR_INVALID, "grid step must be positive and finite on axes with more than one probe");
+    nprobes *= g->counts[a];
+  }
+  if (nprobes > 0xFFFFFFFFull) return fail(ctx, VLB_ERR_INVALID, "grid too large");
+  if (n == 0) return VLB_OK;
+  if (!coeffs || !points || !normals || !out_rgb) return fail(ctx, VLB_ERR_INVALID, "null array");
+  const uint32_t K = k_of(lmax);
+  vlb_status st;
+  const void *dc, *dp, *dn;
+  OutBuf ob, ov;
+  if ((st = stage_in(ctx, coeffs, nprobes * K * 12, "eval_coeffs", &dc)) ||
+      (st = stage_in(ctx, points, size_t(n) * 12, "eval_points", &dp)) ||
+      (st = stage_in(ctx, normals, size_t(n) * 12, "eval_normals", &dn)) ||
+      (st = stage_out(ctx, out_rgb, size_t(n) * 12, "eval_out", &ob)) ||
+      (st = stage_out(ctx, vis_mask, n, "eval_vis", &ov)))
+    return st;
+  vlbk::ProbeEvalArgs a{};
+  if (scene && scene->ntris) { a.nodes = scene->nodes; a.tris = scene->tris; a.ntris = scene->ntris; }
+  a.coeffs = static_cast<const float*>(dc);
+  for (int c = 0; c < 3; ++c) { a.org[c] = g->origin[c]; a.step[c] = g->step[c]; a.counts[c] = g->counts[c]; }
+  a.points = static_cast<const float*>(dp);
+  a.normals = static_cast<const float*>(dn);
+  a.n = n;
+  a.bias = shadow_bias;
+  a.out = static_cast<float*>(ob.dev);
+  a.vis = static_cast<uint8_t*>(ov.dev);
+  a.err = ctx->d_err;
+  {
+    KScope k(ctx, "probe_eval");
+    vlbk::launch_probe_eval(a, lmax, ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, ov))) return st;
+  return finish(ctx, ob.host || ov.host);
+}
+
+vlb_status vlb_sh_eval_dirs(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n,
+                            float* out_rgb) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
+  if (n == 0) return VLB_OK;
+  if (!coeffs || !dirs || !out_rgb) return fail(ctx, VLB_ERR_INVALID, "null array");
+  vlb_status st;
+  const void *dc, *dd;
+  OutBuf ob;
+  if ((st = stage_in(ctx, coeffs, size_t(k_of(lmax)) * 12, "evald_coeffs", &dc)) ||
+      (st = stage_in(ctx, dirs, size_t(n) * 12, "evald_dirs", &dd)) ||
+      (st = stage_out(ctx, out_rgb, size_t(n) * 12, "evald_out", &ob)))
+    return st;
+  {
+    KScope k(ctx, "sh_eval_dirs");
+    vlbk::launch_sh_eval_dirs(static_cast<const float*>(dc), lmax, static_cast<const float*>(dd), n,
+                              static_cast<float*>(ob.dev), ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob))) return st;
+  return finish(ctx, ob.host);
+}
+
 // ---- projection / reconstruction --------------------------------------------------------
 vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint32_t nprobes, const vlb_dirset* dirs,
                        uint32_t lmax, float* out) {

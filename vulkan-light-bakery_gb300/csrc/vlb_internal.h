@@ -200,6 +200,27 @@ void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_i
 void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
                          uint32_t njobs, uint32_t K, cudaStream_t s);
 
+// ---- probe evaluation (consumer side of the baked grid) ----------------------------
+struct ProbeEvalArgs {
+  const float4* nodes;
+  const float4* tris;
+  uint32_t ntris;           // 0: every probe visible
+  const float* coeffs;      // nprobes x K x 3, the bake's breadth-first grid order
+  float org[3], step[3];
+  uint32_t counts[3];
+  const float* points;      // n x 3
+  const float* normals;     // n x 3 (normalised in the kernel)
+  uint32_t n;
+  float bias;
+  float* out;               // n x 3
+  uint8_t* vis;             // n, bit c = corner c visible (or null)
+  int* err;
+};
+void launch_probe_eval(const ProbeEvalArgs& a, uint32_t lmax, cudaStream_t s);
+// out[i] = sum_k c_k Y_k(normalize(dirs[i])), K = (lmax+1)^2 coefficients.
+void launch_sh_eval_dirs(const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n, float* out,
+                         cudaStream_t s);
+
 }  // namespace vlbk
 
 // ---- host internals shared by the C ABI translation units ----------------------

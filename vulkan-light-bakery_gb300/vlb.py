@@ -52,6 +52,10 @@ class BakeDebug(C.Structure):
     _fields_ = [("hit_tri", C.c_void_p), ("shadow", C.c_void_p), ("radiance", C.c_void_p)]
 
 
+class ProbeGrid(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("step", C.c_float * 3), ("counts", C.c_uint32 * 3)]
+
+
 class BakeJob(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("probe_xyz", C.c_void_p), ("nprobes", C.c_uint32),
                 ("params", C.c_void_p), ("out", C.c_void_p)]
@@ -132,6 +136,8 @@ def _load() -> C.CDLL:
         "vlb_gltf_read_light": (I32, [C.c_char_p, C.c_size_t, P, C.POINTER(U32), P, C.c_size_t,
                                       C.POINTER(C.c_size_t)]),
         "vlb_gltf_last_error": (C.c_char_p, []),
+        "vlb_probe_eval": (I32, [P, P, P, U32, P, P, P, U32, F32, P, P]),
+        "vlb_sh_eval_dirs": (I32, [P, P, U32, P, U32, P]),
         "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
         "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
         "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
@@ -298,6 +304,28 @@ class Context:
         self.check(lib.vlb_batch_autotune(self.h, arr, len(jobs), C.byref(params), reps, C.byref(best), C.byref(ms)))
         del keep
         return best, float(ms.value)
+
+    def probe_eval(self, scene, coeffs, lmax: int, origin, step, counts, points, normals, shadow_bias: float = 0.005):
+        """Evaluate a baked grid at shading points; returns (rgb [n,3], visibility mask [n])."""
+        g = ProbeGrid()
+        for a in range(3):
+            g.origin[a], g.step[a], g.counts[a] = float(origin[a]), float(step[a]), int(counts[a])
+        c = coeffs if hasattr(coeffs, "data_ptr") else _f32(coeffs)
+        pt = points if hasattr(points, "data_ptr") else _f32(points).reshape(-1, 3)
+        nm = normals if hasattr(normals, "data_ptr") else _f32(normals).reshape(-1, 3)
+        n = int(pt.shape[0])
+        out = np.empty((n, 3), np.float32)
+        vis = np.empty(n, np.uint8)
+        self.check(lib.vlb_probe_eval(self.h, None if scene is None else scene.h, _ptr(c), lmax, C.byref(g), _ptr(pt),
+                                      _ptr(nm), n, shadow_bias, _ptr(out), _ptr(vis)))
+        return out, vis
+
+    def sh_eval_dirs(self, coeffs, lmax: int, dirs):
+        c = _f32(coeffs).reshape(-1)
+        d = _f32(dirs).reshape(-1, 3)
+        out = np.empty((d.shape[0], 3), np.float32)
+        self.check(lib.vlb_sh_eval_dirs(self.h, _ptr(c), lmax, _ptr(d), d.shape[0], _ptr(out)))
+        return out
 
     def project(self, radiance, nprobes: int, dirs: "DirSet", lmax: int, dtype: int = DTYPE_F32, out=None):
         K = k_of(lmax)
