@@ -367,6 +367,24 @@ vlb_status vlb_gltf_write_light(const char* gltf_json, size_t json_len, const fl
  * gives zeros and *coeffs_bytes = 0.  coeffs NULL: only the sizes. */
 vlb_status vlb_gltf_read_light(const char* gltf_json, size_t json_len, float grid_step[3], uint32_t* coeff_count,
                                void* coeffs, size_t coeffs_cap, size_t* coeffs_bytes);
+/* Scene geometry from a .gltf (external .bin or data-URI buffers) or .glb file,
+ * host only.  Replaces the geometry side of Scene_t::loadNodes / loadNode /
+ * fetchVertices / fetchIndices / loadMatrix (src/scene_manager.cpp:257-337,
+ * 445-538, 860-870): the triangles of glTF scene 0 in world space (node
+ * local matrix T*R*S*M, multiplied along the parent chain as the reference's
+ * TLAS instances are), u8/u16/u32 indices, per-triangle albedo = the
+ * material's baseColorFactor RGB (1 without a material; textures are not
+ * sampled), bounds = the world AABB of the vertices (the reference's
+ * getBounds also starts at the origin: vlb_scene_bounds(scene, 1, ...) gives
+ * that form).  Only triangle primitives (mode 4). */
+typedef struct vlb_gltf_mesh vlb_gltf_mesh;
+vlb_status vlb_gltf_mesh_load(const char* path, vlb_gltf_mesh** out);
+void vlb_gltf_mesh_free(vlb_gltf_mesh* mesh);
+vlb_status vlb_gltf_mesh_info(const vlb_gltf_mesh* mesh, uint32_t* nverts, uint32_t* ntris, float bounds[6]);
+/* positions nverts*3, indices ntris*3, albedo ntris*3 (any may be NULL) */
+vlb_status vlb_gltf_mesh_get(const vlb_gltf_mesh* mesh, float* positions, uint32_t* indices, float* albedo);
+/* vlb_gltf_mesh_load + vlb_scene_create in one call. */
+vlb_status vlb_scene_create_gltf(vlb_ctx* ctx, const char* path, vlb_scene** out);
 /* Message of the calling thread's last failed vlb_gltf_* call (never NULL). */
 const char* vlb_gltf_last_error(void);
 
@@ -398,6 +416,25 @@ vlb_status vlb_probe_eval(vlb_ctx* ctx, const vlb_scene* scene, const float* coe
  * 16-coefficient buffer). coeffs: K x 3. */
 vlb_status vlb_sh_eval_dirs(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n,
                             float* out_rgb);
+
+/* ---- debug env-map images ---------------------------------------------------------
+ * The reference writes, for every probe, its traced equirect env map as an
+ * R8G8B8A8 UNORM image (src/baker/env_map_generator.hpp:39) to "<probe>.png"
+ * (light_baker.cpp:306-307, EnvMapGenerator::saveImage
+ * env_map_generator.cpp:73-112); texels are sRGB-encoded by the shaders
+ * (env_map.rchit:82, main.rmiss:40, main.rchit:49-56) with alpha 1.
+ * vlb_encode_rgba8: rgba[i] = UNORM8(srgb ? sRGB(scale*rgb[i]) : scale*rgb[i]),
+ * alpha 255 (sh_sum.comp:51 is scale 1250 without sRGB).  Host or device. */
+vlb_status vlb_encode_rgba8(vlb_ctx* ctx, const float* rgb, uint32_t n, float scale, uint32_t srgb, uint8_t* rgba);
+/* One probe's env map as the reference's debug image: the probe's traced
+ * radiance over params->dirs, which must be vlb_dirset_create_equirect(w, h)
+ * (sample s = y*w + x is pixel (x, y)), sRGB-encoded into w x h RGBA8. */
+vlb_status vlb_render_envmap(vlb_ctx* ctx, const vlb_scene* scene, const float probe_xyz[3],
+                             const vlb_bake_params* params, uint32_t w, uint32_t h, uint8_t* rgba);
+/* Host only: 8-bit RGBA PNG (stored deflate blocks) and binary PPM (alpha dropped). */
+vlb_status vlb_image_write_png(const char* path, const uint8_t* rgba, uint32_t w, uint32_t h);
+vlb_status vlb_image_write_ppm(const char* path, const uint8_t* rgba, uint32_t w, uint32_t h);
+const char* vlb_image_last_error(void);
 
 /* ---- synthetic inputs (bench and tests) -------------------------------------
  * Seeded SplitMix64 generators for the benchmark workloads.  The room is the

@@ -1409,6 +1409,50 @@ vlb_status vlb_sh_eval_dirs(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, co
   return finish(ctx, ob.host);
 }
 
+// ---- debug env-map images -----------------------------------------------------------------
+vlb_status vlb_encode_rgba8(vlb_ctx* ctx, const float* rgb, uint32_t n, float scale, uint32_t srgb, uint8_t* rgba) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (n == 0) return VLB_OK;
+  if (!rgb || !rgba) return fail(ctx, VLB_ERR_INVALID, "null array");
+  vlb_status st;
+  const void* d;
+  OutBuf ob;
+  if ((st = stage_in(ctx, rgb, size_t(n) * 12, "enc_in", &d)) ||
+      (st = stage_out(ctx, rgba, size_t(n) * 4, "enc_out", &ob)))
+    return st;
+  {
+    KScope k(ctx, "encode_rgba8");
+    vlbk::launch_encode_rgba8(static_cast<const float*>(d), n, scale, srgb ? 1u : 0u,
+                              static_cast<uint8_t*>(ob.dev), ctx->num_sms, ctx->stream);
+  }
+  if ((st = copy_out(ctx, ob))) return st;
+  return finish(ctx, ob.host);
+}
+
+vlb_status vlb_render_envmap(vlb_ctx* ctx, const vlb_scene* scene, const float probe_xyz[3],
+                             const vlb_bake_params* p, uint32_t w, uint32_t h, uint8_t* rgba) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (!p || !p->dirs || !probe_xyz || !rgba) return fail(ctx, VLB_ERR_INVALID, "null argument");
+  if (uint64_t(w) * h != p->dirs->n || w == 0)
+    return fail(ctx, VLB_ERR_INVALID, "params->dirs must hold w*h = %llu samples (it holds %u)",
+                (unsigned long long)(uint64_t(w) * h), p->dirs->n);
+  if (p->precision == VLB_PREC_FUSED)
+    return fail(ctx, VLB_ERR_UNSUPPORTED, "the fused schedule keeps no per-ray radiance");
+  const size_t S = p->dirs->n;
+  void *rad, *sh;
+  vlb_status st;
+  if ((st = scratch(ctx, "env_rad", S * 12, &rad)) || (st = scratch(ctx, "env_sh", 16 * 12, &sh))) return st;
+  float probe[3] = {probe_xyz[0], probe_xyz[1], probe_xyz[2]};
+  const void* dprobe;
+  if ((st = stage_in(ctx, probe, 12, "env_probe", &dprobe))) return st;
+  vlb_bake_debug dbg{nullptr, nullptr, static_cast<float*>(rad)};
+  if ((st = vlb_bake_ex(ctx, scene, static_cast<const float*>(dprobe), 1, p, static_cast<float*>(sh), &dbg)))
+    return st;
+  return vlb_encode_rgba8(ctx, static_cast<const float*>(rad), uint32_t(S), 1.0f, 1u, rgba);
+}
+
 // ---- projection / reconstruction --------------------------------------------------------
 vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint32_t nprobes, const vlb_dirset* dirs,
                        uint32_t lmax, float* out) {

@@ -220,6 +220,9 @@ void launch_probe_eval(const ProbeEvalArgs& a, uint32_t lmax, cudaStream_t s);
 // out[i] = sum_k c_k Y_k(normalize(dirs[i])), K = (lmax+1)^2 coefficients.
 void launch_sh_eval_dirs(const float* coeffs, uint32_t lmax, const float* dirs, uint32_t n, float* out,
                          cudaStream_t s);
+// RGBA8 UNORM from RGB floats: scale, optional sRGB, clamp, round; alpha 255.
+void launch_encode_rgba8(const float* rgb, size_t n, float scale, uint32_t srgb, uint8_t* out, int num_sms,
+                         cudaStream_t s);
 
 }  // namespace vlbk
 

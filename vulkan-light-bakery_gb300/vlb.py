@@ -136,8 +136,18 @@ def _load() -> C.CDLL:
         "vlb_gltf_read_light": (I32, [C.c_char_p, C.c_size_t, P, C.POINTER(U32), P, C.c_size_t,
                                       C.POINTER(C.c_size_t)]),
         "vlb_gltf_last_error": (C.c_char_p, []),
+        "vlb_gltf_mesh_load": (I32, [C.c_char_p, C.POINTER(P)]),
+        "vlb_gltf_mesh_free": (None, [P]),
+        "vlb_gltf_mesh_info": (I32, [P, C.POINTER(U32), C.POINTER(U32), P]),
+        "vlb_gltf_mesh_get": (I32, [P, P, P, P]),
+        "vlb_scene_create_gltf": (I32, [P, C.c_char_p, C.POINTER(P)]),
         "vlb_probe_eval": (I32, [P, P, P, U32, P, P, P, U32, F32, P, P]),
         "vlb_sh_eval_dirs": (I32, [P, P, U32, P, U32, P]),
+        "vlb_encode_rgba8": (I32, [P, P, U32, F32, U32, P]),
+        "vlb_render_envmap": (I32, [P, P, P, P, U32, U32, P]),
+        "vlb_image_write_png": (I32, [C.c_char_p, P, U32, U32]),
+        "vlb_image_write_ppm": (I32, [C.c_char_p, P, U32, U32]),
+        "vlb_image_last_error": (C.c_char_p, []),
         "vlb_project": (I32, [P, P, I32, U32, P, U32, P]),
         "vlb_sh_eval_envmap": (I32, [P, P, U32, U32, U32, F32, P]),
         "vlb_synth_box_scene": (I32, [U64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
@@ -237,6 +247,12 @@ class Context:
     def scene(self, positions, indices, albedo=None, stride_bytes: int = 12) -> "Scene":
         return Scene(self, positions, indices, albedo, stride_bytes)
 
+    def scene_gltf(self, path) -> "Scene":
+        """Device scene straight from a .gltf / .glb file."""
+        h = C.c_void_p()
+        self.check(lib.vlb_scene_create_gltf(self.h, str(path).encode(), C.byref(h)))
+        return Scene._wrap(self, h)
+
     def fibonacci(self, n: int, frame: int = FRAME_WORLD) -> "DirSet":
         h = C.c_void_p()
         self.check(lib.vlb_dirset_create_fibonacci(self.h, n, frame, C.byref(h)))
@@ -319,6 +335,20 @@ class Context:
         self.check(lib.vlb_probe_eval(self.h, None if scene is None else scene.h, _ptr(c), lmax, C.byref(g), _ptr(pt),
                                       _ptr(nm), n, shadow_bias, _ptr(out), _ptr(vis)))
         return out, vis
+
+    def encode_rgba8(self, rgb, scale: float = 1.0, srgb: bool = True):
+        x = _f32(rgb)
+        n = x.size // 3
+        out = np.empty(x.shape[:-1] + (4,), np.uint8)
+        self.check(lib.vlb_encode_rgba8(self.h, _ptr(x), n, scale, 1 if srgb else 0, _ptr(out)))
+        return out
+
+    def render_envmap(self, scene, probe, params: BakeParams, w: int, h: int):
+        """The reference's per-probe debug image: [h, w, 4] RGBA8 (sRGB)."""
+        pr = _f32(probe).reshape(3)
+        out = np.empty((h, w, 4), np.uint8)
+        self.check(lib.vlb_render_envmap(self.h, scene.h, _ptr(pr), C.byref(params), w, h, _ptr(out)))
+        return out
 
     def sh_eval_dirs(self, coeffs, lmax: int, dirs):
         c = _f32(coeffs).reshape(-1)
@@ -418,6 +448,16 @@ def service_plan(probes, nbytes, max_batch_probes: int, budget_bytes: int):
     return np.where(out == 0xFFFFFFFF, -1, out.astype(np.int64)), nb.value
 
 
+def image_write(path, rgba) -> None:
+    """Writes [h, w, 4] RGBA8 as PNG (".png") or PPM (anything else); host only."""
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w = a.shape[:2]
+    fn = lib.vlb_image_write_png if str(path).endswith(".png") else lib.vlb_image_write_ppm
+    st = fn(str(path).encode(), _ptr(a), w, h)
+    if st != OK:
+        raise VlbError(st, lib.vlb_image_last_error().decode())
+
+
 def gltf_write_light(gltf_text: str, coeffs, grid_step) -> str:
     """The reference's baked_<name>.gltf text for coefficients [n, K, 3] (host only)."""
     src = gltf_text.encode()
@@ -434,6 +474,26 @@ def gltf_write_light(gltf_text: str, coeffs, grid_step) -> str:
     if st != OK:
         raise VlbError(st, lib.vlb_gltf_last_error().decode())
     return buf.value.decode()
+
+
+def gltf_load_mesh(path):
+    """(positions [nv,3], indices [nt,3], albedo [nt,3], bounds[6]) of a .gltf/.glb (host only)."""
+    h = C.c_void_p()
+    st = lib.vlb_gltf_mesh_load(str(path).encode(), C.byref(h))
+    if st != OK:
+        raise VlbError(st, lib.vlb_gltf_last_error().decode())
+    try:
+        nv, nt = C.c_uint32(), C.c_uint32()
+        b = np.zeros(6, np.float32)
+        lib.vlb_gltf_mesh_info(h, C.byref(nv), C.byref(nt), _ptr(b))
+        pos = np.empty((nv.value, 3), np.float32)
+        idx = np.empty((nt.value, 3), np.uint32)
+        alb = np.empty((nt.value, 3), np.float32)
+        lib.vlb_gltf_mesh_get(h, _ptr(pos) if pos.size else None, _ptr(idx) if idx.size else None,
+                              _ptr(alb) if alb.size else None)
+        return pos, idx, alb, b
+    finally:
+        lib.vlb_gltf_mesh_free(h)
 
 
 def gltf_read_light(gltf_text: str):
@@ -499,6 +559,13 @@ class Scene:
                                        C.byref(h)))
         self.h = h
         self.ntris = ntris
+
+    @classmethod
+    def _wrap(cls, ctx: Context, h) -> "Scene":
+        s = cls.__new__(cls)
+        s.ctx, s.h = ctx, h
+        s.ntris = int(lib.vlb_scene_triangle_count(h))
+        return s
 
     def bounds(self, include_origin: bool = True) -> np.ndarray:
         b = np.empty(6, np.float32)
