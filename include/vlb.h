@@ -91,6 +91,15 @@ vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts
  * indices: ntris*3 u32.  tri_albedo: ntris*3 linear RGB, or NULL for 1. */
 vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t position_stride_bytes, uint32_t nverts,
                             const uint32_t* indices, uint32_t ntris, const float* tri_albedo, vlb_scene** out);
+/* The traversal tree is built by locally-ordered clustering (PLOC) of the
+ * LBVH's Morton-sorted triangles (surface-area nearest neighbours): fewer
+ * node visits per ray.  VLB_SCENE_TRAVERSAL_LBVH walks the Karras LBVH
+ * itself instead.  Results do not depend on the tree; the exported BVH is
+ * always the LBVH. */
+#define VLB_SCENE_TRAVERSAL_LBVH 1u
+vlb_status vlb_scene_create_ex(vlb_ctx* ctx, const float* positions, uint32_t position_stride_bytes,
+                               uint32_t nverts, const uint32_t* indices, uint32_t ntris, const float* tri_albedo,
+                               uint32_t flags, vlb_scene** out);
 void vlb_scene_destroy(vlb_scene* scene);
 uint32_t vlb_scene_triangle_count(const vlb_scene* scene);
 /* Replaces Scene_t::getBounds (src/scene_manager.hpp:214, cpp:497-507).  The

@@ -126,6 +126,28 @@ def test_traversal_modes_agree(ctx, nboxes, counts):
         assert not cls["unexplained"], cls["unexplained"][:10]
 
 
+@pytest.mark.parametrize("nboxes,counts", [(64, (16, 16, 16)), (4000, (6, 6, 6))])
+def test_traversal_trees_agree(ctx, nboxes, counts):
+    """The clustered traversal tree and the Karras LBVH give the same per-ray
+    decisions and radiance, bit for bit, and the clustered tree visits fewer
+    nodes."""
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=13, nboxes=nboxes, counts=counts)
+    skyh = ctx.sky(sky, 128)
+    ds = ctx.fibonacci(S)
+    res, work = [], []
+    for flags in (0, vlb.SCENE_TRAVERSAL_LBVH):
+        scene = ctx.scene(pos, idx, alb, flags=flags)
+        p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun, sky=skyh)
+        res.append(ctx.bake(scene, probes, p, debug=True))
+        st = vlb.trace_stats(ctx, scene, probes, p)
+        work.append(st["node_tests"] / (st["rays"] + st["shadow_rays"]))
+    (sa, ha, va, ra), (sb, hb, vb, rb) = res
+    print(f"node tests per ray: clustered {work[0]:.1f}, LBVH {work[1]:.1f}")
+    assert np.array_equal(ha, hb) and np.array_equal(va, vb)
+    assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+    assert work[0] < work[1]
+
+
 def test_empty_scene_sees_sky(ctx):
     sky = vlb.synth_cubemap(4, 32)
     pos = np.zeros((3, 3), np.float32)

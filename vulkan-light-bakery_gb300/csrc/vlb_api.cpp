@@ -464,6 +464,12 @@ vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts
 // ---- scene ----------------------------------------------------------------------------
 vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t stride_bytes, uint32_t nverts,
                             const uint32_t* indices, uint32_t ntris, const float* tri_albedo, vlb_scene** out) {
+  return vlb_scene_create_ex(ctx, positions, stride_bytes, nverts, indices, ntris, tri_albedo, 0, out);
+}
+
+vlb_status vlb_scene_create_ex(vlb_ctx* ctx, const float* positions, uint32_t stride_bytes, uint32_t nverts,
+                               const uint32_t* indices, uint32_t ntris, const float* tri_albedo, uint32_t flags,
+                               vlb_scene** out) {
   if (!ctx || !out) return VLB_ERR_INVALID;
   *out = nullptr;
   cudaSetDevice(ctx->device);
@@ -478,6 +484,9 @@ vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t strid
   if (ntris) VLB_CUDA(ctx, cudaMemcpy(hidx.data(), indices, hidx.size() * 4, cudaMemcpyDefault));
   for (size_t i = 0; i < hidx.size(); ++i)
     if (hidx[i] >= nverts) return fail(ctx, VLB_ERR_INVALID, "index %u out of range at %zu", hidx[i], i);
+  for (uint32_t v = 0; v < nverts; ++v)
+    for (int a = 0; a < 3; ++a)
+      if (!std::isfinite(hpos[size_t(v) * sf + a])) return fail(ctx, VLB_ERR_INVALID, "vertex %u is not finite", v);
   vlb_scene* sc = new (std::nothrow) vlb_scene();
   if (!sc) return VLB_ERR_OOM;
   sc->ctx = ctx; sc->ntris = ntris; sc->nverts = nverts;
@@ -524,7 +533,23 @@ vlb_status vlb_scene_create(vlb_ctx* ctx, const float* positions, uint32_t strid
       vlbk::launch_lbvh_build(b, ctx->stream, &launches);
       k.nkernels = launches;
     }
-    st = finish(ctx, true);
+    if (n > 1 && !(flags & VLB_SCENE_TRAVERSAL_LBVH)) {
+      void* pscr = nullptr;
+      if (cudaMalloc(&pscr, vlbk::ploc_scratch_bytes(n)) != cudaSuccess) {
+        cudaGetLastError();
+        st = fail(ctx, VLB_ERR_OOM, "traversal tree scratch allocation failed (%u triangles)", n);
+      } else {
+        int pl = 0;
+        KScope k(ctx, "ploc_build", 0);
+        // a stalled clustering (1) keeps the LBVH already packed into sc->nodes
+        if (vlbk::launch_ploc_build(sc->box + size_t(n - 1) * 6, n, sc->nodes, pscr, ctx->stream, &pl) < 0)
+          st = fail(ctx, VLB_ERR_INTERNAL, "traversal tree build failed");
+        k.nkernels = pl;
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(pscr);
+      }
+    }
+    if (st == VLB_OK) st = finish(ctx, true);
   }
   cudaFree(dpos); cudaFree(didx); if (dalb) cudaFree(dalb); cudaFree(scr);
   if (st != VLB_OK) { vlb_scene_destroy(sc); return st; }

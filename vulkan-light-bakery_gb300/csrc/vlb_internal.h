@@ -100,6 +100,13 @@ struct LbvhBuild {
 };
 size_t lbvh_scratch_bytes(uint32_t ntris);
 void launch_lbvh_build(const LbvhBuild& b, cudaStream_t s, int* launches);
+// Traversal tree by PLOC clustering over the Morton-sorted leaves
+// (k_ploc.cu): overwrites `nodes` (root 0) and returns 0; returns 1 with
+// `nodes` untouched if clustering stalls (more than 64 + 8 log2 n rounds),
+// -1 on a CUDA error or a round that merges nothing.
+size_t ploc_scratch_bytes(uint32_t ntris);
+int launch_ploc_build(const float* leaf_box, uint32_t n, float4* nodes, void* scratch, cudaStream_t s,
+                      int* launches);
 // Permutation of the probes by 24-bit Morton code inside `bounds` (min xyz,
 // max xyz), so that each 32-probe packet is spatially compact.  Returns the
 // number of kernels launched.

@@ -25,6 +25,7 @@ SKY_REF_BGRA_SWAP = 1
 PREC_FP32, PREC_FUSED, PREC_MIXED = 0, 1, 2
 BAKE_FORCE_FUSED_KERNEL = 1
 BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE = 2, 4
+SCENE_TRAVERSAL_LBVH = 1
 DTYPE_F32, DTYPE_BF16 = 0, 1
 
 
@@ -101,6 +102,7 @@ def _load() -> C.CDLL:
         "vlb_ctx_launch_count": (U64, [P]),
         "vlb_probe_grid_ref_order": (I32, [P, P, P, P]),
         "vlb_scene_create": (I32, [P, P, U32, U32, P, U32, P, C.POINTER(P)]),
+        "vlb_scene_create_ex": (I32, [P, P, U32, U32, P, U32, P, U32, C.POINTER(P)]),
         "vlb_scene_destroy": (None, [P]),
         "vlb_scene_triangle_count": (U32, [P]),
         "vlb_scene_bounds": (I32, [P, I32, P]),
@@ -244,8 +246,8 @@ class Context:
         return int(lib.vlb_ctx_launch_count(self.h))
 
     # objects
-    def scene(self, positions, indices, albedo=None, stride_bytes: int = 12) -> "Scene":
-        return Scene(self, positions, indices, albedo, stride_bytes)
+    def scene(self, positions, indices, albedo=None, stride_bytes: int = 12, flags: int = 0) -> "Scene":
+        return Scene(self, positions, indices, albedo, stride_bytes, flags)
 
     def scene_gltf(self, path) -> "Scene":
         """Device scene straight from a .gltf / .glb file."""
@@ -547,7 +549,7 @@ def trace_stats(ctx: Context, scene: "Scene", probes, params: BakeParams) -> dic
 
 
 class Scene:
-    def __init__(self, ctx: Context, positions, indices, albedo, stride_bytes: int):
+    def __init__(self, ctx: Context, positions, indices, albedo, stride_bytes: int, flags: int = 0):
         self.ctx = ctx
         pos = positions if hasattr(positions, "data_ptr") else _f32(positions)
         idx = indices if hasattr(indices, "data_ptr") else np.ascontiguousarray(indices, dtype=np.uint32)
@@ -555,8 +557,8 @@ class Scene:
         nverts = (pos.numel() if hasattr(pos, "numel") else pos.size) * 4 // stride_bytes
         ntris = (idx.numel() if hasattr(idx, "numel") else idx.size) // 3
         h = C.c_void_p()
-        ctx.check(lib.vlb_scene_create(ctx.h, _ptr(pos), stride_bytes, nverts, _ptr(idx), ntris, _ptr(alb),
-                                       C.byref(h)))
+        ctx.check(lib.vlb_scene_create_ex(ctx.h, _ptr(pos), stride_bytes, nverts, _ptr(idx), ntris, _ptr(alb),
+                                          flags, C.byref(h)))
         self.h = h
         self.ntris = ntris
 
