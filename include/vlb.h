@@ -273,8 +273,8 @@ typedef struct vlb_batch_schedule {
  * the library default {0, 1, 1}. */
 vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                           const vlb_batch_schedule* sched);
-/* Times the batch under each candidate schedule (directions per item x job
- * order, reps runs each, outputs written every run), stores the fastest in
+/* Times the batch under each candidate schedule (directions per item 1, 2,
+ * 4, 8, 16 x job order, reps runs each, outputs written every run), stores the fastest in
  * the context for later vlb_bake_batch calls with sched NULL and returns it
  * with its mean milliseconds per batch. */
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,

@@ -100,7 +100,7 @@ def test_batch_autotune(ctx, batch_world):
     ref = _singles(ctx, w, plist)
     jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
     sched, ms = ctx.batch_autotune(jobs, plist[0], reps=1)
-    assert sched.dirs_per_item in (8, 16, 32, 64, 128) and sched.cost_order in (0, 1) and ms > 0
+    assert sched.dirs_per_item in (1, 2, 4, 8, 16) and sched.cost_order in (0, 1) and ms > 0
     for _ in range(3):  # the tuned schedule, graph on
         outs = ctx.bake_batch(jobs, plist[0])
         assert all(np.array_equal(a, b) for a, b in zip(outs, ref))

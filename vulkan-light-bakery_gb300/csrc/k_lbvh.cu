@@ -228,14 +228,10 @@ __global__ void k_probe_codes(const float* __restrict__ probes, uint32_t n, floa
   vals[i] = i;
 }
 
-// Whole probe ordering in one CTA for n <= kSmallSort: codes, then three
+// Whole probe ordering in one CTA of 1024 threads for any n: codes, then three
 // stable 8-bit LSD passes (histogram, scan, ranked scatter) through global
-// ping-pong buffers, with the same warp ranking as k_rs_scatter.  One launch
-// instead of ten for the probe counts of a typical bake request.
-constexpr uint32_t kSmallSort = 16384;
-
-// The whole sort by one CTA of 1024 threads (any n; one launch for up to
-// kSmallSort probes, one CTA per job in the batched bake).
+// ping-pong buffers, with the same warp ranking as k_rs_scatter.  Used for
+// the batched bake's jobs above the counting sort's limit (one CTA per job).
 __device__ __forceinline__ void probe_sort_cta(const float* __restrict__ probes, uint32_t n, float lox, float loy,
                                                float loz, float sx, float sy, float sz, uint32_t* ka, uint32_t* va,
                                                uint32_t* kb, uint32_t* vb, uint32_t* order) {
@@ -314,11 +310,69 @@ __device__ __forceinline__ void probe_sort_cta(const float* __restrict__ probes,
   }
 }
 
-__global__ void __launch_bounds__(1024) k_probe_order_small(const float* __restrict__ probes, uint32_t n, float lox,
-                                                            float loy, float loz, float sx, float sy, float sz,
-                                                            uint32_t* ka, uint32_t* va, uint32_t* kb, uint32_t* vb,
-                                                            uint32_t* order) {
-  probe_sort_cta(probes, n, lox, loy, loz, sx, sy, sz, ka, va, kb, vb, order);
+// Probe order for n <= kCountMax probes in one CTA: a counting sort on the
+// top 12 bits of the 24-bit Morton code (16^3 cells inside the bounds) with
+// shared-memory histogram, scan and atomic cursors -- a handful of barriers
+// instead of the radix sort's dozens.  The order inside a cell follows the
+// atomics; the bake's results never depend on the probe order (each ray's
+// walk and each probe's sums are independent of its packet), only its speed.
+constexpr uint32_t kCountMax = 16384;
+constexpr int kCountBins = 4096;
+
+__device__ __forceinline__ void probe_sort_count(const float* __restrict__ probes, uint32_t n, float lox, float loy,
+                                                 float loz, float sx, float sy, float sz,
+                                                 uint32_t* __restrict__ order) {
+  __shared__ uint32_t bin[kCountBins];
+  __shared__ uint32_t wsum[32];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto cell = [&](uint32_t i) -> uint32_t {
+    auto q = [](float c, float lo, float s) -> uint32_t {
+      const float v = (c - lo) * s;
+      if (!(v > 0.f)) return 0u;
+      return min(__float2uint_rz(v), 255u);
+    };
+    const uint32_t x = q(probes[3 * size_t(i)], lox, sx), y = q(probes[3 * size_t(i) + 1], loy, sy),
+                   z = q(probes[3 * size_t(i) + 2], loz, sz);
+    return ((expand_bits10(x) << 2) | (expand_bits10(y) << 1) | expand_bits10(z)) >> 12;
+  };
+  for (uint32_t b = tid; b < kCountBins; b += 1024) bin[b] = 0;
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += 1024) atomicAdd(&bin[cell(i)], 1u);
+  __syncthreads();
+  // exclusive scan: 4 bins per thread, warp shuffles, then the 32 warp totals
+  uint32_t v[4], t = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { v[k] = bin[4 * tid + k]; t += v[k]; }
+  uint32_t incl = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= uint32_t(o)) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = wsum[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= uint32_t(o)) wi += y;
+    }
+    wsum[lane] = wi - w;
+  }
+  __syncthreads();
+  uint32_t run = wsum[warp] + incl - t;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) { bin[4 * tid + k] = run; run += v[k]; }
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += 1024) order[atomicAdd(&bin[cell(i)], 1u)] = i;
+}
+
+__global__ void __launch_bounds__(1024) k_probe_order_count(const float* __restrict__ probes, uint32_t n, float lox,
+                                                             float loy, float loz, float sx, float sy, float sz,
+                                                             uint32_t* __restrict__ order) {
+  probe_sort_count(probes, n, lox, loy, loz, sx, sy, sz, order);
 }
 
 __global__ void __launch_bounds__(1024) k_probe_order_batch(const BakeJobDev* __restrict__ jobs) {
@@ -328,6 +382,10 @@ __global__ void __launch_bounds__(1024) k_probe_order_batch(const BakeJobDev* __
   for (int i = 0; i < 3; ++i) {
     const float e = j.bounds[3 + i] - j.bounds[i];
     s[i] = e > 0.f ? 256.0f / e : 0.f;
+  }
+  if (n <= kCountMax) {
+    probe_sort_count(j.probes, n, j.bounds[0], j.bounds[1], j.bounds[2], s[0], s[1], s[2], j.order);
+    return;
   }
   uint32_t* sc = j.sort_scratch;  // 4 arrays of n
   probe_sort_cta(j.probes, n, j.bounds[0], j.bounds[1], j.bounds[2], s[0], s[1], s[2], sc, sc + n, sc + 2 * size_t(n),
@@ -341,8 +399,8 @@ void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream
 size_t probe_order_scratch_bytes(uint32_t n) {
   const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
   const size_t a = (size_t(n) * 4 + 255) / 256 * 256;
-  // multi-pass sort: 3 key/value buffers + histogram; one-CTA sort: 4 buffers
-  return std::max(3 * a + size_t(nblk) * 256 * 4, 4 * a);
+  // multi-pass radix sort (above the counting sort's limit): 3 key/value buffers + histogram
+  return 3 * a + size_t(nblk) * 256 * 4;
 }
 
 int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
@@ -359,10 +417,8 @@ int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], u
     const float e = bounds[3 + i] - bounds[i];
     s[i] = e > 0.f ? 256.0f / e : 0.f;
   }
-  if (n <= kSmallSort) {
-    uint32_t* va = reinterpret_cast<uint32_t*>(base + 3 * a);  // fourth buffer (see probe_order_scratch_bytes)
-    k_probe_order_small<<<1, 1024, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka, va,
-                                            kb, vb, order);
+  if (n <= kCountMax) {
+    k_probe_order_count<<<1, 1024, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], order);
     return 1;
   }
   k_probe_codes<<<(n + 255) / 256, 256, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka,

@@ -627,7 +627,7 @@ __global__ void k_scatter_rows(const float* __restrict__ src, float* const* __re
 
 void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
                          uint32_t njobs, uint32_t K, cudaStream_t s) {
-  if (njobs) k_scatter_rows<<<dim3(16, njobs), 256, 0, s>>>(src, dst, src_probe0, nprobes, K);
+  if (njobs) k_scatter_rows<<<dim3(64, njobs), 256, 0, s>>>(src, dst, src_probe0, nprobes, K);
 }
 
 // ---- probe evaluation: the consumer side of a baked grid -------------------------

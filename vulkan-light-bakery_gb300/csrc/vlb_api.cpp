@@ -1040,6 +1040,7 @@ struct BatchPlan {
   uint64_t rows = 0;
   size_t tile_bytes = 0, host_probe_bytes = 0;
   uint32_t K = 0;
+  uint32_t max_probes = 0;  // largest job
   bool bf16 = false;
 };
 
@@ -1080,6 +1081,7 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
     if (j.nprobes == 0) continue;
     if (!j.probe_xyz || !j.out) return fail(ctx, VLB_ERR_INVALID, "job %u: null probes or output", i);
     b.idx = i; b.p = p; b.nprobes = j.nprobes; b.S = p->dirs->n;
+    pl->max_probes = std::max(pl->max_probes, j.nprobes);
     b.cost = double(j.nprobes) * b.S * std::log2(double(j.scene->ntris) + 2.0);
     uint32_t g = 0;
     while (g < pl->groups.size() && pl->groups[g].dirs != p->dirs) ++g;
@@ -1189,10 +1191,12 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
   const size_t esz = pl.bf16 ? 2 : 4;
   uint64_t warp_rays = 0;
   for (const auto& b : pl.jobs) warp_rays += (uint64_t(b.nprobes) + 31) / 32 * b.S;
+  // directions per work item: at least ~16 items per resident warp (item
+  // times vary widely, so fewer items leave warps idle at the tail), at most 8
   uint32_t dpw = sc.dirs_per_item;
   if (!dpw) {
-    const uint64_t target = 8ull * 32 * uint64_t(ctx->num_sms);
-    dpw = uint32_t(std::min<uint64_t>(32, std::max<uint64_t>(1, warp_rays / target)));
+    const uint64_t target = 16ull * 32 * uint64_t(ctx->num_sms);
+    dpw = uint32_t(std::min<uint64_t>(8, std::max<uint64_t>(1, warp_rays / target)));
   }
   auto& table = ctx->batch_table;
   table.assign(ntable, vlbk::BakeJobDev{});
@@ -1254,7 +1258,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
   VLB_CUDA(ctx, cudaMemcpyAsync(meta, meta_h.data(), meta_bytes, cudaMemcpyHostToDevice, ctx->stream));
 
   // shape key: everything the captured launches bake in as parameters
-  std::vector<uint64_t> key = {ntable, uint64_t(items), dpw, pl.bf16, K, ndev_out, uint64_t(uintptr_t(tile)),
+  std::vector<uint64_t> key = {ntable, uint64_t(items), dpw, pl.bf16, K, ndev_out, pl.max_probes, uint64_t(uintptr_t(tile)),
                                uint64_t(uintptr_t(out)), uint64_t(uintptr_t(meta)), uint64_t(uintptr_t(counter)),
                                uint64_t(ctx->num_sms)};
   for (const auto& g : pl.groups) {
@@ -1331,7 +1335,7 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
   if (reps == 0) reps = 1;
-  const uint32_t dpws[] = {8, 16, 32, 64, 128};
+  const uint32_t dpws[] = {1, 2, 4, 8, 16};
   cudaEvent_t e0, e1;
   VLB_CUDA(ctx, cudaEventCreate(&e0));
   VLB_CUDA(ctx, cudaEventCreate(&e1));

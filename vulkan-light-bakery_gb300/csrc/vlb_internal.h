@@ -197,7 +197,9 @@ struct BakeJobDev {
   int2* hits_out;
   const int2* hits_in;
 };
-// One CTA per job: Morton order of each job's probes into job.order.
+// One CTA per job: spatial order of each job's probes into job.order
+// (counting sort on a 12-bit Morton prefix up to 16,384 probes, the CTA
+// radix sort in the job's sort scratch above).
 void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s);
 // Persistent trace over all jobs' items (tile mode), counter zeroed before.
 void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_items, uint32_t* counter,
