@@ -530,7 +530,213 @@ static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
   k_trace<MODE, K, COUNT><<<uint32_t(ctas), kTraceThreads, 0, s>>>(a);
 }
 
+// ---- lane mode with per-lane ray fetch (tile output) ---------------------------------
+// Persistent warps; every lane runs its own ray through a small state machine
+// -- primary walk, shading, shadow walk, output -- one node or triangle per
+// loop turn, and takes a new ray as soon as it is done.  Idle lanes refill
+// together from a global ray counter (one atomic per refill, when half the
+// warp or all of it is idle), so a warp no longer waits for its slowest ray
+// and primary and shadow walks of different rays overlap.  Ray r is
+// (direction position t = r / P, probe slot r % P) with P the probe count
+// rounded up to 32: rays fetched together share a direction and are
+// Morton neighbours.  Box tests take the per-lane octant at run time; the
+// tests, the pruning and the tie rule are those of lane_traverse, so each
+// ray's result is unchanged.
+__device__ __forceinline__ bool slab_rt(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                        float tmin, float tmax, float* tnear) {
+  const float ax = fmaf(lx, r.ix, -r.oix), bx = fmaf(hx, r.ix, -r.oix);
+  const float ay = fmaf(ly, r.iy, -r.oiy), by = fmaf(hy, r.iy, -r.oiy);
+  const float az = fmaf(lz, r.iz, -r.oiz), bz = fmaf(hz, r.iz, -r.oiz);
+  const float tn = fmax3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
+  const float tf = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+  *tnear = tn;
+  return tn <= tf;
+}
+
+__device__ __forceinline__ uint32_t lane_lt_mask() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t P = (a.nprobes + 31) / 32 * 32;
+  const uint32_t R = P * a.S;
+  const int root = a.ntris > 1 ? 0 : ~0;
+  Work w;
+  int stack[kTraceStack];
+  bool has = false, shadow = false, exhausted = false;
+  uint32_t p = 0, s = 0;
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  RayCtx ray;
+  make_ray(ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
+  int cur = root, sp = 0, slot = -1, id = -1;
+  float tb = a.tmax, lit = 0.f;
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, !has);
+    if (!exhausted && (idle == kFull || __popc(idle) >= 16)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (int(lane) == leader) base = atomicAdd(a.work_counter, uint32_t(__popc(idle)));
+      base = __shfl_sync(kFull, base, leader);
+      if (base >= R) exhausted = true;
+      if (!has) {
+        const uint32_t r = base + __popc(idle & lane_lt_mask());
+        if (r < R) {
+          const uint32_t t = r / P, sl = r - t * P;
+          if (sl < a.nprobes) {
+            p = a.order[sl];
+            s = __ldg(a.dir_order + t);
+            d = __ldg(a.dirs + s);
+            ox = a.probes[3 * size_t(p)]; oy = a.probes[3 * size_t(p) + 1]; oz = a.probes[3 * size_t(p) + 2];
+            make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
+            has = true; shadow = false;
+            cur = root; sp = 0; slot = -1; id = -1; tb = a.tmax;
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, has)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (!has) continue;
+    // one step of this lane's walk
+    bool fin = false;
+    const float tlo = shadow ? 0.0f : a.tmin;
+    if (cur >= 0) {
+      if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+      const float4 n0 = __ldg(a.nodes + 4 * cur), n1 = __ldg(a.nodes + 4 * cur + 1), n2 = __ldg(a.nodes + 4 * cur + 2),
+                   n3 = __ldg(a.nodes + 4 * cur + 3);
+      float tn0, tn1;
+      const float lim = prune_limit(tb);
+      const bool h0 = slab_rt(ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
+      const bool h1 = slab_rt(ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (h0 && h1) {
+        const bool first0 = tn0 <= tn1;
+        if (sp < kTraceStack) stack[sp++] = first0 ? c1 : c0;
+        else atomicAdd(a.err + kErrStackOverflow, 1);
+        cur = first0 ? c0 : c1;
+      } else if (h0) {
+        cur = c0;
+      } else if (h1) {
+        cur = c1;
+      } else if (sp == 0) {
+        fin = true;
+      } else {
+        cur = stack[--sp];
+      }
+    } else {
+      if constexpr (COUNT) ++w.wtris;
+      const int ts = ~cur;
+      const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
+      const float t = tri_hit(ray, v0, e1, e2);
+      if (t > tlo) {
+        if (shadow) {
+          if (t < tb) { slot = ts; fin = true; }
+        } else {
+          const int tid = __float_as_int(v0.w);
+          if (t < tb || (t == tb && slot >= 0 && tid < id)) { tb = t; slot = ts; id = tid; }
+        }
+      }
+      if (!fin) {
+        if (sp == 0) fin = true;
+        else cur = stack[--sp];
+      }
+    }
+    if (!fin) continue;
+    // this walk is done
+    float rr = 0.f, rg = 0.f, rbl = 0.f;
+    uint8_t vis = 2;
+    int tri_out = -1;
+    bool emit = true;
+    if (!shadow) {
+      if (slot < 0) {
+        if (a.sky) {
+          const float* tx = a.sky + 3 * size_t(cube_texel(d.x, d.y, d.z, a.sky_n));
+          rr = __ldg(tx); rg = __ldg(tx + 1); rbl = __ldg(tx + 2);
+        }
+      } else {
+        const float4 e1 = __ldg(a.tris + 3 * slot + 1), e2 = __ldg(a.tris + 3 * slot + 2);
+        tri_out = id;
+        float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+        const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
+        nx *= rn; ny *= rn; nz *= rn;
+        if (nx * d.x + ny * d.y + nz * d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
+        const float ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
+        if (ndl > 0.f) {  // the shadow walk follows; the primary's triangle id and sun term wait in id / lit
+          if constexpr (COUNT) ++w.shadow;
+          make_ray(ray, fmaf(tb, d.x, ox) + a.bias * nx, fmaf(tb, d.y, oy) + a.bias * ny,
+                   fmaf(tb, d.z, oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z);
+          lit = a.sun_scale * ndl;
+          shadow = true;
+          cur = root; sp = 0; slot = -1; tb = a.tmax;
+          emit = false;
+        }
+      }
+    } else {
+      tri_out = id;
+      const bool occ = slot >= 0;
+      vis = occ ? 0 : 1;
+      if (!occ) {
+        const float4 alb = __ldg(a.albedo + id);
+        rr = alb.x * lit; rg = alb.y * lit; rbl = alb.z * lit;
+      }
+    }
+    if (!emit) continue;
+    has = false;
+    const size_t ri = size_t(p) * a.S + s, row = size_t(p) * 3;
+    if (a.hit_tri) a.hit_tri[ri] = tri_out;
+    if (a.shadow) a.shadow[ri] = vis;
+    if (a.radiance) {
+      a.radiance[row * a.S + s] = rr;
+      a.radiance[(row + 1) * a.S + s] = rg;
+      a.radiance[(row + 2) * a.S + s] = rbl;
+    }
+    if (a.radiance_bf16) {
+      a.radiance_bf16[row * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rr));
+      a.radiance_bf16[(row + 1) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rg));
+      a.radiance_bf16[(row + 2) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rbl));
+    }
+    if (a.dbg_radiance) {
+      a.dbg_radiance[3 * ri] = rr; a.dbg_radiance[3 * ri + 1] = rg; a.dbg_radiance[3 * ri + 2] = rbl;
+    }
+  }
+  if constexpr (COUNT) {
+    atomicAdd(a.counters + 0, (unsigned long long)w.wnodes);
+    atomicAdd(a.counters + 1, (unsigned long long)w.wtris);
+    atomicAdd(a.counters + 2, (unsigned long long)w.shadow);
+    atomicAdd(a.counters + 3, (unsigned long long)w.lnodes);
+  }
+}
+
+template <bool COUNT>
+static void launch_dyn(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn<COUNT>, kTraceThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t rays = uint64_t((a.nprobes + 31) / 32 * 32) * a.S;
+  const uint64_t ctas = std::min<uint64_t>((rays + kTraceThreads - 1) / kTraceThreads, uint64_t(num_sms) * per_sm);
+  k_trace_dyn<COUNT><<<uint32_t(std::max<uint64_t>(ctas, 1)), kTraceThreads, 0, s>>>(a);
+}
+
+// The ray counter runs past R by at most 32 per resident warp: R < 2^31 keeps it in 32 bits.
+bool trace_dyn_supported(const TraceArgs& a) {
+  return a.lane && a.ntris > 0 && uint64_t((a.nprobes + 31) / 32 * 32) * a.S < (1ull << 31);
+}
+
 void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  if (trace_dyn_supported(a)) {
+    if (a.counters) launch_dyn<true>(a, num_sms, s);
+    else launch_dyn<false>(a, num_sms, s);
+    return;
+  }
   if (a.counters) launch<0, 1, true>(a, num_sms, s);
   else launch<0, 1, false>(a, num_sms, s);
 }
