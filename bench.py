@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
-    ap.add_argument("--only", choices=["skybox", "projection", "batch", "service"], default=None,
+    ap.add_argument("--only", choices=["bake", "skybox", "projection", "batch", "service"], default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
@@ -205,8 +205,8 @@ def main():
     ctx.set_stream(stream.cuda_stream)
     if args.only:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-        fn = {"skybox": skybox_measure, "projection": projection_measure, "batch": batch_measure,
-              "service": service_measure}[args.only]
+        fn = {"bake": bake_measure, "skybox": skybox_measure, "projection": projection_measure,
+              "batch": batch_measure, "service": service_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
         return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
@@ -359,6 +359,28 @@ def main():
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def bake_measure(ctx, torch, stream, steps, hbm_peak):
+    """The headline workload's chosen path alone (config 1, VLB_PREC_FUSED):
+    `steps` bakes with inputs resident in HBM, per-kernel library times."""
+    import vlb
+
+    pos, idx, alb, sky, sun, probes = workload_inputs()
+    scene = ctx.scene(pos, idx, alb)
+    p = vlb.bake_params(ctx.fibonacci(NDIRS), LMAX, vlb.PREC_FUSED, sun, sky=ctx.sky(sky, SKY_N))
+    d_probes = torch.from_numpy(probes).cuda()
+    out = torch.empty((probes.shape[0], vlb.k_of(LMAX), 3), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        ctx.bake(scene, d_probes, p, out=out)
+    torch.cuda.synchronize()
+    ctx.profile_reset()
+    ctx.set_profiling(True)
+    for _ in range(steps):
+        ctx.bake(scene, d_probes, p, out=out)
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
+    return {"workload": WORKLOAD, "kernels_ms": {k: v[1] / max(v[0], 1) for k, v in ctx.profile().items()}}
 
 
 def skybox_measure(ctx, torch, stream, steps, hbm_peak):

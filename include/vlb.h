@@ -249,8 +249,9 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
  * LightBaker (src/baker/light_baker.cpp:27-49, baker/main.cpp:22-24) and one
  * probe per dispatch.  A batch bakes many (scene, probes) jobs at once: one
  * launch sorts every job's probes, ONE persistent trace launch has its warps
- * pull work items from all jobs (costliest jobs first), then one projection
- * per direction set writes all of that set's probes.  Each job's output is
+ * pull chunks of rays from all jobs (costliest jobs first) and hand them to
+ * their lanes as the lanes free up, then one projection per direction set
+ * writes all of that set's probes.  Each job's output is
  * bit-identical to vlb_bake of that job alone with the same parameters:
  * VLB_PREC_FP32 or VLB_PREC_MIXED (VLB_PREC_FUSED bakes as VLB_PREC_FP32).
  * The device part of a batch is captured in a CUDA graph on the second call
@@ -265,7 +266,8 @@ typedef struct vlb_bake_job {
 } vlb_bake_job;
 /* Schedule knobs of the batched trace (results do not depend on them). */
 typedef struct vlb_batch_schedule {
-  uint32_t dirs_per_item; /* directions per warp work item, 1..4096; 0 = library choice */
+  uint32_t dirs_per_item; /* rays per lane in a warp's chunk of a job's rays (chunk = 32 x this), 1..64;
+                             0 = library choice */
   uint32_t cost_order;    /* 1: work items of the costliest jobs (rays x log2 triangles) first */
   uint32_t graph;         /* 1: capture and replay the device part as a CUDA graph */
 } vlb_batch_schedule;
@@ -273,8 +275,8 @@ typedef struct vlb_batch_schedule {
  * the library default {0, 1, 1}. */
 vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                           const vlb_batch_schedule* sched);
-/* Times the batch under each candidate schedule (directions per item 1, 2,
- * 4, 8, 16 x job order, reps runs each, outputs written every run), stores the fastest in
+/* Times the batch under each candidate schedule (rays per lane per chunk 1,
+ * 2, 4, 8, 16 x job order, reps runs each, outputs written every run), stores the fastest in
  * the context for later vlb_bake_batch calls with sched NULL and returns it
  * with its mean milliseconds per batch. */
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,

@@ -559,151 +559,173 @@ __device__ __forceinline__ uint32_t lane_lt_mask() {
   return m;
 }
 
+// One lane's ray: its walk and the pending shading of its primary hit.
+struct LaneRay {
+  bool has = false, shadow = false;
+  uint32_t p = 0, s = 0;
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  RayCtx ray;
+  int cur = 0, sp = 0, slot = -1, id = -1;
+  float tb = 0.f, lit = 0.f;
+};
+
+// A: TraceArgs or BakeJobDev (scene, shading, probes and dirs fields).
+template <class A>
+__device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uint32_t s) {
+  L.p = p;
+  L.s = s;
+  L.d = __ldg(a.dirs + s);
+  L.ox = a.probes[3 * size_t(p)];
+  L.oy = a.probes[3 * size_t(p) + 1];
+  L.oz = a.probes[3 * size_t(p) + 2];
+  make_ray(L.ray, L.ox, L.oy, L.oz, L.d.x, L.d.y, L.d.z);
+  L.has = true;
+  L.shadow = false;
+  L.cur = a.ntris > 1 ? 0 : ~0;
+  L.sp = 0;
+  L.slot = -1;
+  L.id = -1;
+  L.tb = a.tmax;
+}
+
+// One node or triangle of the lane's current walk (nearer child first, the
+// pruning margin and tie rule of lane_traverse); true when the walk is over.
+template <bool COUNT, class A>
+__device__ __forceinline__ bool lr_step(const A& a, LaneRay& L, int* stack, Work& w) {
+  if (a.ntris == 0) return true;
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  if (L.cur >= 0) {
+    if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+    const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
+                 n2 = __ldg(a.nodes + 4 * L.cur + 2), n3 = __ldg(a.nodes + 4 * L.cur + 3);
+    float tn0, tn1;
+    const float lim = prune_limit(L.tb);
+    const bool h0 = slab_rt(L.ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
+    const bool h1 = slab_rt(L.ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
+    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+    if (h0 && h1) {
+      const bool first0 = tn0 <= tn1;
+      if (L.sp < kTraceStack) stack[L.sp++] = first0 ? c1 : c0;
+      else atomicAdd(a.err + kErrStackOverflow, 1);
+      L.cur = first0 ? c0 : c1;
+      return false;
+    }
+    if (h0) { L.cur = c0; return false; }
+    if (h1) { L.cur = c1; return false; }
+  } else {
+    if constexpr (COUNT) ++w.wtris;
+    const int ts = ~L.cur;
+    const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
+    const float t = tri_hit(L.ray, v0, e1, e2);
+    if (t > tlo) {
+      if (L.shadow) {
+        if (t < L.tb) { L.slot = ts; return true; }
+      } else {
+        const int tid = __float_as_int(v0.w);
+        if (t < L.tb || (t == L.tb && L.slot >= 0 && tid < L.id)) { L.tb = t; L.slot = ts; L.id = tid; }
+      }
+    }
+  }
+  if (L.sp == 0) return true;
+  L.cur = stack[--L.sp];
+  return false;
+}
+
+// After a walk.  A finished primary walk is shaded: a miss takes the sky, a
+// lit-facing hit starts its shadow walk (returns false: the lane walks on,
+// the triangle id and sun term wait in id / lit), anything else is done.  A
+// finished shadow walk gives the Lambert term or 0.  Returns true with the
+// sample in `o` when the ray is complete.
+template <bool COUNT, class A>
+__device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Work& w) {
+  o = Shaded{0.f, 0.f, 0.f, -1, 2};
+  if (!L.shadow) {
+    if (L.slot < 0) {
+      if (a.sky) {
+        const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
+        o.r = __ldg(tx); o.g = __ldg(tx + 1); o.b = __ldg(tx + 2);
+      }
+      return true;
+    }
+    const float4 e1 = __ldg(a.tris + 3 * L.slot + 1), e2 = __ldg(a.tris + 3 * L.slot + 2);
+    o.tri = L.id;
+    float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+    const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
+    nx *= rn; ny *= rn; nz *= rn;
+    if (nx * L.d.x + ny * L.d.y + nz * L.d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
+    const float ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
+    if (!(ndl > 0.f)) return true;
+    if constexpr (COUNT) ++w.shadow;
+    make_ray(L.ray, fmaf(L.tb, L.d.x, L.ox) + a.bias * nx, fmaf(L.tb, L.d.y, L.oy) + a.bias * ny,
+             fmaf(L.tb, L.d.z, L.oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z);
+    L.lit = a.sun_scale * ndl;
+    L.shadow = true;
+    L.cur = a.ntris > 1 ? 0 : ~0;
+    L.sp = 0;
+    L.slot = -1;
+    L.tb = a.tmax;
+    return false;
+  }
+  o.tri = L.id;
+  const bool occ = L.slot >= 0;
+  o.vis = occ ? 0 : 1;
+  if (!occ) {
+    const float4 alb = __ldg(a.albedo + L.id);
+    o.r = alb.x * L.lit; o.g = alb.y * L.lit; o.b = alb.z * L.lit;
+  }
+  return true;
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
   const uint32_t R = P * a.S;
-  const int root = a.ntris > 1 ? 0 : ~0;
   Work w;
   int stack[kTraceStack];
-  bool has = false, shadow = false, exhausted = false;
-  uint32_t p = 0, s = 0;
-  float ox = 0.f, oy = 0.f, oz = 0.f;
-  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-  RayCtx ray;
-  make_ray(ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
-  int cur = root, sp = 0, slot = -1, id = -1;
-  float tb = a.tmax, lit = 0.f;
+  LaneRay L;
+  make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
+  bool exhausted = false;
   for (;;) {
-    const unsigned idle = __ballot_sync(kFull, !has);
+    const unsigned idle = __ballot_sync(kFull, !L.has);
     if (!exhausted && (idle == kFull || __popc(idle) >= 16)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (int(lane) == leader) base = atomicAdd(a.work_counter, uint32_t(__popc(idle)));
       base = __shfl_sync(kFull, base, leader);
       if (base >= R) exhausted = true;
-      if (!has) {
+      if (!L.has) {
         const uint32_t r = base + __popc(idle & lane_lt_mask());
         if (r < R) {
           const uint32_t t = r / P, sl = r - t * P;
-          if (sl < a.nprobes) {
-            p = a.order[sl];
-            s = __ldg(a.dir_order + t);
-            d = __ldg(a.dirs + s);
-            ox = a.probes[3 * size_t(p)]; oy = a.probes[3 * size_t(p) + 1]; oz = a.probes[3 * size_t(p) + 2];
-            make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
-            has = true; shadow = false;
-            cur = root; sp = 0; slot = -1; id = -1; tb = a.tmax;
-          }
+          if (sl < a.nprobes) lr_start(a, L, a.order[sl], __ldg(a.dir_order + t));
         }
       }
     }
-    if (!__any_sync(kFull, has)) {
+    if (!__any_sync(kFull, L.has)) {
       if (exhausted) break;
       continue;
     }
-    if (!has) continue;
-    // one step of this lane's walk
-    bool fin = false;
-    const float tlo = shadow ? 0.0f : a.tmin;
-    if (cur >= 0) {
-      if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
-      const float4 n0 = __ldg(a.nodes + 4 * cur), n1 = __ldg(a.nodes + 4 * cur + 1), n2 = __ldg(a.nodes + 4 * cur + 2),
-                   n3 = __ldg(a.nodes + 4 * cur + 3);
-      float tn0, tn1;
-      const float lim = prune_limit(tb);
-      const bool h0 = slab_rt(ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
-      const bool h1 = slab_rt(ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
-      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-      if (h0 && h1) {
-        const bool first0 = tn0 <= tn1;
-        if (sp < kTraceStack) stack[sp++] = first0 ? c1 : c0;
-        else atomicAdd(a.err + kErrStackOverflow, 1);
-        cur = first0 ? c0 : c1;
-      } else if (h0) {
-        cur = c0;
-      } else if (h1) {
-        cur = c1;
-      } else if (sp == 0) {
-        fin = true;
-      } else {
-        cur = stack[--sp];
-      }
-    } else {
-      if constexpr (COUNT) ++w.wtris;
-      const int ts = ~cur;
-      const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
-      const float t = tri_hit(ray, v0, e1, e2);
-      if (t > tlo) {
-        if (shadow) {
-          if (t < tb) { slot = ts; fin = true; }
-        } else {
-          const int tid = __float_as_int(v0.w);
-          if (t < tb || (t == tb && slot >= 0 && tid < id)) { tb = t; slot = ts; id = tid; }
-        }
-      }
-      if (!fin) {
-        if (sp == 0) fin = true;
-        else cur = stack[--sp];
-      }
-    }
-    if (!fin) continue;
-    // this walk is done
-    float rr = 0.f, rg = 0.f, rbl = 0.f;
-    uint8_t vis = 2;
-    int tri_out = -1;
-    bool emit = true;
-    if (!shadow) {
-      if (slot < 0) {
-        if (a.sky) {
-          const float* tx = a.sky + 3 * size_t(cube_texel(d.x, d.y, d.z, a.sky_n));
-          rr = __ldg(tx); rg = __ldg(tx + 1); rbl = __ldg(tx + 2);
-        }
-      } else {
-        const float4 e1 = __ldg(a.tris + 3 * slot + 1), e2 = __ldg(a.tris + 3 * slot + 2);
-        tri_out = id;
-        float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
-        const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
-        nx *= rn; ny *= rn; nz *= rn;
-        if (nx * d.x + ny * d.y + nz * d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
-        const float ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
-        if (ndl > 0.f) {  // the shadow walk follows; the primary's triangle id and sun term wait in id / lit
-          if constexpr (COUNT) ++w.shadow;
-          make_ray(ray, fmaf(tb, d.x, ox) + a.bias * nx, fmaf(tb, d.y, oy) + a.bias * ny,
-                   fmaf(tb, d.z, oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z);
-          lit = a.sun_scale * ndl;
-          shadow = true;
-          cur = root; sp = 0; slot = -1; tb = a.tmax;
-          emit = false;
-        }
-      }
-    } else {
-      tri_out = id;
-      const bool occ = slot >= 0;
-      vis = occ ? 0 : 1;
-      if (!occ) {
-        const float4 alb = __ldg(a.albedo + id);
-        rr = alb.x * lit; rg = alb.y * lit; rbl = alb.z * lit;
-      }
-    }
-    if (!emit) continue;
-    has = false;
-    const size_t ri = size_t(p) * a.S + s, row = size_t(p) * 3;
-    if (a.hit_tri) a.hit_tri[ri] = tri_out;
-    if (a.shadow) a.shadow[ri] = vis;
+    if (!L.has || !lr_step<COUNT>(a, L, stack, w)) continue;
+    Shaded o;
+    if (!lr_finish<COUNT>(a, L, o, w)) continue;
+    L.has = false;
+    const size_t ri = size_t(L.p) * a.S + L.s, row = size_t(L.p) * 3;
+    if (a.hit_tri) a.hit_tri[ri] = o.tri;
+    if (a.shadow) a.shadow[ri] = o.vis;
     if (a.radiance) {
-      a.radiance[row * a.S + s] = rr;
-      a.radiance[(row + 1) * a.S + s] = rg;
-      a.radiance[(row + 2) * a.S + s] = rbl;
+      a.radiance[row * a.S + L.s] = o.r;
+      a.radiance[(row + 1) * a.S + L.s] = o.g;
+      a.radiance[(row + 2) * a.S + L.s] = o.b;
     }
     if (a.radiance_bf16) {
-      a.radiance_bf16[row * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rr));
-      a.radiance_bf16[(row + 1) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rg));
-      a.radiance_bf16[(row + 2) * a.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(rbl));
+      a.radiance_bf16[row * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
+      a.radiance_bf16[(row + 1) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
+      a.radiance_bf16[(row + 2) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
     }
     if (a.dbg_radiance) {
-      a.dbg_radiance[3 * ri] = rr; a.dbg_radiance[3 * ri + 1] = rg; a.dbg_radiance[3 * ri + 2] = rbl;
+      a.dbg_radiance[3 * ri] = o.r; a.dbg_radiance[3 * ri + 1] = o.g; a.dbg_radiance[3 * ri + 2] = o.b;
     }
   }
   if constexpr (COUNT) {
@@ -745,79 +767,101 @@ void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
 // jobs (job j owns items [item_begin, item_begin + packets * chunks)); a warp
 // finds its job by binary search over the item ranges and traces that job's
 // scene.  Radiance goes to the job's rows of its direction set's tile.
+__device__ __forceinline__ void batch_emit(const BakeJobDev& j, uint32_t p, uint32_t s, const Shaded& o) {
+  const size_t row = size_t(p) * 3;
+  if (j.radiance) {
+    j.radiance[row * j.S + s] = o.r;
+    j.radiance[(row + 1) * j.S + s] = o.g;
+    j.radiance[(row + 2) * j.S + s] = o.b;
+  } else {
+    j.radiance_bf16[row * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
+    j.radiance_bf16[(row + 1) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
+    j.radiance_bf16[(row + 2) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
+  }
+}
+
+// Batched bake.  Job j owns the rays [ray_begin, ray_begin + P*S) of one
+// numbering over all jobs (P: its probe count rounded up to 32; ray r of a job
+// is direction position r / P, probe slot r % P), each job's range rounded up
+// to whole chunks of 32 * chunk_lanes rays.  A warp takes a chunk from the
+// counter (one atomic), finds its job by binary search over the ranges, and
+// hands the chunk's rays to whichever lanes are idle; every lane runs its rays
+// through its own state machine (lr_*), so lanes wait for each other only at
+// the chunk's end, and the job's fields stay warp-uniform.  Kept hits are
+// written after the primary walk; a relight starts from the kept hit with only
+// its shadow walk.  Every job walks per lane: results do not depend on the
+// traversal mode.
 __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobDev* __restrict__ jobs, uint32_t njobs,
-                                                               uint32_t total, uint32_t* counter) {
+                                                               uint32_t total, uint32_t chunk, uint32_t* counter) {
   const uint32_t lane = threadIdx.x & 31;
   Work w;
+  int stack[kTraceStack];
+  LaneRay L;
+  make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
   for (;;) {
-    uint32_t item = 0;
-    if (lane == 0) item = atomicAdd(counter, 1u);
-    item = __shfl_sync(kFull, item, 0);
-    if (item >= total) break;
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(counter, chunk);
+    c = __shfl_sync(kFull, c, 0);
+    if (c >= total) break;
     uint32_t lo = 0, hi = njobs - 1;
     while (lo < hi) {
       const uint32_t mid = (lo + hi + 1) >> 1;
-      if (__ldg(&jobs[mid].item_begin) <= item) lo = mid; else hi = mid - 1;
+      if (__ldg(&jobs[mid].ray_begin) <= c) lo = mid; else hi = mid - 1;
     }
     const BakeJobDev& j = jobs[lo];
-    const uint32_t npg = (j.nprobes + 31) / 32;
-    const uint32_t li = item - j.item_begin;
-    const uint32_t chunk = li / npg, pg = li - chunk * npg;
-    const uint32_t slot = pg * 32 + lane;
-    const bool valid = slot < j.nprobes;
-    const uint32_t p = valid ? j.order[slot] : 0;
-    const float ox = valid ? j.probes[3 * size_t(p)] : 0.f, oy = valid ? j.probes[3 * size_t(p) + 1] : 0.f,
-                oz = valid ? j.probes[3 * size_t(p) + 2] : 0.f;
-    const uint32_t s0 = min(j.S, chunk * j.dpw), s1 = min(j.S, s0 + j.dpw);
-    for (uint32_t t = s0; t < s1; ++t) {
-      const uint32_t s = __ldg(j.dir_order + t);
-      const float4 dv = __ldg(j.dirs + s);
-      const size_t ray_i = size_t(p) * j.S + s;
-      RayCtx ray;
-      make_ray(ray, ox, oy, oz, dv.x, dv.y, dv.z);
-      int slot = -1, id = -1;
-      float tb = j.tmax;
-      if (j.hits_in) {  // relight: the kept primary hit, only the shadow ray is traced
-        if (valid) {
-          const int2 h = __ldg(j.hits_in + ray_i);
-          slot = h.x;
-          tb = __int_as_float(h.y);
-          if (slot >= 0) id = __float_as_int(__ldg(j.tris + 3 * slot).w);
+    const uint32_t P = (j.nprobes + 31) / 32 * 32;
+    const uint32_t R = P * j.S;
+    uint32_t r0 = c - j.ray_begin;                // the chunk's first ray in the job
+    const uint32_t r1 = min(R, r0 + chunk);       // end of its real rays (the rest is padding)
+    for (;;) {
+      const unsigned idle = __ballot_sync(kFull, !L.has);
+      if (idle && r0 < r1) {  // idle lanes take the chunk's next rays, in lane order
+        const uint32_t r = r0 + __popc(idle & lane_lt_mask());
+        r0 = min(r1, r0 + uint32_t(__popc(idle)));
+        if (!L.has && r < r1) {
+          const uint32_t t = r / P, sl = r - t * P;
+          if (sl < j.nprobes) {
+            const uint32_t p = j.order[sl];
+            lr_start(j, L, p, __ldg(j.dir_order + t));
+            if (j.hits_in) {  // relight: the kept primary hit, only the shadow walk remains
+              const int2 h = __ldg(j.hits_in + size_t(p) * j.S + L.s);
+              L.slot = h.x;
+              L.tb = __int_as_float(h.y);
+              L.id = h.x >= 0 ? __float_as_int(__ldg(j.tris + 3 * h.x).w) : -1;
+              Shaded o;
+              if (lr_finish<false>(j, L, o, w)) {
+                L.has = false;
+                batch_emit(j, L.p, L.s, o);
+              }
+            }
+          }
         }
-      } else if (j.lane) {
-        primary_hit<false, true>(j, valid, ray, dv, slot, id, tb, w);
-      } else {
-        primary_hit<false, false>(j, valid, ray, dv, slot, id, tb, w);
       }
-      if (j.hits_out && valid) j.hits_out[ray_i] = make_int2(slot, __float_as_int(tb));
-      const Shaded o = j.lane ? shade_hit<false, true>(j, valid, ray, ox, oy, oz, dv, slot, id, tb, w)
-                              : shade_hit<false, false>(j, valid, ray, ox, oy, oz, dv, slot, id, tb, w);
-      if (!valid) continue;
-      const size_t row = size_t(p) * 3;
-      if (j.radiance) {
-        j.radiance[row * j.S + s] = o.r;
-        j.radiance[(row + 1) * j.S + s] = o.g;
-        j.radiance[(row + 2) * j.S + s] = o.b;
-      } else {
-        j.radiance_bf16[row * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
-        j.radiance_bf16[(row + 1) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
-        j.radiance_bf16[(row + 2) * j.S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
+      if (!__any_sync(kFull, L.has)) {
+        if (r0 >= r1) break;
+        continue;
       }
+      if (!L.has || !lr_step<false>(j, L, stack, w)) continue;
+      if (!L.shadow && j.hits_out) j.hits_out[size_t(L.p) * j.S + L.s] = make_int2(L.slot, __float_as_int(L.tb));
+      Shaded o;
+      if (!lr_finish<false>(j, L, o, w)) continue;
+      L.has = false;
+      batch_emit(j, L.p, L.s, o);
     }
   }
 }
 
-void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_items, uint32_t* counter,
-                        int num_sms, cudaStream_t s) {
-  if (!total_items || !njobs) return;
+void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
+                        uint32_t* counter, int num_sms, cudaStream_t s) {
+  if (!total_rays || !njobs) return;
   static int per_sm = 0;
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
   }
-  const uint64_t ctas = std::min<uint64_t>((uint64_t(total_items) + kTraceWarps - 1) / kTraceWarps,
+  const uint64_t ctas = std::min<uint64_t>((uint64_t(total_rays) / chunk + kTraceWarps - 1) / kTraceWarps + 1,
                                            uint64_t(num_sms) * per_sm);
-  k_trace_batch<<<uint32_t(ctas), kTraceThreads, 0, s>>>(jobs, njobs, total_items, counter);
+  k_trace_batch<<<uint32_t(ctas), kTraceThreads, 0, s>>>(jobs, njobs, total_rays, chunk, counter);
 }
 
 __global__ void k_scatter_rows(const float* __restrict__ src, float* const* __restrict__ dst,

@@ -1112,7 +1112,7 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
 // The device work of a batch on ctx->stream (capturable: no allocation, no
 // synchronisation).
 static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBufs& bb, uint32_t ntable,
-                                uint32_t total_items) {
+                                uint32_t total_rays, uint32_t chunk) {
   const uint32_t V = 3 * pl.K;
   const auto* table = reinterpret_cast<const vlbk::BakeJobDev*>(bb.meta);
   VLB_CUDA(ctx, cudaMemsetAsync(bb.counter, 0, 4, ctx->stream));
@@ -1122,7 +1122,7 @@ static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBu
   }
   {
     KScope k(ctx, "trace_batch");
-    vlbk::launch_trace_batch(table, ntable, total_items, bb.counter, ctx->num_sms, ctx->stream);
+    vlbk::launch_trace_batch(table, ntable, total_rays, chunk, bb.counter, ctx->num_sms, ctx->stream);
   }
   for (const auto& g : pl.groups) {
     float* out = bb.out + g.row0 * V;
@@ -1191,13 +1191,16 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
   const size_t esz = pl.bf16 ? 2 : 4;
   uint64_t warp_rays = 0;
   for (const auto& b : pl.jobs) warp_rays += (uint64_t(b.nprobes) + 31) / 32 * b.S;
-  // directions per work item: at least ~16 items per resident warp (item
-  // times vary widely, so fewer items leave warps idle at the tail), at most 8
+  // rays per lane per chunk (a warp takes 32 x that many rays at a time):
+  // at least ~16 chunks per resident warp, at most 8 rays per lane
   uint32_t dpw = sc.dirs_per_item;
   if (!dpw) {
-    const uint64_t target = 16ull * 32 * uint64_t(ctx->num_sms);
-    dpw = uint32_t(std::min<uint64_t>(8, std::max<uint64_t>(1, warp_rays / target)));
+    uint64_t rays = 0;
+    for (const auto& b : pl.jobs) rays += (uint64_t(b.nprobes) + 31) / 32 * 32 * b.S;
+    const uint64_t target = 16ull * 32 * 32 * uint64_t(ctx->num_sms);
+    dpw = uint32_t(std::min<uint64_t>(8, std::max<uint64_t>(1, rays / target)));
   }
+  const uint32_t chunk = 32 * dpw;
   auto& table = ctx->batch_table;
   table.assign(ntable, vlbk::BakeJobDev{});
   size_t poff = 0;
@@ -1230,16 +1233,13 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
     if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
     else d.radiance = reinterpret_cast<float*>(rad);
-    d.lane = lane_mode(j.scene, b.nprobes, p->flags);
-    d.dpw = std::min(dpw, b.S);
-    d.chunks = (b.S + d.dpw - 1) / d.dpw;
-    d.item_begin = uint32_t(items);
-    items += (uint64_t(b.nprobes) + 31) / 32 * d.chunks;
+    d.ray_begin = uint32_t(items);
+    items += ((uint64_t(b.nprobes) + 31) / 32 * 32 * b.S + chunk - 1) / chunk * chunk;
     for (int a = 0; a < 6; ++a) d.bounds[a] = j.scene->bounds[a];
     d.sort_scratch = bb.sort + 4 * b.row0;
     if (ext) { d.hits_out = ext[b.idx].hits_out; d.hits_in = ext[b.idx].hits_in; }
   }
-  if (items > 0xFFFFFFFFull) return fail(ctx, VLB_ERR_INVALID, "batch has too many work items");
+  if (items >= (1ull << 31)) return fail(ctx, VLB_ERR_INVALID, "batch has 2^31 rays or more; split it");
   auto& meta_h = ctx->batch_meta;
   meta_h.assign(meta_bytes, 0);
   std::memcpy(meta_h.data(), table.data(), table.size() * sizeof(vlbk::BakeJobDev));
@@ -1277,7 +1277,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
       ctx->profiling = false;
       cudaGraph_t g = nullptr;
       VLB_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items));
+      st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk);
       const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->profiling = prof;
       ctx->batch_graph_kernels = uint32_t(ctx->launches - l0);
@@ -1290,7 +1290,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     }
     KScope k(ctx, "bake_batch_graph", int(ctx->batch_graph_kernels));
     VLB_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, ctx->stream));
-  } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items)))) {
+  } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk))) {
     return st;
   }
   for (const auto& b : pl.jobs) {
@@ -1326,7 +1326,7 @@ vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
   vlb_batch_schedule sc = sched ? *sched : ctx->batch_sched;
-  if (sc.dirs_per_item > 4096) return fail(ctx, VLB_ERR_INVALID, "dirs_per_item %u > 4096", sc.dirs_per_item);
+  if (sc.dirs_per_item > 64) return fail(ctx, VLB_ERR_INVALID, "dirs_per_item %u > 64", sc.dirs_per_item);
   return batch_run(ctx, jobs, njobs, params, sc);
 }
 

@@ -185,9 +185,9 @@ struct BakeJobDev {
   // this job's rows of its direction set's radiance tile
   float* radiance;
   uint16_t* radiance_bf16;
-  // work items [item_begin, item_begin + packets * chunks), chunk-major
-  uint32_t item_begin, chunks, dpw;
-  uint32_t lane;          // 1: per-lane traversal, 0: packet traversal
+  // rays [ray_begin, ray_begin + P * S) of the batch's numbering (P: nprobes
+  // rounded up to 32), the range rounded up to whole chunks
+  uint32_t ray_begin;
   // probe sort: bounds for the Morton codes, 4 scratch arrays of nprobes
   float bounds[6];
   uint32_t* sort_scratch;
@@ -201,9 +201,10 @@ struct BakeJobDev {
 // (counting sort on a 12-bit Morton prefix up to 16,384 probes, the CTA
 // radix sort in the job's sort scratch above).
 void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s);
-// Persistent trace over all jobs' items (tile mode), counter zeroed before.
-void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_items, uint32_t* counter,
-                        int num_sms, cudaStream_t s);
+// Persistent trace over all jobs' rays (tile output), warps taking chunks of
+// `chunk` rays (a multiple of 32); counter zeroed before.
+void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
+                        uint32_t* counter, int num_sms, cudaStream_t s);
 // Copies job j's rows of a projected group output to its own output:
 // dst[j] <- src + src_row0[j]*K*3 floats, nprobes[j]*K*3 floats.
 void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
