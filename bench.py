@@ -56,6 +56,23 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest of every rank's x (the job's time is its slowest replica's)."""
+    import torch
+
+    if dist is None:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, max_ms: float) -> float:
+    """Replicas (weak scaling): every rank bakes the workload; the job's rate is
+    all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / (max_ms / 1e3)
+
+
 def workload_inputs():
     import vlb
 
@@ -263,15 +280,12 @@ def main():
     shadow_rays = stats["shadow_rays"]
 
     def agg(ms):
-        t = torch.tensor([sum(ms)], dtype=torch.float64, device="cuda")
-        if dist is not None:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(sum(ms), dist, "cuda")
 
     tot_chosen = agg(ms_chosen)
     tot_plain = agg(ms_plain)
-    value = world * P * args.steps / (tot_chosen / 1e3)
-    plain = world * P * args.steps / (tot_plain / 1e3)
+    value = whole_job_rate(P * args.steps, world, tot_chosen)
+    plain = whole_job_rate(P * args.steps, world, tot_plain)
 
     # e2e: public call with pinned host buffers (H2D probes, D2H SH) inside the timed region
     h_probes = torch.from_numpy(probes).pin_memory()
@@ -285,7 +299,7 @@ def main():
         t0 = time.perf_counter()
         ctx.bake(scene, h_probes, params[chosen], out=h_out)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
-    e2e_value = world * P * args.steps / (agg(e2e_ms) / 1e3)
+    e2e_value = whole_job_rate(P * args.steps, world, agg(e2e_ms))
 
     if rank != 0:
         return 0
