@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
-    ap.add_argument("--only", choices=["bake", "skybox", "projection", "batch", "service"], default=None,
+    ap.add_argument("--only", choices=["bake", "skybox", "projection", "bake_c2", "batch", "service"], default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
@@ -223,7 +223,7 @@ def main():
     if args.only:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         fn = {"bake": bake_measure, "skybox": skybox_measure, "projection": projection_measure,
-              "batch": batch_measure, "service": service_measure}[args.only]
+              "bake_c2": bake_c2_measure, "batch": batch_measure, "service": service_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
         return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
@@ -366,6 +366,7 @@ def main():
         "clocks": clk,
         "skybox_c0": skybox_measure(ctx, torch, stream, args.steps, hbm_peak),
         "projection_c2": projection_measure(ctx, torch, stream, args.steps, hbm_peak),
+        "bake_c2": bake_c2_measure(ctx, torch, stream, args.steps, hbm_peak),
         "batch_c3": batch_measure(ctx, torch, stream, args.steps, hbm_peak),
         "service_c4": service_measure(ctx, torch, stream, args.steps, hbm_peak),
     }
@@ -484,6 +485,67 @@ def projection_measure(ctx, torch, stream, steps, hbm_peak, nprobes=262144, S=10
         "fp32_cuda_cores": {"probes_per_s": nprobes / (m32 / 1e3), "ms": m32,
                             "achieved_gbs": b32 / (m32 * 1e-3) / 1e9},
     }
+
+
+def bake_c2_measure(ctx, torch, stream, steps, hbm_peak, sample=64):
+    """Config 2 as a whole bake: the config-1 scene scaled to 4096 boxes (49,162
+    triangles), 64^3 = 262,144 probes x 1024 Fibonacci directions (268 M primary
+    rays), L2 SH; BF16 radiance tile + tcgen05 hi/lo projection vs the plain
+    FP32 path, inputs resident in HBM, L2 flushed before every bake.  Error vs
+    the FP64 oracle on a probe sample."""
+    import vlb
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    pos, idx, alb = vlb.synth_box_scene(SEED, 4096)
+    sky = vlb.synth_cubemap(SEED, SKY_N)
+    sun = vlb.synth_sun(SEED)
+    bounds = np.concatenate([np.minimum(pos.min(0), 0), np.maximum(pos.max(0), 0)]).astype(np.float32)
+    probes, _ = vlb.probe_grid_ref_order(bounds, (64, 64, 64))
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(1024)
+    skyh = ctx.sky(sky, SKY_N)
+    P, K = probes.shape[0], vlb.k_of(LMAX)
+    d_probes = torch.from_numpy(probes).cuda()
+    out = torch.empty((P, K, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    steps = max(3, min(steps, 5))
+    res = {"workload": f"config 2 bake: {int(idx.shape[0])} triangles, {P} probes x 1024 dirs, L{LMAX} SH",
+           "primary_rays": P * 1024}
+    outs = {}
+    for name, prec in (("mixed_bf16_tcgen05", vlb.PREC_MIXED), ("fp32", vlb.PREC_FP32)):
+        p = vlb.bake_params(ds, LMAX, prec, sun, sky=skyh)
+        ctx.bake(scene, d_probes, p, out=out)
+        torch.cuda.synchronize()
+        ctx.profile_reset()
+        ctx.set_profiling(True)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            ctx.bake(scene, d_probes, p, out=out)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ctx.set_profiling(False)
+        ms = sorted(a.elapsed_time(b) for a, b in evs)[len(evs) // 2]
+        outs[name] = out.cpu().numpy().copy()
+        res[name] = {"ms": ms, "probes_per_s": P / (ms / 1e3), "grays_per_s": P * 1024 / (ms / 1e3) / 1e9,
+                     "kernels_ms": {k: v[1] / max(v[0], 1) for k, v in ctx.profile().items()}}
+    # error vs the FP64 oracle on an evenly spread probe sample
+    sel = np.linspace(0, P - 1, sample).astype(int)
+    d32, w = O.dirs_fibonacci(1024)
+    B = O.basis_matrix(d32.astype(np.float64), w, LMAX)
+    ref = O.Scene(pos, idx, alb).bake(probes[sel], d32, B, sun, sky=sky, sky_n=SKY_N)
+    for name in outs:
+        g = outs[name][sel].astype(np.float64)
+        e = np.linalg.norm((g - ref).reshape(sample, -1), axis=1) / np.maximum(
+            np.linalg.norm(ref.reshape(sample, -1), axis=1), 1e-30)
+        res[name]["rel_err_vs_fp64"] = {"max": float(e.max()), "median": float(np.median(e)), "probes": sample}
+    e = np.linalg.norm((outs["mixed_bf16_tcgen05"] - outs["fp32"]).reshape(P, -1), axis=1) / np.maximum(
+        np.linalg.norm(outs["fp32"].reshape(P, -1), axis=1), 1e-30)
+    res["mixed_vs_fp32_all_probes"] = {"max": float(e.max()), "mean": float(e.mean())}
+    return res
 
 
 def batch_volumes(seed=SEED, nvol=256):
