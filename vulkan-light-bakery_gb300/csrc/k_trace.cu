@@ -677,6 +677,8 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
   return true;
 }
 
+constexpr int kStepsPerTurn = 4;
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
@@ -707,7 +709,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
       if (exhausted) break;
       continue;
     }
-    if (!L.has || !lr_step<COUNT>(a, L, stack, w)) continue;
+    if (!L.has) continue;
+    // up to kStepsPerTurn walk steps per turn: the refill bookkeeping is paid once
+    bool fin = false;
+#pragma unroll 1
+    for (int k = 0; k < kStepsPerTurn && !fin; ++k) fin = lr_step<COUNT>(a, L, stack, w);
+    if (!fin) continue;
     Shaded o;
     if (!lr_finish<COUNT>(a, L, o, w)) continue;
     L.has = false;
