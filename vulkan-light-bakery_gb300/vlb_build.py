@@ -98,12 +98,30 @@ def build_oracle(verbose: bool = False) -> Path:
     return out
 
 
+CLI = BUILD / "vlb-bake"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The vlb-bake executable (cli/vlb_bake.cpp) linked to libvlb.so, found
+    next to it at run time."""
+    src = PKG / "cli" / "vlb_bake.cpp"
+    if _stale(CLI, [src, LIB, REPO / "include" / "vlb.h"]):
+        tmp = BUILD / "vlb-bake.tmp"
+        _run(["g++", "-O2", "-std=c++17", "-Wall", f"-I{REPO / 'include'}", "-o", str(tmp), str(src),
+              f"-L{BUILD}", "-lvlb", "-Wl,-rpath,$ORIGIN"])
+        os.replace(tmp, CLI)
+    if verbose:
+        print(f"built {CLI}")
+    return CLI
+
+
 def build_all(verbose: bool = False) -> None:
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         f1 = ex.submit(build_library, verbose)
         f2 = ex.submit(build_oracle, verbose)
         f1.result()
         f2.result()
+    build_cli(verbose)
 
 
 if __name__ == "__main__":
