@@ -5,8 +5,9 @@
 // Tile layout: row r = probe*3 + channel, S samples contiguous per row.  The
 // basis table is S x 16 FP32 with the sample weight folded in.  One thread
 // owns one row; a CTA stages a [128 rows x 64 samples] block of the tile in
-// shared memory with coalesced row-segment loads (rows padded to 65 words so
-// the per-thread column walk is bank-conflict free), and the matching 64 x 16
+// shared memory with coalesced row-segment copies (cp.async for FP32, so a
+// thread's copies are all in flight at once; rows padded to 65 words so the
+// per-thread column walk is bank-conflict free), and the matching 64 x 16
 // basis block is read as warp-wide broadcasts.  Each row's sum runs in FP32
 // over its samples in a fixed order, so the result does not depend on the
 // launch shape or on other probes in the tile.
@@ -27,21 +28,52 @@ __device__ __forceinline__ float to_f32<float>(float v) { return v; }
 template <>
 __device__ __forceinline__ float to_f32<uint16_t>(uint16_t v) { return __uint_as_float(uint32_t(v) << 16); }
 
-template <typename T, int K>
-__global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad, uint32_t rows, uint32_t S,
-                                                       const float* __restrict__ basis16, float* __restrict__ out) {
-  __shared__ float tile[kProjRows][kProjCols + 1];
-  __shared__ __align__(16) float bas[kProjCols][16];
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t row0 = blockIdx.x * kProjRows;
-  const uint32_t row = row0 + tid;
-  float acc[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+// Global -> shared copies without a register round trip; valid == false
+// writes zeros (no bytes are read from src, which stays a valid address).
+__device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(gsrc), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* sdst, const float* gsrc, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(gsrc), "r"(valid ? 16 : 0) : "memory");
+}
 
-  for (uint32_t s0 = 0; s0 < S; s0 += kProjCols) {
-    const uint32_t ns = min(uint32_t(kProjCols), S - s0);
-    // coalesced staging: each warp loads 32 rows, two 32-sample halves per row
+// One stage: the [kProjRows x kProjCols] tile block (rows padded to
+// kProjCols + 1 words) and the matching basis rows.
+constexpr int kProjTileWords = kProjRows * (kProjCols + 1);
+constexpr int kProjStageWords = kProjTileWords + kProjCols * 16;
+static_assert(kProjTileWords % 4 == 0, "basis block must stay 16-byte aligned");
+
+// Stage loads.  FP32: asynchronous copies, so that all of a thread's loads
+// are in flight at once, zero-filled outside the tile; BF16: loads converted
+// through registers.  Coalesced: each warp loads 32 rows, 32-sample segments
+// per row.
+template <typename T>
+__device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_t rows, uint32_t S,
+                                              const float* __restrict__ basis16, uint32_t row0, uint32_t s0,
+                                              float* stage) {
+  float(*tile)[kProjCols + 1] = reinterpret_cast<float(*)[kProjCols + 1]>(stage);
+  float(*bas)[16] = reinterpret_cast<float(*)[16]>(stage + kProjTileWords);
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t ns = min(uint32_t(kProjCols), S - s0);
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll 8
+    for (uint32_t rr = warp; rr < kProjRows; rr += kProjRows / 32) {
+      const uint32_t gr = row0 + rr;
+#pragma unroll
+      for (int h = 0; h < kProjCols / 32; ++h) {
+        const uint32_t c = h * 32 + lane;
+        const bool ok = gr < rows && c < ns;
+        cp_async4(&tile[rr][c], ok ? reinterpret_cast<const float*>(rad) + size_t(gr) * S + s0 + c
+                                   : reinterpret_cast<const float*>(rad), ok);
+      }
+    }
+    for (uint32_t i = tid; i < kProjCols * 4; i += kProjRows) {
+      const uint32_t j = i / 4, q = i % 4;
+      cp_async16(&bas[j][4 * q], j < ns ? basis16 + size_t(s0 + j) * 16 + 4 * q : basis16, j < ns);
+    }
+  } else {
     for (uint32_t rr = warp; rr < kProjRows; rr += kProjRows / 32) {
       const uint32_t gr = row0 + rr;
 #pragma unroll
@@ -56,6 +88,26 @@ __global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad
       const uint32_t j = i / 16, k = i % 16;
       bas[j][k] = (j < ns) ? basis16[size_t(s0 + j) * 16 + k] : 0.f;
     }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad, uint32_t rows, uint32_t S,
+                                                       const float* __restrict__ basis16, float* __restrict__ out) {
+  __shared__ __align__(16) float stage[kProjStageWords];
+  const float(*tile)[kProjCols + 1] = reinterpret_cast<const float(*)[kProjCols + 1]>(stage);
+  const float(*bas)[16] = reinterpret_cast<const float(*)[16]>(stage + kProjTileWords);
+  const uint32_t tid = threadIdx.x;
+  const uint32_t row0 = blockIdx.x * kProjRows;
+  const uint32_t row = row0 + tid;
+  float acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.f;
+
+  for (uint32_t s0 = 0; s0 < S; s0 += kProjCols) {
+    project_stage<T>(rad, rows, S, basis16, row0, s0, stage);
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 #pragma unroll 4
     for (uint32_t j = 0; j < kProjCols; ++j) {

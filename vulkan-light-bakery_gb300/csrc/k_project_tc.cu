@@ -256,11 +256,8 @@ int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, co
   CUtensorMap ta, tb;
   if (!make_map(&ta, radiance, S, rows, S, kTileM)) return -1;
   if (!make_map(&tb, basis_bt, S, kTileN, bt_pitch, kTileN)) return -1;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_project_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
-    attr = true;
-  }
+  static std::atomic<uint64_t> opted{0};
+  smem_opt_in(k_project_tc, int(kSmemBytes), opted);
   const uint32_t ntiles = (rows + kTileM - 1) / kTileM;
   const uint32_t grid = std::min<uint32_t>(ntiles, uint32_t(num_sms));
   k_project_tc<<<grid, kTcThreads, kSmemBytes, s>>>(ta, tb, rows, S, K, out, err);

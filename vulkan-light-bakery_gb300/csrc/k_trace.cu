@@ -46,6 +46,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <climits>
 
 #include "vlb_device.cuh"
 #include "vlb_internal.h"
@@ -532,8 +533,9 @@ static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
 
 // ---- lane mode with per-lane ray fetch (tile output) ---------------------------------
 // Persistent warps; every lane runs its own ray through a small state machine
-// -- primary walk, shading, shadow walk, output -- one node or triangle per
-// loop turn, and takes a new ray as soon as it is done.  Idle lanes refill
+// -- primary walk, shading, shadow walk, output -- and takes a new ray as
+// soon as it is done (a turn walks nodes until the warp's lanes have each
+// found a leaf, then tests those leaves: lr_node / lr_leaf).  Idle lanes refill
 // together from a global ray counter (one atomic per refill, when half the
 // warp or all of it is idle), so a warp no longer waits for its slowest ray
 // and primary and shadow walks of different rays overlap.  Ray r is
@@ -560,13 +562,16 @@ __device__ __forceinline__ uint32_t lane_lt_mask() {
 }
 
 // One lane's ray: its walk and the pending shading of its primary hit.
+// cur: the next node (>= 0), triangle slot ~cur, or kWalkEnd; leaf: a
+// triangle slot parked for the next leaf phase (-1 none).
+constexpr int kWalkEnd = INT_MIN;
 struct LaneRay {
   bool has = false, shadow = false;
   uint32_t p = 0, s = 0;
   float ox = 0.f, oy = 0.f, oz = 0.f;
   float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
   RayCtx ray;
-  int cur = 0, sp = 0, slot = -1, id = -1;
+  int cur = 0, sp = 0, slot = -1, id = -1, leaf = -1;
   float tb = 0.f, lit = 0.f;
 };
 
@@ -586,6 +591,7 @@ __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uin
   L.sp = 0;
   L.slot = -1;
   L.id = -1;
+  L.leaf = -1;
   L.tb = a.tmax;
 }
 
@@ -677,7 +683,89 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
   return true;
 }
 
-constexpr int kStepsPerTurn = 4;
+// Speculative while-while walk.  Run one step per turn, a warp's lanes at an
+// inner node and its lanes at a (single-triangle) leaf take different
+// branches nearly every turn.  Here a turn has a node phase -- every lane
+// walks inner nodes until it meets a leaf, parks it (one slot), and walks on
+// past it while other lanes of the warp still look for theirs -- and then a
+// leaf phase in which all parked triangles are tested together.  Only the
+// visiting order changes: box tests are conservative, pruning keeps a margin
+// and ties go to the lower triangle id, so every ray's result is unchanged.
+__device__ __forceinline__ bool lr_is_tri(int cur) { return cur < 0 && cur != kWalkEnd; }
+
+__device__ __forceinline__ void lr_park(LaneRay& L, const int* stack) {
+  if (L.has && L.leaf < 0 && lr_is_tri(L.cur)) {
+    L.leaf = ~L.cur;
+    L.cur = L.sp ? stack[--L.sp] : kWalkEnd;
+  }
+}
+
+// One inner node: nearer hit child next, the farther one on the stack.
+template <bool COUNT, class A>
+__device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work& w) {
+  if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
+               n2 = __ldg(a.nodes + 4 * L.cur + 2), n3 = __ldg(a.nodes + 4 * L.cur + 3);
+  float tn0, tn1;
+  const float lim = prune_limit(L.tb);
+  const bool h0 = slab_rt(L.ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
+  const bool h1 = slab_rt(L.ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
+  const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+  if (h0 && h1) {
+    const bool first0 = tn0 <= tn1;
+    if (L.sp < kTraceStack) stack[L.sp++] = first0 ? c1 : c0;
+    else atomicAdd(a.err + kErrStackOverflow, 1);
+    L.cur = first0 ? c0 : c1;
+  } else if (h0) {
+    L.cur = c0;
+  } else if (h1) {
+    L.cur = c1;
+  } else {
+    L.cur = L.sp ? stack[--L.sp] : kWalkEnd;
+  }
+}
+
+// The parked triangle; an occluder ends a shadow walk.
+template <bool COUNT, class A>
+__device__ __forceinline__ void lr_leaf(const A& a, LaneRay& L, Work& w) {
+  if constexpr (COUNT) ++w.wtris;
+  const int ts = L.leaf;
+  L.leaf = -1;
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
+  const float t = tri_hit(L.ray, v0, e1, e2);
+  if (!(t > tlo)) return;
+  if (L.shadow) {
+    if (t < L.tb) { L.slot = ts; L.cur = kWalkEnd; L.sp = 0; }
+    return;
+  }
+  const int tid = __float_as_int(v0.w);
+  if (t < L.tb || (t == L.tb && L.slot >= 0 && tid < L.id)) { L.tb = t; L.slot = ts; L.id = tid; }
+}
+
+constexpr int kNodeSteps = 6;   // bound on one turn's node phase
+constexpr int kRefillIdle = 16; // idle lanes that trigger a refill (all idle always does)
+
+// A finished ray's tile entries (and debug arrays).
+__device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, const Shaded& o) {
+  const size_t ri = size_t(L.p) * a.S + L.s, row = size_t(L.p) * 3;
+  if (a.hit_tri) a.hit_tri[ri] = o.tri;
+  if (a.shadow) a.shadow[ri] = o.vis;
+  if (a.radiance) {
+    a.radiance[row * a.S + L.s] = o.r;
+    a.radiance[(row + 1) * a.S + L.s] = o.g;
+    a.radiance[(row + 2) * a.S + L.s] = o.b;
+  }
+  if (a.radiance_bf16) {
+    a.radiance_bf16[row * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
+    a.radiance_bf16[(row + 1) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
+    a.radiance_bf16[(row + 2) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
+  }
+  if (a.dbg_radiance) {
+    a.dbg_radiance[3 * ri] = o.r; a.dbg_radiance[3 * ri + 1] = o.g; a.dbg_radiance[3 * ri + 2] = o.b;
+  }
+}
 
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
@@ -691,7 +779,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
   bool exhausted = false;
   for (;;) {
     const unsigned idle = __ballot_sync(kFull, !L.has);
-    if (!exhausted && (idle == kFull || __popc(idle) >= 16)) {
+    if (!exhausted && (idle == kFull || __popc(idle) >= kRefillIdle)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (int(lane) == leader) base = atomicAdd(a.work_counter, uint32_t(__popc(idle)));
@@ -709,31 +797,23 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
       if (exhausted) break;
       continue;
     }
-    if (!L.has) continue;
-    // up to kStepsPerTurn walk steps per turn: the refill bookkeeping is paid once
-    bool fin = false;
+    // node phase (all lanes take part in the vote)
 #pragma unroll 1
-    for (int k = 0; k < kStepsPerTurn && !fin; ++k) fin = lr_step<COUNT>(a, L, stack, w);
-    if (!fin) continue;
+    for (int k = 0; k < kNodeSteps; ++k) {
+      lr_park(L, stack);
+      const bool at_node = L.has && L.cur >= 0;
+      if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
+      if (at_node) lr_node<COUNT>(a, L, stack, w);
+    }
+    lr_park(L, stack);
+    if (!L.has) continue;
+    // leaf phase
+    if (L.leaf >= 0) lr_leaf<COUNT>(a, L, w);
+    if (L.cur != kWalkEnd) continue;
     Shaded o;
     if (!lr_finish<COUNT>(a, L, o, w)) continue;
     L.has = false;
-    const size_t ri = size_t(L.p) * a.S + L.s, row = size_t(L.p) * 3;
-    if (a.hit_tri) a.hit_tri[ri] = o.tri;
-    if (a.shadow) a.shadow[ri] = o.vis;
-    if (a.radiance) {
-      a.radiance[row * a.S + L.s] = o.r;
-      a.radiance[(row + 1) * a.S + L.s] = o.g;
-      a.radiance[(row + 2) * a.S + L.s] = o.b;
-    }
-    if (a.radiance_bf16) {
-      a.radiance_bf16[row * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.r));
-      a.radiance_bf16[(row + 1) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.g));
-      a.radiance_bf16[(row + 2) * a.S + L.s] = __bfloat16_as_ushort(__float2bfloat16_rn(o.b));
-    }
-    if (a.dbg_radiance) {
-      a.dbg_radiance[3 * ri] = o.r; a.dbg_radiance[3 * ri + 1] = o.g; a.dbg_radiance[3 * ri + 2] = o.b;
-    }
+    emit_tile(a, L, o);
   }
   if constexpr (COUNT) {
     atomicAdd(a.counters + 0, (unsigned long long)w.wnodes);
@@ -745,19 +825,21 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
 
 template <bool COUNT>
 static void launch_dyn(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  auto kern = k_trace_dyn<COUNT>;
   static int per_sm = 0;
   if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_dyn<COUNT>, kTraceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
   }
   const uint64_t rays = uint64_t((a.nprobes + 31) / 32 * 32) * a.S;
   const uint64_t ctas = std::min<uint64_t>((rays + kTraceThreads - 1) / kTraceThreads, uint64_t(num_sms) * per_sm);
-  k_trace_dyn<COUNT><<<uint32_t(std::max<uint64_t>(ctas, 1)), kTraceThreads, 0, s>>>(a);
+  kern<<<uint32_t(std::max<uint64_t>(ctas, 1)), kTraceThreads, 0, s>>>(a);
 }
 
 // The ray counter runs past R by at most 32 per resident warp: R < 2^31 keeps it in 32 bits.
 bool trace_dyn_supported(const TraceArgs& a) {
-  return a.lane && a.ntris > 0 && uint64_t((a.nprobes + 31) / 32 * 32) * a.S < (1ull << 31);
+  return a.lane && a.ntris > 0 && a.ntris < 0x7fffffffu &&
+         uint64_t((a.nprobes + 31) / 32 * 32) * a.S < (1ull << 31);
 }
 
 void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {

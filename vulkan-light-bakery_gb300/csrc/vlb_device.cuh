@@ -3,9 +3,23 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 namespace vlbk {
+
+// Opts a kernel in to `bytes` of dynamic shared memory on the current device,
+// once per device (the attribute is per device; `done` is the caller's
+// per-kernel bit set of devices already set).
+template <class F>
+inline void smem_opt_in(F* kernel, int bytes, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+  if (bit && (done.load(std::memory_order_relaxed) & bit)) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  done.fetch_or(bit, std::memory_order_relaxed);
+}
 
 // Real SH basis with the reference's 6-digit constants
 // (shaders/sh_common.h:26-116), index k = l(l+1)+m, l <= LMAX.
