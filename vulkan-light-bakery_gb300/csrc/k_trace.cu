@@ -595,49 +595,6 @@ __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uin
   L.tb = a.tmax;
 }
 
-// One node or triangle of the lane's current walk (nearer child first, the
-// pruning margin and tie rule of lane_traverse); true when the walk is over.
-template <bool COUNT, class A>
-__device__ __forceinline__ bool lr_step(const A& a, LaneRay& L, int* stack, Work& w) {
-  if (a.ntris == 0) return true;
-  const float tlo = L.shadow ? 0.0f : a.tmin;
-  if (L.cur >= 0) {
-    if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
-    const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
-                 n2 = __ldg(a.nodes + 4 * L.cur + 2), n3 = __ldg(a.nodes + 4 * L.cur + 3);
-    float tn0, tn1;
-    const float lim = prune_limit(L.tb);
-    const bool h0 = slab_rt(L.ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
-    const bool h1 = slab_rt(L.ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
-    const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-    if (h0 && h1) {
-      const bool first0 = tn0 <= tn1;
-      if (L.sp < kTraceStack) stack[L.sp++] = first0 ? c1 : c0;
-      else atomicAdd(a.err + kErrStackOverflow, 1);
-      L.cur = first0 ? c0 : c1;
-      return false;
-    }
-    if (h0) { L.cur = c0; return false; }
-    if (h1) { L.cur = c1; return false; }
-  } else {
-    if constexpr (COUNT) ++w.wtris;
-    const int ts = ~L.cur;
-    const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
-    const float t = tri_hit(L.ray, v0, e1, e2);
-    if (t > tlo) {
-      if (L.shadow) {
-        if (t < L.tb) { L.slot = ts; return true; }
-      } else {
-        const int tid = __float_as_int(v0.w);
-        if (t < L.tb || (t == L.tb && L.slot >= 0 && tid < L.id)) { L.tb = t; L.slot = ts; L.id = tid; }
-      }
-    }
-  }
-  if (L.sp == 0) return true;
-  L.cur = stack[--L.sp];
-  return false;
-}
-
 // After a walk.  A finished primary walk is shaded: a miss takes the sky, a
 // lit-facing hit starts its shadow walk (returns false: the lane walks on,
 // the triangle id and sun term wait in id / lit), anything else is done.  A
@@ -930,7 +887,18 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
         if (r0 >= r1) break;
         continue;
       }
-      if (!L.has || !lr_step<false>(j, L, stack, w)) continue;
+      // one while-while turn, as in k_trace_dyn
+#pragma unroll 1
+      for (int k = 0; k < kNodeSteps; ++k) {
+        lr_park(L, stack);
+        const bool at_node = L.has && L.cur >= 0;
+        if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
+        if (at_node) lr_node<false>(j, L, stack, w);
+      }
+      lr_park(L, stack);
+      if (!L.has) continue;
+      if (L.leaf >= 0) lr_leaf<false>(j, L, w);
+      if (L.cur != kWalkEnd) continue;
       if (!L.shadow && j.hits_out) j.hits_out[size_t(L.p) * j.S + L.s] = make_int2(L.slot, __float_as_int(L.tb));
       Shaded o;
       if (!lr_finish<false>(j, L, o, w)) continue;
