@@ -201,13 +201,17 @@ typedef enum vlb_precision {
 } vlb_precision;
 /* vlb_bake_params.flags: with VLB_PREC_FUSED, always run the one-kernel schedule. */
 #define VLB_BAKE_FORCE_FUSED_KERNEL 1u
-/* vlb_bake_params.flags: BVH traversal mode.  Packet: a warp walks the union
- * of its 32 probes' paths once (coherent probes); lane: every ray walks its own
- * path (probes sparse against the geometry).  Results do not depend on the
- * mode; without either bit the library picks per bake from the triangle and
- * probe counts. */
+/* vlb_bake_params.flags: traversal mode.  Packet: a warp walks the union of
+ * its 32 probes' BVH paths once (coherent probes); lane: every ray walks its
+ * own BVH path (probes sparse against the geometry); grid: the rays of each
+ * direction are parallel, so each direction (and the sun) gets a 2D grid of
+ * the projected triangles and a ray tests only its own cell (scenes of at
+ * most 4096 triangles; others walk the tree; only on request).  Results do
+ * not depend on the mode; without a bit the library picks packet or lane per
+ * bake from the triangle and probe counts. */
 #define VLB_BAKE_TRAVERSAL_PACKET 2u
 #define VLB_BAKE_TRAVERSAL_LANE 4u
+#define VLB_BAKE_TRAVERSAL_GRID 8u
 
 typedef struct vlb_bake_params {
   uint32_t lmax;          /* 2: 9 coefficients, 3: 16 (the reference) */

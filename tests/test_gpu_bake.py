@@ -126,6 +126,58 @@ def test_traversal_modes_agree(ctx, nboxes, counts):
         assert not cls["unexplained"], cls["unexplained"][:10]
 
 
+def _big_triangles(seed, n):
+    """n large random triangles across the unit cube (every grid cell holds
+    most of them: the grids overflow and the rays walk the tree)."""
+    rng = np.random.default_rng(seed)
+    pos = rng.random((3 * n, 3)).astype(np.float32)
+    idx = np.arange(3 * n, dtype=np.uint32).reshape(n, 3)
+    alb = rng.uniform(0.2, 0.8, (n, 3)).astype(np.float32)
+    return pos, idx, alb
+
+
+@pytest.mark.parametrize("case", ["c1", "random_probes", "far_probes", "overflow", "one_triangle"])
+def test_grid_mode_agrees(ctx, case):
+    """Grid mode (per-direction triangle grids) gives the tree walk's per-ray
+    decisions, radiance and coefficients bit for bit: dense grid probes,
+    random probes in a 3.6k-triangle scene (16 x 16 cells), probes far
+    outside the scene (their rays walk the tree), grids that overflow their
+    capacity (all rays walk the tree) and a one-triangle scene."""
+    rng = np.random.default_rng(7)
+    S = 256
+    sun = vlb.synth_sun(3)
+    if case == "c1":
+        pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=11)
+    elif case in ("random_probes", "far_probes"):
+        pos, idx, alb = vlb.synth_box_scene(5, 300)
+        probes = rng.random((2048, 3)).astype(np.float32)
+        if case == "far_probes":
+            probes[::3] = probes[::3] * 600.0 - 300.0
+    elif case == "overflow":
+        pos, idx, alb = _big_triangles(2, 4000)
+        probes = rng.random((512, 3)).astype(np.float32)
+    else:
+        pos = np.float32([[0.1, 0.1, 0.5], [0.9, 0.2, 0.5], [0.4, 0.9, 0.5]])
+        idx, alb = np.uint32([[0, 1, 2]]), np.float32([[0.5, 0.6, 0.7]])
+        probes = rng.random((300, 3)).astype(np.float32)
+    scene = ctx.scene(pos, idx, alb)
+    ds = ctx.fibonacci(S)
+    res = []
+    for flag in (vlb.BAKE_TRAVERSAL_GRID, vlb.BAKE_TRAVERSAL_LANE):
+        p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun)
+        p.flags = flag
+        ctx.profile_reset(); ctx.set_profiling(True)
+        res.append(ctx.bake(scene, probes, p, debug=True))
+        ctx.set_profiling(False)
+        if flag == vlb.BAKE_TRAVERSAL_GRID:
+            assert "grid_build" in ctx.profile()
+    (sa, ha, va, ra), (sb, hb, vb, rb) = res
+    diff = np.argwhere((ha != hb) | (va != vb))
+    assert len(diff) == 0, f"{len(diff)} of {ha.size} rays differ, first {diff[:5].tolist()}"
+    assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+    assert (hb >= 0).any()
+
+
 @pytest.mark.parametrize("nboxes,counts", [(64, (16, 16, 16)), (4000, (6, 6, 6))])
 def test_traversal_trees_agree(ctx, nboxes, counts):
     """The clustered traversal tree and the Karras LBVH give the same per-ray
@@ -138,6 +190,7 @@ def test_traversal_trees_agree(ctx, nboxes, counts):
     for flags in (0, vlb.SCENE_TRAVERSAL_LBVH):
         scene = ctx.scene(pos, idx, alb, flags=flags)
         p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun, sky=skyh)
+        p.flags = vlb.BAKE_TRAVERSAL_LANE  # a tree walk in both
         res.append(ctx.bake(scene, probes, p, debug=True))
         st = vlb.trace_stats(ctx, scene, probes, p)
         work.append(st["node_tests"] / (st["rays"] + st["shadow_rays"]))

@@ -799,7 +799,369 @@ bool trace_dyn_supported(const TraceArgs& a) {
          uint64_t((a.nprobes + 31) / 32 * 32) * a.S < (1ull << 31);
 }
 
+// ---- grid mode: parallel rays through per-direction triangle grids -----------------
+// Every probe of a bake traces the same directions and every shadow ray goes
+// toward the sun, so the rays of one direction are parallel.  For each
+// direction (grid g < S) and for the sun (grid S) one CTA projects the
+// triangles onto a plane across the direction, bins their 2D boxes (widened
+// by a margin) into a G x G grid over the projected scene and sorts each
+// cell by near depth.  A ray then visits only the cell of its 2D point:
+// entries that end before its interval are skipped, entries whose widened
+// box misses the point are skipped, and the rest are tested with tri_hit in
+// near-depth order until the next entry's nearest possible depth exceeds
+// the pruning limit of the best hit (the tree walks' margin).  Every
+// triangle tri_hit can report for the ray is in that cell (the margin,
+// 2^-12 of the scene's coordinate scale, covers the FP32 projection error of
+// triangles and of origins within grid_far of the origin), so each ray's
+// result is that of the tree walks.  A grid whose entries overflow its
+// capacity, and origins beyond grid_far, walk the tree instead.
+
+// Monotone cell index (the same function bins the boxes and locates rays).
+__device__ __forceinline__ uint32_t grid_cell(float x, float lo, float inv, uint32_t G) {
+  return uint32_t(fminf(fmaxf((x - lo) * inv, 0.f), float(G - 1)));
+}
+
+// A basis (u, v) across d (any: exactness comes from the margins).
+__device__ __forceinline__ void grid_basis(float dx, float dy, float dz, float3& u, float3& v) {
+  const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  const float cx = (ax <= ay && ax <= az) ? 1.f : 0.f;
+  const float cy = (cx == 0.f && ay <= az) ? 1.f : 0.f;
+  const float cz = (cx == 0.f && cy == 0.f) ? 1.f : 0.f;
+  float ux = dy * cz - dz * cy, uy = dz * cx - dx * cz, uz = dx * cy - dy * cx;
+  const float rn = rsqrtf(ux * ux + uy * uy + uz * uz);
+  ux *= rn; uy *= rn; uz *= rn;
+  u = make_float3(ux, uy, uz);
+  v = make_float3(dy * uz - dz * uy, dz * ux - dx * uz, dx * uy - dy * ux);
+}
+
+__device__ __forceinline__ float dot3(float x, float y, float z, float3 a) {
+  return fmaf(z, a.z, fmaf(y, a.y, x * a.x));
+}
+
+size_t grid_build_smem(uint32_t G, uint32_t ntris) {
+  return (2 * size_t(G) * G + 1) * 4 + size_t(ntris) * 8 + size_t(kGridCap) * 2;
+}
+
+// Block-wide exclusive scan of v[0, n) in place (kGridThreads threads, runs of
+// ceil(n / threads) per thread); returns the total.
+__device__ uint32_t grid_scan(uint32_t* v, uint32_t n, uint32_t* wsum) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t per = (n + kGridThreads - 1) / kGridThreads, c0 = tid * per;
+  uint32_t run = 0;
+  for (uint32_t k = 0; k < per; ++k)
+    if (c0 + k < n) run += v[c0 + k];
+  uint32_t inc = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (int(lane) >= o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t off = 0, total = 0;
+  for (uint32_t k = 0; k < kGridThreads / 32; ++k) {
+    if (k < warp) off += wsum[k];
+    total += wsum[k];
+  }
+  off += inc - run;
+  for (uint32_t k = 0; k < per; ++k)
+    if (c0 + k < n) {
+      const uint32_t x = v[c0 + k];
+      v[c0 + k] = off;
+      off += x;
+    }
+  __syncthreads();
+  return total;
+}
+
+// One CTA per grid.  Shared memory: counts / start offsets (G*G+1), fill
+// cursors (G*G), per triangle its packed cell range and near depth, then the
+// entries.
+__global__ void __launch_bounds__(kGridThreads) k_grid_build(const TraceArgs a) {
+  extern __shared__ __align__(16) uint8_t gsm[];
+  const uint32_t G = a.grid_g, GG = G * G, T = a.ntris;
+  uint32_t* start = reinterpret_cast<uint32_t*>(gsm);
+  uint32_t* cur = start + GG + 1;
+  uint32_t* tcell = cur + GG;
+  float* tnear = reinterpret_cast<float*>(tcell + T);
+  uint16_t* ent = reinterpret_cast<uint16_t*>(tnear + T);
+  __shared__ float red[4][kGridThreads / 32];
+  __shared__ uint32_t wsum[kGridThreads / 32];
+  const uint32_t gi = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float dx, dy, dz;
+  if (gi < a.S) {
+    const float4 d = __ldg(a.dirs + gi);
+    dx = d.x; dy = d.y; dz = d.z;
+  } else {
+    dx = a.sun.x; dy = a.sun.y; dz = a.sun.z;
+  }
+  float3 u, v;
+  grid_basis(dx, dy, dz, u, v);
+  const float id2 = 1.0f / (dx * dx + dy * dy + dz * dz);
+  const float3 dn = make_float3(dx * id2, dy * id2, dz * id2);  // depth in units of t
+  const float m = a.grid_margin;
+  float4* box = a.grid_box + size_t(gi) * T;
+  float2* dep = a.grid_dep + size_t(gi) * T;
+  for (uint32_t c = tid; c < GG; c += kGridThreads) start[c] = 0;
+  // pass 1: widened 2D boxes and depth ranges; the extent of the boxes
+  float lu = INFINITY, hu = -INFINITY, lv = INFINITY, hv = -INFINITY;
+  for (uint32_t t = tid; t < T; t += kGridThreads) {
+    const float4 v0 = __ldg(a.tris + 3 * t), e1 = __ldg(a.tris + 3 * t + 1), e2 = __ldg(a.tris + 3 * t + 2);
+    const float px[3] = {v0.x, v0.x + e1.x, v0.x + e2.x}, py[3] = {v0.y, v0.y + e1.y, v0.y + e2.y},
+                pz[3] = {v0.z, v0.z + e1.z, v0.z + e2.z};
+    float pu[3], pv[3], pd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      pu[k] = dot3(px[k], py[k], pz[k], u);
+      pv[k] = dot3(px[k], py[k], pz[k], v);
+      pd[k] = dot3(px[k], py[k], pz[k], dn);
+    }
+    const float4 b = make_float4(fmin3(pu[0], pu[1], pu[2]) - m, fmax3(pu[0], pu[1], pu[2]) + m,
+                                 fmin3(pv[0], pv[1], pv[2]) - m, fmax3(pv[0], pv[1], pv[2]) + m);
+    const float2 dd = make_float2(fmin3(pd[0], pd[1], pd[2]), fmax3(pd[0], pd[1], pd[2]));
+    box[t] = b;
+    dep[t] = dd;
+    tnear[t] = dd.x;
+    lu = fminf(lu, b.x); hu = fmaxf(hu, b.y); lv = fminf(lv, b.z); hv = fmaxf(hv, b.w);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lu = fminf(lu, __shfl_xor_sync(kFull, lu, o)); hu = fmaxf(hu, __shfl_xor_sync(kFull, hu, o));
+    lv = fminf(lv, __shfl_xor_sync(kFull, lv, o)); hv = fmaxf(hv, __shfl_xor_sync(kFull, hv, o));
+  }
+  if (lane == 0) { red[0][warp] = lu; red[1][warp] = hu; red[2][warp] = lv; red[3][warp] = hv; }
+  __syncthreads();
+  lu = red[0][0]; hu = red[1][0]; lv = red[2][0]; hv = red[3][0];
+  for (int k = 1; k < kGridThreads / 32; ++k) {
+    lu = fminf(lu, red[0][k]); hu = fmaxf(hu, red[1][k]); lv = fminf(lv, red[2][k]); hv = fmaxf(hv, red[3][k]);
+  }
+  const float iu = float(G) / fmaxf(hu - lu, 1e-30f), iv = float(G) / fmaxf(hv - lv, 1e-30f);
+  // pass 2: cell ranges and counts
+  for (uint32_t t = tid; t < T; t += kGridThreads) {
+    const float4 b = box[t];
+    const uint32_t i0 = grid_cell(b.x, lu, iu, G), i1 = grid_cell(b.y, lu, iu, G);
+    const uint32_t j0 = grid_cell(b.z, lv, iv, G), j1 = grid_cell(b.w, lv, iv, G);
+    tcell[t] = i0 | (i1 << 8) | (j0 << 16) | (j1 << 24);
+    for (uint32_t i = i0; i <= i1; ++i)
+      for (uint32_t j = j0; j <= j1; ++j) atomicAdd(&start[i * G + j], 1u);
+  }
+  __syncthreads();
+  const uint32_t total = grid_scan(start, GG, wsum);
+  for (uint32_t c = tid; c < GG; c += kGridThreads) cur[c] = start[c];
+  if (tid == 0) start[GG] = total;
+  float4* hdr = a.grid_hdr + 4 * size_t(gi);
+  if (total > kGridCap) {  // too many entries: this grid's rays walk the tree
+    if (tid == 0) hdr[3] = make_float4(iv, __int_as_float(0), 0.f, 0.f);
+    return;
+  }
+  __syncthreads();
+  // pass 3: fill
+  for (uint32_t t = tid; t < T; t += kGridThreads) {
+    const uint32_t cr = tcell[t];
+    const uint32_t i0 = cr & 255, i1 = (cr >> 8) & 255, j0 = (cr >> 16) & 255, j1 = cr >> 24;
+    for (uint32_t i = i0; i <= i1; ++i)
+      for (uint32_t j = j0; j <= j1; ++j) ent[atomicAdd(&cur[i * G + j], 1u)] = uint16_t(t);
+  }
+  __syncthreads();
+  // pass 4: each cell by (near depth, slot): Shell sort with Ciura's gaps
+  for (uint32_t c = tid; c < GG; c += kGridThreads) {
+    uint16_t* e = ent + start[c];
+    const int n = int(start[c + 1] - start[c]);
+    const int gaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+    for (int gk = 0; gk < 8; ++gk) {
+      const int gap = gaps[gk];
+      for (int i = gap; i < n; ++i) {
+        const uint16_t x = e[i];
+        const float kx = tnear[x];
+        int j = i;
+        while (j >= gap) {
+          const uint16_t y = e[j - gap];
+          const float ky = tnear[y];
+          if (ky < kx || (ky == kx && y < x)) break;
+          e[j] = y;
+          j -= gap;
+        }
+        e[j] = x;
+      }
+    }
+  }
+  __syncthreads();
+  // pass 5: out
+  uint32_t* cells = a.grid_cells + size_t(gi) * (GG + 1);
+  for (uint32_t c = tid; c <= GG; c += kGridThreads) cells[c] = start[c];
+  uint16_t* eo = a.grid_ent + size_t(gi) * kGridCap;
+  for (uint32_t k = tid; k < total; k += kGridThreads) eo[k] = ent[k];
+  if (tid == 0) {
+    hdr[0] = make_float4(u.x, u.y, u.z, lu);
+    hdr[1] = make_float4(v.x, v.y, v.z, lv);
+    hdr[2] = make_float4(dn.x, dn.y, dn.z, iu);
+    hdr[3] = make_float4(iv, __int_as_float(1), 0.f, 0.f);
+  }
+}
+
+void launch_grid_build(const TraceArgs& a, cudaStream_t s) {
+  if (!a.grid_hdr || a.ntris == 0) return;
+  static std::atomic<uint64_t> opted{0};
+  smem_opt_in(k_grid_build, int(grid_build_smem(32, kGridMaxTris)), opted);  // the largest launch
+  const size_t smem = grid_build_smem(a.grid_g, a.ntris);
+  k_grid_build<<<a.S + 1, kGridThreads, smem, s>>>(a);
+}
+
+// A lane's walk through one grid cell: the cell's entry range [e, e1), the
+// ray's 2D point and depth, and the next entry's triangle (loaded a step
+// ahead, so a step's depth-range, box and next-entry loads go out together).
+struct GridWalk {
+  uint32_t e = 0, e1 = 0, gi = 0, nt = 0;
+  float pu = 0.f, pv = 0.f, pd = 0.f;
+};
+
+// Sets up the walk of L's current ray through grid gi; false when the grid
+// overflowed or the origin is beyond grid_far (the caller walks the tree).
+__device__ __forceinline__ bool grid_setup(const TraceArgs& a, uint32_t gi, const LaneRay& L, GridWalk& g) {
+  const float4 h3 = __ldg(a.grid_hdr + 4 * gi + 3);
+  const float ox = L.ray.ox, oy = L.ray.oy, oz = L.ray.oz;
+  if (__float_as_int(h3.y) == 0 || fmax3(fabsf(ox), fabsf(oy), fabsf(oz)) > a.grid_far) return false;
+  const float4 h0 = __ldg(a.grid_hdr + 4 * gi), h1 = __ldg(a.grid_hdr + 4 * gi + 1),
+               h2 = __ldg(a.grid_hdr + 4 * gi + 2);
+  const uint32_t G = a.grid_g;
+  g.gi = gi;
+  g.pu = dot3(ox, oy, oz, make_float3(h0.x, h0.y, h0.z));
+  g.pv = dot3(ox, oy, oz, make_float3(h1.x, h1.y, h1.z));
+  g.pd = dot3(ox, oy, oz, make_float3(h2.x, h2.y, h2.z));
+  const uint32_t c = grid_cell(g.pu, h0.w, h2.w, G) * G + grid_cell(g.pv, h1.w, h3.x, G);
+  const uint32_t* cells = a.grid_cells + size_t(gi) * (G * G + 1);
+  g.e = __ldg(cells + c);
+  g.e1 = __ldg(cells + c + 1);
+  if (g.e < g.e1) g.nt = __ldg(a.grid_ent + size_t(gi) * kGridCap + g.e);
+  return true;
+}
+
+// One entry of the walk (shadow walks: any hit in (0, L.tb); primary walks:
+// nearest hit beyond tmin with the tie rule); g.e = g.e1 when the walk is over.
+template <bool COUNT>
+__device__ __forceinline__ void grid_step(const TraceArgs& a, LaneRay& L, GridWalk& g, Work& w) {
+  const uint32_t t = g.nt, T = a.ntris;
+  const float2 dd = __ldg(a.grid_dep + size_t(g.gi) * T + t);
+  const float4 b = __ldg(a.grid_box + size_t(g.gi) * T + t);
+  if (g.e + 1 < g.e1) g.nt = __ldg(a.grid_ent + size_t(g.gi) * kGridCap + g.e + 1);
+  ++g.e;
+  if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+  const float tlo = L.shadow ? 0.0f : a.tmin, m = a.grid_margin;
+  if (dd.y - g.pd + m <= tlo) return;                                   // ends before the interval
+  if (dd.x - g.pd - m > prune_limit(L.tb)) { g.e = g.e1; return; }      // this and every later entry too far
+  if (g.pu < b.x || g.pu > b.y || g.pv < b.z || g.pv > b.w) return;
+  if constexpr (COUNT) ++w.wtris;
+  const float4 v0 = __ldg(a.tris + 3 * t), e1 = __ldg(a.tris + 3 * t + 1), e2 = __ldg(a.tris + 3 * t + 2);
+  const float th = tri_hit(L.ray, v0, e1, e2);
+  if (!(th > tlo)) return;
+  if (L.shadow) {
+    if (th < L.tb) { L.slot = int(t); g.e = g.e1; }
+    return;
+  }
+  const int tid = __float_as_int(v0.w);
+  if (th < L.tb || (th == L.tb && L.slot >= 0 && tid < L.id)) { L.tb = th; L.slot = int(t); L.id = tid; }
+}
+
+// Starts the current walk of L (primary: grid L.s; shadow: grid S).  Where
+// the grid cannot take the ray, the tree walk runs to its end here and the
+// grid walk is left empty.
+template <bool COUNT>
+__device__ __forceinline__ void grid_begin(const TraceArgs& a, LaneRay& L, GridWalk& g, Work& w) {
+  const uint32_t gi = L.shadow ? a.S : L.s;
+  if (grid_setup(a, gi, L, g)) return;
+  g.e = g.e1 = 0;
+  bool active = true;
+  const float dx = L.shadow ? a.sun.x : L.d.x, dy = L.shadow ? a.sun.y : L.d.y, dz = L.shadow ? a.sun.z : L.d.z;
+  if (L.shadow)
+    traverse<true, COUNT, true>(octant_of(dx, dy, dz), L.ray, active, a.nodes, a.tris, a.ntris, 0.0f, L.tb, L.slot,
+                                L.id, a.err, w);
+  else
+    traverse<false, COUNT, true>(octant_of(dx, dy, dz), L.ray, active, a.nodes, a.tris, a.ntris, a.tmin, L.tb,
+                                 L.slot, L.id, a.err, w);
+}
+
+constexpr int kGridSteps = 8;  // entry steps per turn
+
+// Persistent warps; each lane runs its rays through a small state machine --
+// primary cell walk, shading, shadow cell walk, tile entries -- and idle
+// lanes refill together from the ray counter (as k_trace_dyn): rays fetched
+// together share a direction and are Morton neighbours.
+template <bool COUNT>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_grid(const TraceArgs a) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t P = (a.nprobes + 31) / 32 * 32;
+  const uint32_t R = P * a.S;
+  Work w;
+  LaneRay L;
+  GridWalk g;
+  make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
+  bool exhausted = false;
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, !L.has);
+    if (!exhausted && (idle == kFull || __popc(idle) >= kRefillIdle)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (int(lane) == leader) base = atomicAdd(a.work_counter, uint32_t(__popc(idle)));
+      base = __shfl_sync(kFull, base, leader);
+      if (base >= R) exhausted = true;
+      if (!L.has) {
+        const uint32_t r = base + __popc(idle & lane_lt_mask());
+        if (r < R) {
+          const uint32_t t = r / P, sl = r - t * P;
+          if (sl < a.nprobes) {
+            lr_start(a, L, a.order[sl], __ldg(a.dir_order + t));
+            grid_begin<COUNT>(a, L, g, w);
+          }
+        }
+      }
+    }
+    if (!__any_sync(kFull, L.has)) {
+      if (exhausted) break;
+      continue;
+    }
+#pragma unroll 1
+    for (int k = 0; k < kGridSteps; ++k) {
+      const bool walking = L.has && g.e < g.e1;
+      if (!__any_sync(kFull, walking)) break;
+      if (walking) grid_step<COUNT>(a, L, g, w);
+    }
+    if (!L.has || g.e < g.e1) continue;
+    Shaded o;
+    if (!lr_finish<COUNT>(a, L, o, w)) {  // a lit hit: its shadow walk
+      grid_begin<COUNT>(a, L, g, w);
+      continue;
+    }
+    L.has = false;
+    emit_tile(a, L, o);
+  }
+  if constexpr (COUNT) {
+    atomicAdd(a.counters + 0, (unsigned long long)w.wnodes);
+    atomicAdd(a.counters + 1, (unsigned long long)w.wtris);
+    atomicAdd(a.counters + 2, (unsigned long long)w.shadow);
+    atomicAdd(a.counters + 3, (unsigned long long)w.lnodes);
+  }
+}
+
+template <bool COUNT>
+static void launch_grid_trace(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_grid<COUNT>, kTraceThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const uint64_t rays = uint64_t((a.nprobes + 31) / 32 * 32) * a.S;
+  const uint64_t ctas = std::min<uint64_t>((rays + kTraceThreads - 1) / kTraceThreads, uint64_t(num_sms) * per_sm);
+  k_trace_grid<COUNT><<<uint32_t(std::max<uint64_t>(ctas, 1)), kTraceThreads, 0, s>>>(a);
+}
+
+bool grid_supported(uint32_t ntris, uint32_t nprobes, uint32_t S) {
+  return ntris > 0 && ntris <= kGridMaxTris && uint64_t((nprobes + 31) / 32 * 32) * S < (1ull << 31);
+}
+
 void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
+  if (a.grid_hdr) {
+    if (a.counters) launch_grid_trace<true>(a, num_sms, s);
+    else launch_grid_trace<false>(a, num_sms, s);
+    return;
+  }
   if (trace_dyn_supported(a)) {
     if (a.counters) launch_dyn<true>(a, num_sms, s);
     else launch_dyn<false>(a, num_sms, s);

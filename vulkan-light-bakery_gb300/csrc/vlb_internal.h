@@ -151,7 +151,22 @@ struct TraceArgs {
   uint32_t lane;          // 1: per-lane traversal, 0: packet traversal
   unsigned long long* counters;  // null, or [warp node fetches, warp triangle fetches, shadow rays, lane node tests]
   int* err;
+  // grid mode (null grid_hdr: tree walks): grid g < S for direction g, grid S for the sun
+  float4* grid_hdr;       // [S+1][4]: (u, lo_u), (v, lo_v), (d / |d|^2, 1 / cell_u), (1 / cell_v, ok, -, -)
+  uint32_t* grid_cells;   // [S+1][G*G+1] entry offsets per cell
+  uint16_t* grid_ent;     // [S+1][kGridCap] triangle slots, cell by cell, by near depth
+  float4* grid_box;       // [S+1][ntris] widened 2D boxes (umin, umax, vmin, vmax)
+  float2* grid_dep;       // [S+1][ntris] depth range along d in units of t
+  uint32_t grid_g;        // cells per side
+  float grid_margin;      // 2^-12 of the scene's coordinate scale
+  float grid_far;         // origins with a larger coordinate walk the tree
 };
+constexpr int kGridThreads = 256;
+constexpr uint32_t kGridMaxTris = 4096;  // grid mode's triangle limit
+constexpr uint32_t kGridCap = 24576;     // entries per grid
+size_t grid_build_smem(uint32_t G, uint32_t ntris);
+bool grid_supported(uint32_t ntris, uint32_t nprobes, uint32_t S);
+void launch_grid_build(const TraceArgs& a, cudaStream_t s);
 constexpr int kTraceWarps = 4;
 // Chooses dirs_per_warp / chunks for nprobes x S rays on num_sms SMs: fine
 // items for load balance, coarser in fused mode where each item leaves a
@@ -259,6 +274,7 @@ struct vlb_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   int* d_err = nullptr;  // vlbk::kErrSlots ints
+  int* h_err = nullptr;  // pinned host copy, read back with a synchronised call's last copy
   uint64_t launches = 0;
   bool host_inputs_pending = false;  // a host array was copied in by the current call
   bool profiling = false;

@@ -24,7 +24,7 @@ TEXEL_RGB32F, TEXEL_RGBA8 = 0, 1
 SKY_REF_BGRA_SWAP = 1
 PREC_FP32, PREC_FUSED, PREC_MIXED = 0, 1, 2
 BAKE_FORCE_FUSED_KERNEL = 1
-BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE = 2, 4
+BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE, BAKE_TRAVERSAL_GRID = 2, 4, 8
 SCENE_TRAVERSAL_LBVH = 1
 DTYPE_F32, DTYPE_BF16 = 0, 1
 

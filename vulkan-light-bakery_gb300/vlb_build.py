@@ -52,11 +52,14 @@ def build_library(verbose: bool = False, extra_nvcc: list[str] | None = None) ->
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     inc = _cuda_home() / "include"
-    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "vlb.h"]
+    # every object also depends on this file (its compiler flags)
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "vlb.h", Path(__file__)]
     jobs = []
     for cu in sorted(CSRC.glob("*.cu")):
         obj = BUILD / (cu.stem + ".o")
-        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+        # -fmad=false: device arithmetic exactly as written (explicit fmaf stays fused), so a ray's
+        # FP32 decisions do not depend on how a build schedules or allocates registers
+        cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
                "-ffp-contract=off", *(extra_nvcc or []), "-c", str(cu), "-o", str(obj)]
         jobs.append((obj, [cu, *headers], cmd))
     for cpp in sorted(CSRC.glob("*.cpp")):
