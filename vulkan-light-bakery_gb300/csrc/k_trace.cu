@@ -539,11 +539,14 @@ static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
 // together from a global ray counter (one atomic per refill, when half the
 // warp or all of it is idle), so a warp no longer waits for its slowest ray
 // and primary and shadow walks of different rays overlap.  Ray r is
-// (direction position t = r / P, probe slot r % P) with P the probe count
-// rounded up to 32: rays fetched together share a direction and are
-// Morton neighbours.  Box tests take the per-lane octant at run time; the
-// tests, the pruning and the tie rule are those of lane_traverse, so each
-// ray's result is unchanged.
+// (probe slot r / S, direction position r % S): rays fetched together share
+// their origin and take neighbouring directions of the trace order (grouped
+// by octant, then by position on the octant's face), so their walks share
+// the nodes around the probe (5 % faster than rays of one direction from
+// Morton-neighbour probes on a 16^3 grid, 19 % on random probes); slots run
+// to the probe count rounded up to 32.  Box tests take the per-lane octant
+// at run time; the tests, the pruning and the tie rule are those of
+// lane_traverse, so each ray's result is unchanged.
 __device__ __forceinline__ bool slab_rt(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
                                         float tmin, float tmax, float* tnear) {
   const float ax = fmaf(lx, r.ix, -r.oix), bx = fmaf(hx, r.ix, -r.oix);
@@ -745,7 +748,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
       if (!L.has) {
         const uint32_t r = base + __popc(idle & lane_lt_mask());
         if (r < R) {
-          const uint32_t t = r / P, sl = r - t * P;
+          const uint32_t sl = r / a.S, t = r - sl * a.S;
           if (sl < a.nprobes) lr_start(a, L, a.order[sl], __ldg(a.dir_order + t));
         }
       }
@@ -1190,7 +1193,7 @@ __device__ __forceinline__ void batch_emit(const BakeJobDev& j, uint32_t p, uint
 
 // Batched bake.  Job j owns the rays [ray_begin, ray_begin + P*S) of one
 // numbering over all jobs (P: its probe count rounded up to 32; ray r of a job
-// is direction position r / P, probe slot r % P), each job's range rounded up
+// is probe slot r / S, direction position r % S), each job's range rounded up
 // to whole chunks of 32 * chunk_lanes rays.  A warp takes a chunk from the
 // counter (one atomic), finds its job by binary search over the ranges, and
 // hands the chunk's rays to whichever lanes are idle; every lane runs its rays
@@ -1227,7 +1230,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
         const uint32_t r = r0 + __popc(idle & lane_lt_mask());
         r0 = min(r1, r0 + uint32_t(__popc(idle)));
         if (!L.has && r < r1) {
-          const uint32_t t = r / P, sl = r - t * P;
+          const uint32_t sl = r / j.S, t = r - sl * j.S;
           if (sl < j.nprobes) {
             const uint32_t p = j.order[sl];
             lr_start(j, L, p, __ldg(j.dir_order + t));

@@ -23,11 +23,6 @@ namespace {
 
 constexpr double kPiRef = 3.1415926538;  // shaders/sh_common.h:1
 constexpr double kPi = 3.141592653589793;
-// Packet traversal pays off only for dense probe sets: at least this many
-// probes and at most one triangle per probe (measured on box scenes of
-// 200 to 200k triangles with 64 to 32k probes; elsewhere lane mode is up to
-// 6.5x faster, here packets are up to 1.7x faster).
-constexpr uint32_t kPacketMinProbes = 16384;
 
 vlb_status fail(vlb_ctx* ctx, vlb_status s, const char* fmt, ...) {
   if (ctx) {
@@ -230,8 +225,10 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
   VLB_CUDA(ctx, cudaMemcpy(d->d_dirs, d4.data(), d4.size() * 4, cudaMemcpyHostToDevice));
   VLB_CUDA(ctx, cudaMemcpy(d->d_basis16, d->h_basis32.data(), d->h_basis32.size() * 4, cudaMemcpyHostToDevice));
   // trace order: directions grouped by ray octant (sign of 1/d per axis, as
-  // the traversal sees it), stable; warps in flight then share one traversal
-  // variant.  Outputs stay indexed by the caller's direction order.
+  // the traversal sees it; warps in flight then share one traversal variant),
+  // within an octant by a Morton code of the position on the octant's face
+  // (|x|, |y| over |x| + |y| + |z|), so neighbouring positions are close
+  // directions.  Outputs stay indexed by the caller's direction order.
   std::vector<uint32_t> order(n);
   auto oct = [&](uint32_t s) {
     int o = 0;
@@ -242,8 +239,19 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
     }
     return o;
   };
-  for (uint32_t s = 0; s < n; ++s) order[s] = s;
-  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return oct(x) < oct(y); });
+  auto key = [&](uint32_t s) {
+    const float ax = std::fabs(d->h_dirs[3 * s]), ay = std::fabs(d->h_dirs[3 * s + 1]),
+                az = std::fabs(d->h_dirs[3 * s + 2]);
+    const float l1 = ax + ay + az;
+    const uint32_t u = l1 > 0.f ? uint32_t(std::min(1023.f, ax / l1 * 1023.f)) : 0u;
+    const uint32_t v = l1 > 0.f ? uint32_t(std::min(1023.f, ay / l1 * 1023.f)) : 0u;
+    uint32_t m = 0;
+    for (int b = 0; b < 10; ++b) m |= (((u >> b) & 1u) << (2 * b)) | (((v >> b) & 1u) << (2 * b + 1));
+    return (uint64_t(oct(s)) << 32) | m;
+  };
+  std::vector<uint64_t> keys(n);
+  for (uint32_t s = 0; s < n; ++s) { order[s] = s; keys[s] = key(s); }
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return keys[x] < keys[y]; });
   VLB_CUDA(ctx, cudaMalloc(&d->d_order, size_t(n) * 4));
   VLB_CUDA(ctx, cudaMemcpy(d->d_order, order.data(), size_t(n) * 4, cudaMemcpyHostToDevice));
   // BF16 basis for the tensor-core projection, transposed [32][pitch]: row k
@@ -852,13 +860,14 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
 
 // Common part of a bake launch: validated parameters -> trace arguments,
 // probes staged on the device and sorted into spatially compact packets.
-// Traversal mode of one bake: forced by the flags, else packets for dense
-// probe sets (neighbouring probes share most of their paths) and lane mode
-// otherwise (packets of sparse probes walk long union paths).
-static uint32_t lane_mode(const vlb_scene* scene, uint32_t nprobes, uint32_t flags) {
-  if (flags & VLB_BAKE_TRAVERSAL_LANE) return 1;
-  if (flags & VLB_BAKE_TRAVERSAL_PACKET) return 0;
-  return nprobes >= kPacketMinProbes && scene->ntris <= nprobes ? 0 : 1;
+// Traversal mode of one bake: packets only when the flag asks for them.  The
+// lane walk (per-lane state machines, rays of one probe fetched together)
+// is faster on every box scene measured, 200 to 200k triangles with 64 to
+// 32k probes (1.04x on 32k probes in 200 triangles to 8.6x on 64 probes in
+// 200k triangles; 262,144 grid probes x 1024 directions in 49k triangles:
+// 179 ms against 242 ms).
+static uint32_t lane_mode(const vlb_scene*, uint32_t, uint32_t flags) {
+  return (flags & VLB_BAKE_TRAVERSAL_PACKET) && !(flags & VLB_BAKE_TRAVERSAL_LANE) ? 0 : 1;
 }
 
 // Grid mode (per-direction triangle grids) runs when the grid flag asks for
@@ -977,10 +986,11 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     a.shadow = static_cast<uint8_t*>(os.dev);
     a.dbg_radiance = static_cast<float*>(orad.dev);
   }
-  // VLB_PREC_FUSED runs the one-kernel schedule when every packet's directions
-  // fit at most two work items (large probe counts); smaller bakes are faster
-  // through the radiance tile, which then stays in L2.
-  bool fused = p->precision == VLB_PREC_FUSED && a.chunks <= 2 && !a.dbg_radiance && !a.grid_hdr;
+  // VLB_PREC_FUSED runs the one-kernel schedule for packet walks whose
+  // directions fit at most two work items per packet (large probe counts);
+  // lane walks (the default) and smaller bakes are faster through the
+  // radiance tile, which then stays in L2.
+  bool fused = p->precision == VLB_PREC_FUSED && !a.lane && a.chunks <= 2 && !a.dbg_radiance && !a.grid_hdr;
   if (p->precision == VLB_PREC_FUSED && (p->flags & VLB_BAKE_FORCE_FUSED_KERNEL)) {
     if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "the fused kernel keeps no per-ray radiance");
     fused = true;
