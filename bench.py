@@ -84,6 +84,25 @@ def workload_inputs():
     return pos, idx, alb, sky, sun, probes
 
 
+def cpu_model() -> str:
+    """The host CPU's model line from /proc/cpuinfo (x86 "model name", Arm
+    "CPU implementer/part"), else the machine type."""
+    import platform
+
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return platform.machine()
+    for ln in info:
+        if ln.lower().startswith("model name"):
+            return ln.split(":", 1)[1].strip()
+    impl = [ln.split(":", 1)[1].strip() for ln in info if ln.startswith("CPU implementer")]
+    part = [ln.split(":", 1)[1].strip() for ln in info if ln.startswith("CPU part")]
+    if impl and part:
+        return f"{platform.machine()} implementer {impl[0]} part {part[0]}"
+    return platform.machine()
+
+
 def cpu_time_oracle(pos, idx, alb, sky, sun, probes, nthreads):
     """Times the FP64 CPU restatement (the oracle) on all host threads."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -186,7 +205,8 @@ def run_reference(args, rank: int):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "probes_per_step": len(sample), "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": pps, "unit": "probes/s", "cores": nthreads, "kind": "port",
-                         "sample": f"first {len(sample)} of {len(probes)} probes, {NDIRS} dirs each, per step"},
+                         "sample": f"first {len(sample)} of {len(probes)} probes, {NDIRS} dirs each, per step",
+                         "cpu": cpu_model()},
         "e2e": {"value": pps, "unit": "probes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference bake needs Vulkan ray tracing (unavailable on this box); its math runs here as "
                 "the FP64 multithreaded CPU restatement",
@@ -362,7 +382,8 @@ def main():
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
         "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)} for k, v in prof.items()},
         "cpu_baseline": {"value": len(sample) / cpu_dt, "unit": "probes/s", "cores": os.cpu_count() or 1,
-                         "kind": "port", "sample": f"first {len(sample)} of {P} probes, {NDIRS} dirs each"},
+                         "kind": "port", "sample": f"first {len(sample)} of {P} probes, {NDIRS} dirs each",
+                         "cpu": cpu_model()},
         "clocks": clk,
         "skybox_c0": skybox_measure(ctx, torch, stream, args.steps, hbm_peak),
         "projection_c2": projection_measure(ctx, torch, stream, args.steps, hbm_peak),
@@ -536,7 +557,13 @@ def bake_c2_measure(ctx, torch, stream, steps, hbm_peak, sample=64):
     sel = np.linspace(0, P - 1, sample).astype(int)
     d32, w = O.dirs_fibonacci(1024)
     B = O.basis_matrix(d32.astype(np.float64), w, LMAX)
-    ref = O.Scene(pos, idx, alb).bake(probes[sel], d32, B, sun, sky=sky, sky_n=SKY_N)
+    orc = O.Scene(pos, idx, alb)
+    t0 = time.perf_counter()
+    ref = orc.bake(probes[sel], d32, B, sun, sky=sky, sky_n=SKY_N)
+    cpu_s = time.perf_counter() - t0
+    res["cpu_oracle"] = {"probes_per_s": sample / cpu_s, "threads": os.cpu_count() or 1, "cpu": cpu_model(),
+                         "sample": f"{sample} evenly spread probes x 1024 dirs ({cpu_s:.2f} s)",
+                         "full_bake_s": cpu_s * P / sample, "label": "extrapolated from the sample"}
     for name in outs:
         g = outs[name][sel].astype(np.float64)
         e = np.linalg.norm((g - ref).reshape(sample, -1), axis=1) / np.maximum(

@@ -8,9 +8,11 @@
  *
  * Memory: every array argument may be host memory (pageable or pinned) or
  * device memory of the context's GPU; the library inspects each pointer.
- * A call whose outputs are all device pointers is asynchronous on the
- * context's stream; a call with a host output returns after the result is in
- * host memory.  Input and output arrays are never retained after a call.
+ * A call whose arrays are all device pointers is asynchronous on the
+ * context's stream: those arrays must stay valid until the stream passes the
+ * call (vlb_ctx_synchronize, or an event the caller records on the stream).
+ * A call with a host array returns after every host input has been read and
+ * every host output written.  Nothing is retained beyond that.
  * A context is externally synchronised: one thread at a time, and calls on
  * one context run in stream order.
  */
