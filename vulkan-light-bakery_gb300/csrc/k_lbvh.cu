@@ -371,7 +371,8 @@ __device__ __forceinline__ void probe_sort_count(const float* __restrict__ probe
 
 __global__ void __launch_bounds__(1024) k_probe_order_count(const float* __restrict__ probes, uint32_t n, float lox,
                                                              float loy, float loz, float sx, float sy, float sz,
-                                                             uint32_t* __restrict__ order) {
+                                                             uint32_t* __restrict__ order, uint32_t* zero_word) {
+  if (threadIdx.x == 0 && zero_word) *zero_word = 0;  // the next kernel's work counter
   probe_sort_count(probes, n, lox, loy, loz, sx, sy, sz, order);
 }
 
@@ -404,8 +405,11 @@ size_t probe_order_scratch_bytes(uint32_t n) {
 }
 
 int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
-                       cudaStream_t st) {
-  if (n == 0) return 0;
+                       uint32_t* zero_word, cudaStream_t st) {
+  if (n == 0) {
+    if (zero_word) cudaMemsetAsync(zero_word, 0, 4, st);
+    return 0;
+  }
   const size_t a = (size_t(n) * 4 + 255) / 256 * 256;
   char* base = static_cast<char*>(scratch);
   uint32_t* ka = reinterpret_cast<uint32_t*>(base);
@@ -418,9 +422,11 @@ int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], u
     s[i] = e > 0.f ? 256.0f / e : 0.f;
   }
   if (n <= kCountMax) {
-    k_probe_order_count<<<1, 1024, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], order);
+    k_probe_order_count<<<1, 1024, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], order,
+                                            zero_word);
     return 1;
   }
+  if (zero_word) cudaMemsetAsync(zero_word, 0, 4, st);
   k_probe_codes<<<(n + 255) / 256, 256, 0, st>>>(probes, n, bounds[0], bounds[1], bounds[2], s[0], s[1], s[2], ka,
                                                  order);
   uint32_t *kin = ka, *vin = order, *kout = kb, *vout = vb;

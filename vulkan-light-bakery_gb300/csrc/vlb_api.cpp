@@ -911,16 +911,18 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   if (!probe_xyz) return fail(ctx, VLB_ERR_INVALID, "null probes");
   const void* dprobes;
   if ((st = stage_in(ctx, probe_xyz, size_t(nprobes) * 12, "probes_in", &dprobes))) return st;
-  void *order, *oscr;
+  void *order, *oscr, *wc;
   if ((st = scratch(ctx, "probe_order", size_t(nprobes) * 4, &order)) ||
-      (st = scratch(ctx, "probe_order_tmp", vlbk::probe_order_scratch_bytes(nprobes), &oscr)))
+      (st = scratch(ctx, "probe_order_tmp", vlbk::probe_order_scratch_bytes(nprobes), &oscr)) ||
+      (st = scratch(ctx, "trace_work", 256, &wc)))
     return st;
   {
     float b[6];
     for (int a = 0; a < 6; ++a) b[a] = scene->bounds[a];
     KScope k(ctx, "probe_order", 0);
     k.nkernels = vlbk::launch_probe_order(static_cast<const float*>(dprobes), nprobes, b,
-                                          static_cast<uint32_t*>(order), oscr, ctx->stream);
+                                          static_cast<uint32_t*>(order), oscr, static_cast<uint32_t*>(wc),
+                                          ctx->stream);
   }
   vlbk::TraceArgs& a = *out;
   a = vlbk::TraceArgs{};
@@ -957,10 +959,7 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
     vlbk::launch_grid_build(a, ctx->stream);
   }
   vlbk::plan_trace(a, ctx->num_sms, p->precision == VLB_PREC_FUSED);
-  void* wc;
-  if ((st = scratch(ctx, "trace_work", 256, &wc))) return st;
-  VLB_CUDA(ctx, cudaMemsetAsync(wc, 0, 4, ctx->stream));
-  a.work_counter = static_cast<uint32_t*>(wc);
+  a.work_counter = static_cast<uint32_t*>(wc);  // zeroed by the probe-order launch
   return VLB_OK;
 }
 

@@ -108,11 +108,12 @@ size_t ploc_scratch_bytes(uint32_t ntris);
 int launch_ploc_build(const float* leaf_box, uint32_t n, float4* nodes, void* scratch, cudaStream_t s,
                       int* launches);
 // Permutation of the probes by 24-bit Morton code inside `bounds` (min xyz,
-// max xyz), so that each 32-probe packet is spatially compact.  Returns the
-// number of kernels launched.
+// max xyz), so that each 32-probe packet is spatially compact; also zeroes
+// *zero_word (the trace's work counter; may be null) in stream order.
+// Returns the number of kernels launched.
 size_t probe_order_scratch_bytes(uint32_t n);
 int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], uint32_t* order, void* scratch,
-                       cudaStream_t s);
+                       uint32_t* zero_word, cudaStream_t s);
 
 // ---- trace + shade --------------------------------------------------------------
 struct TraceArgs {
