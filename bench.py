@@ -173,16 +173,35 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def load_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def load_profile_figure(name: str, kernel: str):
+    """A per-launch figure `name[kernel]: value` from the committed ncu summaries, if any."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for ln in f.read_text().splitlines():
-            if ln.startswith(f"traffic_bytes_per_launch[{kernel}]:"):
+            if ln.startswith(f"{name}[{kernel}]:"):
                 try:
                     return float(ln.split(":", 1)[1].split()[0])
                 except ValueError:
                     pass
     return None
+
+
+def load_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    return load_profile_figure("traffic_bytes_per_launch", kernel)
+
+
+def issue_roofline(torch, kernel: str, avg_ms: float, clk: dict):
+    """The trace kernel's real bound: warp instructions issued per second (the
+    per-launch count from the committed ncu summary over the live launch time)
+    against the SM issue peak (SMs x 4 schedulers x the maximum SM clock)."""
+    inst = load_profile_figure("warp_instructions_per_launch", kernel)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clk.get("sm_max_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6
+    achieved = inst / (avg_ms * 1e-3) if inst and avg_ms > 0 else None
+    return {"unit": "warp instructions/s", "achieved": achieved, "peak": peak,
+            "frac": achieved / peak if achieved else None, "warp_instructions_per_launch": inst,
+            "peak_source": f"{sms} SMs x 4 issue slots x {mhz:.0f} MHz"}
 
 
 def run_reference(args, rank: int):
@@ -379,7 +398,8 @@ def main():
                              "by nature",
                      "node_tests_per_ray": stats["node_tests_per_ray"],
                      "node_fetches_per_ray": stats["node_fetches_per_ray"],
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                     "issue": issue_roofline(torch, kname, k_avg_ms, clk)},
         "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)} for k, v in prof.items()},
         "cpu_baseline": {"value": len(sample) / cpu_dt, "unit": "probes/s", "cores": os.cpu_count() or 1,
                          "kind": "port", "sample": f"first {len(sample)} of {P} probes, {NDIRS} dirs each",
