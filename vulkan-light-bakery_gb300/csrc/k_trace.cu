@@ -87,6 +87,14 @@ __device__ __forceinline__ void make_ray(RayCtx& r, float ox, float oy, float oz
   r.oix = ox * r.ix; r.oiy = oy * r.iy; r.oiz = oz * r.iz;
 }
 
+// make_ray with the reciprocals of d precomputed (host_safe_inv: the same bits).
+__device__ __forceinline__ void make_ray_inv(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz,
+                                             float ix, float iy, float iz) {
+  r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
+  r.ix = ix; r.iy = iy; r.iz = iz;
+  r.oix = ox * ix; r.oiy = oy * iy; r.oiz = oz * iz;
+}
+
 // Slab test for a ray in octant OCT (bit a set: 1/d_a < 0).  The octant is
 // the same for every lane of a packet (one direction per packet), so the
 // entry and exit planes of each axis are chosen at compile time and no
@@ -587,7 +595,8 @@ __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uin
   L.ox = a.probes[3 * size_t(p)];
   L.oy = a.probes[3 * size_t(p) + 1];
   L.oz = a.probes[3 * size_t(p) + 2];
-  make_ray(L.ray, L.ox, L.oy, L.oz, L.d.x, L.d.y, L.d.z);
+  const float4 inv = __ldg(a.dinv + s);
+  make_ray_inv(L.ray, L.ox, L.oy, L.oz, L.d.x, L.d.y, L.d.z, inv.x, inv.y, inv.z);
   L.has = true;
   L.shadow = false;
   L.cur = a.ntris > 1 ? 0 : ~0;
@@ -623,8 +632,9 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
     const float ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
     if (!(ndl > 0.f)) return true;
     if constexpr (COUNT) ++w.shadow;
-    make_ray(L.ray, fmaf(L.tb, L.d.x, L.ox) + a.bias * nx, fmaf(L.tb, L.d.y, L.oy) + a.bias * ny,
-             fmaf(L.tb, L.d.z, L.oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z);
+    make_ray_inv(L.ray, fmaf(L.tb, L.d.x, L.ox) + a.bias * nx, fmaf(L.tb, L.d.y, L.oy) + a.bias * ny,
+                 fmaf(L.tb, L.d.z, L.oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z, a.sun_inv.x, a.sun_inv.y,
+                 a.sun_inv.z);
     L.lit = a.sun_scale * ndl;
     L.shadow = true;
     L.cur = a.ntris > 1 ? 0 : ~0;

@@ -217,12 +217,17 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
       d->h_basis32[size_t(s) * 16 + k] = float(w[s] * Y[k]);
     }
   }
-  std::vector<float> d4(size_t(n) * 4, 0.f);
+  std::vector<float> d4(size_t(n) * 4, 0.f), i4(size_t(n) * 4, 0.f);
   for (uint32_t s = 0; s < n; ++s)
-    for (int a = 0; a < 3; ++a) d4[4 * s + a] = d->h_dirs[3 * s + a];
+    for (int a = 0; a < 3; ++a) {
+      d4[4 * s + a] = d->h_dirs[3 * s + a];
+      i4[4 * s + a] = vlbk::host_safe_inv(d->h_dirs[3 * s + a]);
+    }
   VLB_CUDA(ctx, cudaMalloc(&d->d_dirs, size_t(n) * sizeof(float4)));
+  VLB_CUDA(ctx, cudaMalloc(&d->d_dinv, size_t(n) * sizeof(float4)));
   VLB_CUDA(ctx, cudaMalloc(&d->d_basis16, size_t(n) * 16 * sizeof(float)));
   VLB_CUDA(ctx, cudaMemcpy(d->d_dirs, d4.data(), d4.size() * 4, cudaMemcpyHostToDevice));
+  VLB_CUDA(ctx, cudaMemcpy(d->d_dinv, i4.data(), i4.size() * 4, cudaMemcpyHostToDevice));
   VLB_CUDA(ctx, cudaMemcpy(d->d_basis16, d->h_basis32.data(), d->h_basis32.size() * 4, cudaMemcpyHostToDevice));
   // trace order: directions grouped by ray octant (sign of 1/d per axis, as
   // the traversal sees it; warps in flight then share one traversal variant),
@@ -683,6 +688,7 @@ void vlb_dirset_destroy(vlb_dirset* d) {
   if (!d) return;
   if (d->ctx) { cudaSetDevice(d->ctx->device); cudaStreamSynchronize(d->ctx->stream); }
   cudaFree(d->d_dirs);
+  cudaFree(d->d_dinv);
   cudaFree(d->d_basis16);
   cudaFree(d->d_order);
   cudaFree(d->d_bt);
@@ -931,6 +937,8 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a.order = static_cast<const uint32_t*>(order);
   a.dirs = p->dirs->d_dirs; a.dir_order = p->dirs->d_order; a.S = p->dirs->n;
   a.sun = make_float3(float(p->sun_dir[0] / sl), float(p->sun_dir[1] / sl), float(p->sun_dir[2] / sl));
+  a.sun_inv = make_float3(vlbk::host_safe_inv(a.sun.x), vlbk::host_safe_inv(a.sun.y), vlbk::host_safe_inv(a.sun.z));
+  a.dinv = p->dirs->d_dinv;
   a.sun_scale = float(double(p->sun_intensity) / kPi);
   a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
   a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
@@ -1267,6 +1275,8 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     d.tmin = p->tmin; d.tmax = p->tmax; d.bias = p->shadow_bias;
     d.sun = make_float3(float(p->sun_dir[0] / b.sun_len), float(p->sun_dir[1] / b.sun_len),
                         float(p->sun_dir[2] / b.sun_len));
+    d.sun_inv =
+        make_float3(vlbk::host_safe_inv(d.sun.x), vlbk::host_safe_inv(d.sun.y), vlbk::host_safe_inv(d.sun.z));
     d.sun_scale = float(double(p->sun_intensity) / kPi);
     d.sky = p->sky ? p->sky->d_texels : nullptr; d.sky_n = p->sky ? p->sky->n : 0;
     d.err = ctx->d_err;
@@ -1281,7 +1291,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     }
     d.order = bb.order + b.row0;
     d.nprobes = b.nprobes;
-    d.dirs = p->dirs->d_dirs; d.dir_order = p->dirs->d_order; d.S = b.S;
+    d.dirs = p->dirs->d_dirs; d.dinv = p->dirs->d_dinv; d.dir_order = p->dirs->d_order; d.S = b.S;
     uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
     if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
     else d.radiance = reinterpret_cast<float*>(rad);

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -125,9 +126,11 @@ struct TraceArgs {
   const uint32_t* order;  // device permutation: packet slot -> probe index
   uint32_t nprobes;
   const float4* dirs;     // device S (xyz), caller order
+  const float4* dinv;     // device S: per-axis reciprocals of dirs (zero components nudged to 1e-30)
   const uint32_t* dir_order;  // device S: trace position -> direction index (grouped by octant)
   uint32_t S;
   float3 sun;             // unit
+  float3 sun_inv;         // per-axis reciprocals of sun, as dinv
   float sun_scale;        // intensity / pi
   float tmin, tmax, bias;
   const float* sky;       // device cubemap or null
@@ -169,6 +172,9 @@ size_t grid_build_smem(uint32_t G, uint32_t ntris);
 bool grid_supported(uint32_t ntris, uint32_t nprobes, uint32_t S);
 void launch_grid_build(const TraceArgs& a, cudaStream_t s);
 constexpr int kTraceWarps = 4;
+// 1/d with zero components nudged to +-1e-30, the reciprocal every ray setup
+// uses: one IEEE FP32 division, so host and device give the same bits.
+inline float host_safe_inv(float d) { return 1.0f / (std::fabs(d) > 1e-30f ? d : std::copysign(1e-30f, d)); }
 // Chooses dirs_per_warp / chunks for nprobes x S rays on num_sms SMs: fine
 // items for load balance, coarser in fused mode where each item leaves a
 // K x 3 partial per probe.
@@ -187,6 +193,7 @@ struct BakeJobDev {
   uint32_t ntris;
   float tmin, tmax, bias;
   float3 sun;
+  float3 sun_inv;
   float sun_scale;
   const float* sky;
   uint32_t sky_n;
@@ -196,6 +203,7 @@ struct BakeJobDev {
   uint32_t* order;        // device nprobes: packet slot -> probe (written by the batched sort)
   uint32_t nprobes;
   const float4* dirs;
+  const float4* dinv;
   const uint32_t* dir_order;
   uint32_t S;
   // this job's rows of its direction set's radiance tile
@@ -317,6 +325,7 @@ struct vlb_dirset {
   vlb_ctx* ctx = nullptr;
   uint32_t n = 0;
   float4* d_dirs = nullptr;     // n trace directions
+  float4* d_dinv = nullptr;     // n per-axis reciprocals of the trace directions (vlbk::host_safe_inv)
   uint32_t* d_order = nullptr;  // n direction indices sorted by ray octant (stable)
   uint16_t* d_bt = nullptr;     // [32][bt_pitch] BF16 weighted basis, high rows 0..15, low rows 16..31
   uint32_t bt_pitch = 0;
