@@ -1095,8 +1095,9 @@ constexpr int kGridSteps = 8;  // entry steps per turn
 
 // Persistent warps; each lane runs its rays through a small state machine --
 // primary cell walk, shading, shadow cell walk, tile entries -- and idle
-// lanes refill together from the ray counter (as k_trace_dyn): rays fetched
-// together share a direction and are Morton neighbours.
+// lanes refill together from the ray counter (as k_trace_dyn, but numbered
+// direction-major: rays fetched together share a direction, hence a grid, and
+// are Morton-neighbour probes).
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_grid(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
