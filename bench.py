@@ -99,7 +99,9 @@ def cpu_model() -> str:
     impl = [ln.split(":", 1)[1].strip() for ln in info if ln.startswith("CPU implementer")]
     part = [ln.split(":", 1)[1].strip() for ln in info if ln.startswith("CPU part")]
     if impl and part:
-        return f"{platform.machine()} implementer {impl[0]} part {part[0]}"
+        arm = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd0c": "Neoverse-N1", "0xd49": "Neoverse-N2"}
+        name = arm.get(part[0].lower()) if impl[0].lower() == "0x41" else None
+        return f"{platform.machine()} {name}" if name else f"{platform.machine()} implementer {impl[0]} part {part[0]}"
     return platform.machine()
 
 
