@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-probes", type=int, default=1024, help="probes in the CPU baseline sample")
-    ap.add_argument("--only", choices=["bake", "skybox", "projection", "bake_c2", "batch", "service"], default=None,
+    ap.add_argument("--only", choices=["bake", "skybox", "projection", "bake_c2", "batch", "service", "refbake"],
+                    default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     return ap.parse_args()
 
@@ -264,7 +265,8 @@ def main():
     if args.only:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         fn = {"bake": bake_measure, "skybox": skybox_measure, "projection": projection_measure,
-              "bake_c2": bake_c2_measure, "batch": batch_measure, "service": service_measure}[args.only]
+              "bake_c2": bake_c2_measure, "batch": batch_measure, "service": service_measure,
+              "refbake": refbake_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, peaks.get("hbm_gbs", 6800.0))), flush=True)
         return 0
     pos, idx, alb, sky, sun, probes = workload_inputs()
@@ -412,6 +414,7 @@ def main():
         "bake_c2": bake_c2_measure(ctx, torch, stream, args.steps, hbm_peak),
         "batch_c3": batch_measure(ctx, torch, stream, args.steps, hbm_peak),
         "service_c4": service_measure(ctx, torch, stream, args.steps, hbm_peak),
+        "reference_bake": refbake_measure(ctx, torch, stream, args.steps, hbm_peak),
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -615,6 +618,41 @@ def batch_volumes(seed=SEED, nvol=256):
         probes = (lo + rng.random((int(nprobes[i]), 3)) * (hi - lo)).astype(np.float32)
         vols.append((pos, idx, alb, probes, int(rays[i]), vlb.synth_sun(seed * 104729 + i)))
     return vols
+
+
+def refbake_measure(ctx, torch, stream, steps, hbm_peak, reps=3):
+    """The reference baker's own workload on the config-1 scene: a 7^3 probe grid
+    over the origin-inclusive bounds in the reference's order, one ray per pixel
+    of the 3141 x 1000 equirect env map (3,141,000 rays per probe, 1.08e9 in
+    all), L3 (16 coefficients), FP32 and BF16 + tcgen05; device-resident
+    probes and output, L2 flushed before each bake."""
+    import vlb
+
+    pos, idx, alb, sky, sun, _ = workload_inputs()
+    scene = ctx.scene(pos, idx, alb)
+    probes, _ = vlb.probe_grid_ref_order(scene.bounds(include_origin=True), (7, 7, 7))
+    P, W, H = probes.shape[0], 3141, 1000
+    ds = ctx.equirect(W, H)
+    skyh = ctx.sky(sky, SKY_N)
+    d_probes = torch.from_numpy(probes).cuda()
+    out = torch.empty((P, 16, 3), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    res = {"workload": f"{P} probes (7^3 reference grid) x {W}x{H} equirect rays, config-1 scene, L3",
+           "primary_rays": P * W * H}
+    for name, prec in (("fp32", vlb.PREC_FUSED), ("mixed_bf16_tcgen05", vlb.PREC_MIXED)):
+        p = vlb.bake_params(ds, 3, prec, sun, sky=skyh)
+        ctx.bake(scene, d_probes, p, out=out)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        torch.cuda.synchronize()
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            ctx.bake(scene, d_probes, p, out=out)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = sorted(a.elapsed_time(b) for a, b in evs)[len(evs) // 2]
+        res[name] = {"ms": ms, "grays_per_s": P * W * H / (ms / 1e3) / 1e9}
+    return res
 
 
 def batch_measure(ctx, torch, stream, steps, hbm_peak):

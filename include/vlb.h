@@ -241,6 +241,15 @@ vlb_status vlb_bake(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz
                     const vlb_bake_params* params, float* out);
 vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
                        const vlb_bake_params* params, float* out, const vlb_bake_debug* debug);
+/* The asynchronous form of vlb_bake: probe_xyz and out must be device memory
+ * of the context's GPU (VLB_ERR_INVALID otherwise).  The call enqueues the
+ * bake on the context's stream and returns; done_event (a cudaEvent_t the
+ * caller created, may be NULL) is recorded after the bake's last kernel.  The
+ * arrays must stay valid until that event completes.  Device-side checks
+ * (e.g. a traversal stack overflow) surface at the next synchronising call
+ * on the context (vlb_ctx_synchronize). */
+vlb_status vlb_bake_async(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                          const vlb_bake_params* params, float* out, void* done_event);
 /* Measurement aid (no reference counterpart; the reference's traversal is
  * inside the driver): one instrumented bake of the same rays, counting
  * out[0] primary rays, out[1] shadow rays, out[2] BVH node fetches (64 B

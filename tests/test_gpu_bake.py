@@ -239,6 +239,34 @@ def test_device_resident_probes_and_output(ctx):
     assert np.array_equal(out.cpu().numpy(), host)
 
 
+def test_bake_async_on_caller_stream(ctx):
+    """vlb_bake_async on a caller-owned stream: returns before the bake is
+    done, records the caller's event after it, gives vlb_bake's result; host
+    arrays are refused."""
+    torch = pytest.importorskip("torch")
+    pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=10, counts=(8, 8, 8))
+    scene = ctx.scene(pos, idx, alb)
+    p = vlb.bake_params(ctx.fibonacci(S), 3, vlb.PREC_FP32, sun, sky=ctx.sky(sky, 128))
+    want = ctx.bake(scene, probes, p)
+    stream = torch.cuda.Stream()
+    done = torch.cuda.Event()
+    done.record(stream)  # creates the event
+    d_probes = torch.from_numpy(probes).cuda()
+    out = torch.zeros((probes.shape[0], 16, 3), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.set_stream(stream.cuda_stream)
+    try:
+        ctx.bake_async(scene, d_probes, p, out, done)
+        done.synchronize()
+        assert np.array_equal(out.cpu().numpy(), want)
+        with pytest.raises(vlb.VlbError) as e:
+            ctx.bake_async(scene, probes, p, out, done)
+        assert e.value.status == vlb.ERR_INVALID
+        ctx.synchronize()
+    finally:
+        ctx.set_stream(None)
+
+
 def test_invalid_params(ctx):
     pos, idx, alb = vlb.synth_box_scene(1, 2)
     scene = ctx.scene(pos, idx, alb)

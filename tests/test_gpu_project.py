@@ -39,8 +39,10 @@ def test_xzy_frame(ctx):
 
 
 @pytest.mark.parametrize("lmax", [2, 3])
-@pytest.mark.parametrize("nprobes,S", [(1, 64), (37, 256), (700, 1024), (5, 100)])
+@pytest.mark.parametrize("nprobes,S", [(1, 64), (37, 256), (700, 1024), (5, 100), (5, 65536), (343, 20000)])
 def test_project_f32_matches_oracle(ctx, lmax, nprobes, S):
+    """Includes tiles of few rows and many samples, projected in sample splits
+    (ragged last split) whose partials are added in FP64."""
     ds = ctx.fibonacci(S)
     d, w = O.dirs_fibonacci(S)
     B = O.basis_matrix(d.astype(np.float64), w, lmax)
@@ -61,6 +63,22 @@ def test_project_bf16_matches_oracle_on_rounded_input(ctx):
     rad = torch.from_numpy(rng.random((n, 3, S)).astype(np.float32) * 5).to(torch.bfloat16)
     bits = rad.view(torch.int16).numpy().copy()
     got = ctx.project(bits, n, ds, 2, dtype=vlb.DTYPE_BF16)
+    ref = O.project(rad.float().numpy(), n, S, B)
+    assert rel(got, ref) < 1e-5
+
+
+def test_project_bf16_split_simt_matches_oracle(ctx):
+    """BF16 tile whose sample count rules out the tensor-core kernel (not a
+    multiple of 8), few rows: the CUDA-core kernel in sample splits."""
+    torch = pytest.importorskip("torch")
+    S, n = 30001, 7
+    ds = ctx.fibonacci(S)
+    d, w = O.dirs_fibonacci(S)
+    B = O.basis_matrix(d.astype(np.float64), w, 3)
+    rng = np.random.default_rng(5)
+    rad = torch.from_numpy(rng.random((n, 3, S)).astype(np.float32) * 5).to(torch.bfloat16)
+    bits = rad.view(torch.int16).numpy().copy()
+    got = ctx.project(bits, n, ds, 3, dtype=vlb.DTYPE_BF16)
     ref = O.project(rad.float().numpy(), n, S, B)
     assert rel(got, ref) < 1e-5
 

@@ -13,6 +13,8 @@
 // launch shape or on other probes in the tile.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "vlb_device.cuh"
 #include "vlb_internal.h"
 
@@ -50,13 +52,13 @@ static_assert(kProjTileWords % 4 == 0, "basis block must stay 16-byte aligned");
 // through registers.  Coalesced: each warp loads 32 rows, 32-sample segments
 // per row.
 template <typename T>
-__device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_t rows, uint32_t S,
+__device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_t rows, uint32_t S, uint32_t s_end,
                                               const float* __restrict__ basis16, uint32_t row0, uint32_t s0,
                                               float* stage) {
   float(*tile)[kProjCols + 1] = reinterpret_cast<float(*)[kProjCols + 1]>(stage);
   float(*bas)[16] = reinterpret_cast<float(*)[16]>(stage + kProjTileWords);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t ns = min(uint32_t(kProjCols), S - s0);
+  const uint32_t ns = min(uint32_t(kProjCols), s_end - s0);
   if constexpr (sizeof(T) == 4) {
 #pragma unroll 8
     for (uint32_t rr = warp; rr < kProjRows; rr += kProjRows / 32) {
@@ -92,21 +94,50 @@ __device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+// Launch grid: row tiles x sample splits.  A tile of few rows and many
+// samples (the reference's 343 probes x 3.14 M samples: 9 row tiles) is split
+// along the samples so that about kProjSplitCtas CTAs run; each split sums its
+// range in FP32 in order and k_project_reduce adds the splits in FP64 in
+// split order.  The split count depends on the tile's shape only, so results
+// stay deterministic; tiles with enough rows (C1, C2) run unsplit, one
+// sequential FP32 sum per row.
+constexpr uint32_t kProjSplitCtas = 304;
+constexpr uint32_t kProjMinSplitSamples = 16 * kProjCols;
+
+static uint32_t project_splits(uint32_t rows, uint32_t S, uint32_t* per) {
+  const uint32_t tiles = (rows + kProjRows - 1) / kProjRows;
+  uint32_t splits = 1;
+  if (tiles && tiles < kProjSplitCtas)
+    splits = std::max(1u, std::min((kProjSplitCtas + tiles - 1) / tiles, S / kProjMinSplitSamples));
+  uint32_t p = (S + splits - 1) / splits;
+  p = (p + kProjCols - 1) / kProjCols * kProjCols;  // whole stages
+  *per = p;
+  return p ? (S + p - 1) / p : 1;
+}
+
+size_t project_partial_bytes(uint32_t nprobes, uint32_t S, uint32_t K) {
+  uint32_t per;
+  const uint32_t splits = project_splits(nprobes * 3, S, &per);
+  return splits > 1 ? size_t(splits) * nprobes * 3 * K * sizeof(float) : 0;
+}
+
 template <typename T, int K>
 __global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad, uint32_t rows, uint32_t S,
-                                                       const float* __restrict__ basis16, float* __restrict__ out) {
+                                                       uint32_t per, const float* __restrict__ basis16,
+                                                       float* __restrict__ out, float* __restrict__ partial) {
   __shared__ __align__(16) float stage[kProjStageWords];
   const float(*tile)[kProjCols + 1] = reinterpret_cast<const float(*)[kProjCols + 1]>(stage);
   const float(*bas)[16] = reinterpret_cast<const float(*)[16]>(stage + kProjTileWords);
   const uint32_t tid = threadIdx.x;
   const uint32_t row0 = blockIdx.x * kProjRows;
   const uint32_t row = row0 + tid;
+  const uint32_t s_begin = blockIdx.y * per, s_end = min(S, s_begin + per);
   float acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.f;
 
-  for (uint32_t s0 = 0; s0 < S; s0 += kProjCols) {
-    project_stage<T>(rad, rows, S, basis16, row0, s0, stage);
+  for (uint32_t s0 = s_begin; s0 < s_end; s0 += kProjCols) {
+    project_stage<T>(rad, rows, S, s_end, basis16, row0, s0, stage);
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 #pragma unroll 4
@@ -124,31 +155,52 @@ __global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad
     }
     __syncthreads();
   }
-  if (row < rows) {
+  if (row >= rows) return;
+  if (gridDim.y == 1) {
     const uint32_t p = row / 3, c = row - 3 * p;
 #pragma unroll
     for (int k = 0; k < K; ++k) out[(size_t(p) * K + k) * 3 + c] = acc[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < K; ++k) partial[(size_t(blockIdx.y) * rows + row) * K + k] = acc[k];
   }
+}
+
+// out (probe, k, channel) = the splits' partials of (row, k) added in FP64 in split order.
+__global__ void k_project_reduce(const float* __restrict__ partial, uint32_t splits, uint32_t rows, uint32_t K,
+                                 float* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * K) return;
+  const uint32_t row = i / K, k = i - row * K;
+  double sum = 0.0;
+  for (uint32_t y = 0; y < splits; ++y) sum += double(partial[(size_t(y) * rows + row) * K + k]);
+  const uint32_t p = row / 3, c = row - 3 * p;
+  out[(size_t(p) * K + k) * 3 + c] = float(sum);
 }
 
 template <typename T>
 static void launch_project(const T* rad, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K, float* out,
-                           cudaStream_t s) {
+                           float* partial, cudaStream_t s) {
   const uint32_t rows = nprobes * 3;
-  const uint32_t grid = (rows + kProjRows - 1) / kProjRows;
-  if (grid == 0) return;
-  if (K == 9) k_project<T, 9><<<grid, kProjRows, 0, s>>>(rad, rows, S, basis16, out);
-  else k_project<T, 16><<<grid, kProjRows, 0, s>>>(rad, rows, S, basis16, out);
+  const uint32_t tiles = (rows + kProjRows - 1) / kProjRows;
+  if (tiles == 0) return;
+  uint32_t per = 0;
+  const uint32_t splits = S ? project_splits(rows, S, &per) : 1;
+  if (!S) per = 0;
+  const dim3 grid(tiles, splits);
+  if (K == 9) k_project<T, 9><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial);
+  else k_project<T, 16><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial);
+  if (splits > 1) k_project_reduce<<<(rows * K + 255) / 256, 256, 0, s>>>(partial, splits, rows, K, out);
 }
 
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
-                        float* out, cudaStream_t s) {
-  launch_project<float>(radiance, nprobes, S, basis16, K, out, s);
+                        float* out, float* partial, cudaStream_t s) {
+  launch_project<float>(radiance, nprobes, S, basis16, K, out, partial, s);
 }
 
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
-                              uint32_t K, float* out, cudaStream_t s) {
-  launch_project<uint16_t>(radiance, nprobes, S, basis16, K, out, s);
+                              uint32_t K, float* out, float* partial, cudaStream_t s) {
+  launch_project<uint16_t>(radiance, nprobes, S, basis16, K, out, partial, s);
 }
 
 // sh_sum.comp:35-52 -- one thread per pixel, direction from the per-column

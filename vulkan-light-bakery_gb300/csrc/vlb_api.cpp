@@ -849,8 +849,10 @@ void vlb_bake_params_default(vlb_bake_params* p) {
 
 // BF16 tile projection: the tcgen05 kernel when the tile meets its alignment
 // (S a multiple of 8, 16-byte aligned), else the CUDA-core kernel.
+// `part_name`: the scratch for split partials (the batch path, whose launches
+// a CUDA graph may replay, keeps its own).
 static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprobes, const vlb_dirset* dirs,
-                               uint32_t K, float* out) {
+                               uint32_t K, float* out, const char* part_name = "project_partial") {
   const uint32_t S = dirs->n;
   if (vlbk::project_tc_supported(rad, S)) {
     KScope k(ctx, "project_tc");
@@ -859,8 +861,28 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
       return fail(ctx, VLB_ERR_CUDA, "tensor map encoding failed for the BF16 projection");
     return VLB_OK;
   }
-  KScope k(ctx, "project_bf16");
-  vlbk::launch_project_bf16_simt(rad, nprobes, S, dirs->d_basis16, K, out, ctx->stream);
+  void* part = nullptr;
+  const size_t pb = vlbk::project_partial_bytes(nprobes, S, K);
+  if (pb) {
+    vlb_status st = scratch(ctx, part_name, pb, &part);
+    if (st) return st;
+  }
+  KScope k(ctx, "project_bf16", pb ? 2 : 1);
+  vlbk::launch_project_bf16_simt(rad, nprobes, S, dirs->d_basis16, K, out, static_cast<float*>(part), ctx->stream);
+  return VLB_OK;
+}
+
+// FP32 tile projection (k_project; few-row tiles split along the samples).
+static vlb_status project_f32(vlb_ctx* ctx, const float* rad, uint32_t nprobes, const vlb_dirset* dirs, uint32_t K,
+                              float* out, const char* part_name = "project_partial") {
+  void* part = nullptr;
+  const size_t pb = vlbk::project_partial_bytes(nprobes, dirs->n, K);
+  if (pb) {
+    vlb_status st = scratch(ctx, part_name, pb, &part);
+    if (st) return st;
+  }
+  KScope k(ctx, "project_f32", pb ? 2 : 1);
+  vlbk::launch_project_f32(rad, nprobes, dirs->n, dirs->d_basis16, K, out, static_cast<float*>(part), ctx->stream);
   return VLB_OK;
 }
 
@@ -1029,10 +1051,8 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     }
     if (bf16) {
       if ((st = project_bf16(ctx, a.radiance_bf16, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) return st;
-    } else {
-      KScope k(ctx, "project_f32");
-      vlbk::launch_project_f32(a.radiance, nprobes, S, p->dirs->d_basis16, K, static_cast<float*>(ob.dev),
-                               ctx->stream);
+    } else if ((st = project_f32(ctx, a.radiance, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) {
+      return st;
     }
   }
   if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) || (st = copy_out(ctx, orad)))
@@ -1043,6 +1063,18 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
 vlb_status vlb_bake(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
                     const vlb_bake_params* params, float* out) {
   return vlb_bake_ex(ctx, scene, probe_xyz, nprobes, params, out, nullptr);
+}
+
+vlb_status vlb_bake_async(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
+                          const vlb_bake_params* params, float* out, void* done_event) {
+  if (!ctx) return VLB_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (nprobes && (!is_device_ptr(probe_xyz) || !is_device_ptr(out)))
+    return fail(ctx, VLB_ERR_INVALID, "vlb_bake_async needs device probes and a device output");
+  const vlb_status st = vlb_bake_ex(ctx, scene, probe_xyz, nprobes, params, out, nullptr);
+  if (st) return st;
+  if (done_event) VLB_CUDA(ctx, cudaEventRecord(static_cast<cudaEvent_t>(done_event), ctx->stream));
+  return VLB_OK;
 }
 
 vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
@@ -1188,12 +1220,13 @@ static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBu
     float* out = bb.out + g.row0 * V;
     const uint32_t n = uint32_t(g.rows);
     if (pl.bf16) {
-      vlb_status st = project_bf16(ctx, reinterpret_cast<const uint16_t*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out);
+      vlb_status st = project_bf16(ctx, reinterpret_cast<const uint16_t*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out,
+                                   "batch_project_partial");
       if (st) return st;
     } else {
-      KScope k(ctx, "project_f32");
-      vlbk::launch_project_f32(reinterpret_cast<const float*>(bb.tile + g.tile_off), n, g.dirs->n,
-                               g.dirs->d_basis16, pl.K, out, ctx->stream);
+      vlb_status st = project_f32(ctx, reinterpret_cast<const float*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out,
+                                  "batch_project_partial");
+      if (st) return st;
     }
   }
   if (bb.ndev_out) {
@@ -1562,9 +1595,8 @@ vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint
   OutBuf ob;
   if ((st = stage_out(ctx, out, size_t(nprobes) * K * 12, "proj_out", &ob))) return st;
   if (dtype == VLB_DTYPE_F32) {
-    KScope k(ctx, "project_f32");
-    vlbk::launch_project_f32(static_cast<const float*>(drad), nprobes, S, dirs->d_basis16, K,
-                             static_cast<float*>(ob.dev), ctx->stream);
+    if ((st = project_f32(ctx, static_cast<const float*>(drad), nprobes, dirs, K, static_cast<float*>(ob.dev))))
+      return st;
   } else if ((st = project_bf16(ctx, static_cast<const uint16_t*>(drad), nprobes, dirs, K,
                                 static_cast<float*>(ob.dev)))) {
     return st;

@@ -64,10 +64,13 @@ void launch_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, ui
                         cudaStream_t s);
 
 // ---- projection of a radiance tile --------------------------------------------
+// `partial`: project_partial_bytes(nprobes, S, K) of device scratch (null when
+// that is 0: the tile is projected unsplit).
+size_t project_partial_bytes(uint32_t nprobes, uint32_t S, uint32_t K);
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
-                        float* out, cudaStream_t s);
+                        float* out, float* partial, cudaStream_t s);
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
-                              uint32_t K, float* out, cudaStream_t s);
+                              uint32_t K, float* out, float* partial, cudaStream_t s);
 // tcgen05 projection of a BF16 tile (k_project_tc.cu).  basis_bt: [32][bt_pitch]
 // BF16, rows 0..15 the high and 16..31 the low part of the weighted basis.
 // Needs S % 8 == 0 and a 16-byte aligned tile; returns -1 if the tensor maps

@@ -122,6 +122,7 @@ def _load() -> C.CDLL:
         "vlb_bake_params_default": (None, [P]),
         "vlb_bake": (I32, [P, P, P, U32, P, P]),
         "vlb_bake_ex": (I32, [P, P, P, U32, P, P, P]),
+        "vlb_bake_async": (I32, [P, P, P, U32, P, P, P]),
         "vlb_bake_trace_stats": (I32, [P, P, P, U32, P, P]),
         "vlb_bake_batch": (I32, [P, P, U32, P, P]),
         "vlb_batch_autotune": (I32, [P, P, U32, P, U32, P, P]),
@@ -305,6 +306,14 @@ class Context:
         dbg = BakeDebug(_ptr(hit), _ptr(vis), _ptr(rad))
         self.check(lib.vlb_bake_ex(self.h, scene.h, _ptr(probes), n, C.byref(params), _ptr(ret), C.byref(dbg)))
         return ret, hit.reshape(n, S), vis.reshape(n, S), (None if rad is None else rad.reshape(n, S, 3))
+
+    def bake_async(self, scene: "Scene", probes, params: BakeParams, out, done_event=None) -> None:
+        """Enqueues a bake of device probes into the device tensor `out` on the
+        context's stream; `done_event` (a recorded-once torch.cuda.Event or a raw
+        cudaEvent_t) is recorded after the bake."""
+        ev = done_event.cuda_event if hasattr(done_event, "cuda_event") else done_event
+        self.check(lib.vlb_bake_async(self.h, scene.h, _ptr(probes), int(probes.shape[0]), C.byref(params),
+                                      _ptr(out), ev))
 
     def bake_batch(self, jobs, params: BakeParams, schedule: "BatchSchedule | None" = None):
         """jobs: list of (scene, probes, out-or-None[, job params]); returns the outputs."""
