@@ -601,7 +601,6 @@ void launch_lbvh_build(const LbvhBuild& b, cudaStream_t st, int* launches) {
   k_cbounds_partial<<<nred, kRedThreads, 0, st>>>(s.cen, n, s.part); ++L;
   k_cbounds_final<<<1, 32, 0, st>>>(s.part, nred, s.params); ++L;
   k_morton<<<g, 256, 0, st>>>(s.cen, n, s.params, s.ka, s.va); ++L;
-  const uint32_t nblk = (n + kRsTile - 1) / kRsTile;
   uint32_t *kin = s.ka, *kout = s.kb, *vin = s.va, *vout = s.vb;
   L += radix_passes(kin, vin, kout, vout, n, s.hist, 4, st);
   cudaMemcpyAsync(b.codes, kin, size_t(n) * 4, cudaMemcpyDeviceToDevice, st);
