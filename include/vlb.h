@@ -52,6 +52,8 @@ typedef struct vlb_sky vlb_sky;
 uint32_t vlb_version(void);
 const char* vlb_status_string(vlb_status s);
 vlb_status vlb_ctx_create(int device, vlb_ctx** out);
+/* Destroy every scene, direction set, sky and service made on a context
+ * before the context itself: their destroy calls use it. */
 void vlb_ctx_destroy(vlb_ctx* ctx);
 /* Run the context's work on a caller-owned cudaStream_t (NULL restores the
  * context's own stream). */

@@ -267,6 +267,23 @@ def test_bake_async_on_caller_stream(ctx):
         ctx.set_stream(None)
 
 
+def test_context_close_closes_its_objects_first():
+    """Closing a context with its scene, direction set and sky still referenced
+    destroys them first (their destroy calls use the context), so dropping
+    them afterwards is safe."""
+    import gc
+
+    c = vlb.Context(0)
+    pos, idx, alb = vlb.synth_box_scene(2, 4)
+    scene, ds, sky = c.scene(pos, idx, alb), c.fibonacci(64), c.sky(vlb.synth_cubemap(2, 8), 8)
+    out = c.bake(scene, np.float32([[0.5, 0.5, 0.5]]), vlb.bake_params(ds, 2, sky=sky))
+    assert np.isfinite(out).all()
+    c.close()
+    assert scene.h is None and ds.h is None and sky.h is None
+    del scene, ds, sky
+    gc.collect()
+
+
 def test_invalid_params(ctx):
     pos, idx, alb = vlb.synth_box_scene(1, 2)
     scene = ctx.scene(pos, idx, alb)

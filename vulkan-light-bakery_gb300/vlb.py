@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -197,13 +198,21 @@ class Context:
         if st != OK:
             raise VlbError(st, f"vlb_ctx_create(device={device}) failed: {lib.vlb_status_string(st).decode()}")
         self.h = h
+        self._objects = weakref.WeakSet()  # scenes, direction sets, skies, services made on this context
 
     def check(self, st: int) -> None:
         if st != OK:
             raise VlbError(st, lib.vlb_last_error(self.h).decode())
 
+    def _own(self, obj) -> None:
+        self._objects.add(obj)
+
     def close(self) -> None:
+        """Destroys the context, after every object still open on it (the C ABI
+        wants a context's objects destroyed before the context)."""
         if getattr(self, "h", None):
+            for obj in list(getattr(self, "_objects", ())):
+                obj.close()
             lib.vlb_ctx_destroy(self.h)
             self.h = None
 
@@ -392,6 +401,7 @@ class Service:
         self.lmax = lmax
         self._check(lib.vlb_service_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h
+        ctx._own(self)
         self._keep = {}  # ticket -> objects the request names (kept alive until collected)
         self._n = {}
 
@@ -570,12 +580,14 @@ class Scene:
                                           flags, C.byref(h)))
         self.h = h
         self.ntris = ntris
+        ctx._own(self)
 
     @classmethod
     def _wrap(cls, ctx: Context, h) -> "Scene":
         s = cls.__new__(cls)
         s.ctx, s.h = ctx, h
         s.ntris = int(lib.vlb_scene_triangle_count(h))
+        ctx._own(s)
         return s
 
     def bounds(self, include_origin: bool = True) -> np.ndarray:
@@ -614,6 +626,7 @@ class DirSet:
         self.ctx = ctx
         self.h = h
         self.n = int(lib.vlb_dirset_count(h))
+        ctx._own(self)
 
     def export(self):
         d = np.empty((self.n, 3), np.float32)
@@ -638,6 +651,7 @@ class Sky:
         self.ctx = ctx
         self.h = h
         self.n = n
+        ctx._own(self)
 
     def close(self) -> None:
         if getattr(self, "h", None):
