@@ -15,6 +15,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "vlb_internal.h"
@@ -204,25 +206,53 @@ float bf16_to_float(uint16_t h) {
   return f;
 }
 
+// Runs f(begin, end) over [0, n) split across up to 16 host threads (one
+// range below `grain` items).  Every item's result depends on that item
+// alone, so the output does not depend on the split; a thread that cannot be
+// started runs its range on the calling thread.
+template <class F>
+void parallel_ranges(size_t n, size_t grain, F f) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t parts = std::min<size_t>(hw, (n + grain - 1) / std::max<size_t>(grain, 1));
+  if (parts <= 1) {
+    f(size_t(0), n);
+    return;
+  }
+  const size_t per = (n + parts - 1) / parts;
+  std::vector<std::thread> th;
+  for (size_t p = 1; p < parts; ++p) {
+    const size_t b = p * per, e = std::min(n, b + per);
+    if (b >= e) break;
+    try {
+      th.emplace_back(f, b, e);
+    } catch (const std::system_error&) {
+      f(b, e);
+    }
+  }
+  f(size_t(0), std::min(n, per));
+  for (auto& t : th) t.join();
+}
+
 // Builds the host + device halves of a direction set.
 vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>& bdirs, const std::vector<double>& w) {
   const uint32_t n = d->n;
   d->h_basis.assign(size_t(n) * 16, 0.0);
   d->h_basis32.assign(size_t(n) * 16, 0.f);
-  for (uint32_t s = 0; s < n; ++s) {
-    double Y[16];
-    sh_basis16(bdirs[3 * s], bdirs[3 * s + 1], bdirs[3 * s + 2], Y);
-    for (int k = 0; k < 16; ++k) {
-      d->h_basis[size_t(s) * 16 + k] = w[s] * Y[k];
-      d->h_basis32[size_t(s) * 16 + k] = float(w[s] * Y[k]);
-    }
-  }
   std::vector<float> d4(size_t(n) * 4, 0.f), i4(size_t(n) * 4, 0.f);
-  for (uint32_t s = 0; s < n; ++s)
-    for (int a = 0; a < 3; ++a) {
-      d4[4 * s + a] = d->h_dirs[3 * s + a];
-      i4[4 * s + a] = vlbk::host_safe_inv(d->h_dirs[3 * s + a]);
+  parallel_ranges(n, 1 << 16, [&](size_t b, size_t e) {
+    for (size_t s = b; s < e; ++s) {
+      double Y[16];
+      sh_basis16(bdirs[3 * s], bdirs[3 * s + 1], bdirs[3 * s + 2], Y);
+      for (int k = 0; k < 16; ++k) {
+        d->h_basis[s * 16 + k] = w[s] * Y[k];
+        d->h_basis32[s * 16 + k] = float(w[s] * Y[k]);
+      }
+      for (int a = 0; a < 3; ++a) {
+        d4[4 * s + a] = d->h_dirs[3 * s + a];
+        i4[4 * s + a] = vlbk::host_safe_inv(d->h_dirs[3 * s + a]);
+      }
     }
+  });
   VLB_CUDA(ctx, cudaMalloc(&d->d_dirs, size_t(n) * sizeof(float4)));
   VLB_CUDA(ctx, cudaMalloc(&d->d_dinv, size_t(n) * sizeof(float4)));
   VLB_CUDA(ctx, cudaMalloc(&d->d_basis16, size_t(n) * 16 * sizeof(float)));
@@ -252,24 +282,37 @@ vlb_status dirset_finish(vlb_ctx* ctx, vlb_dirset* d, const std::vector<double>&
     const uint32_t v = l1 > 0.f ? uint32_t(std::min(1023.f, ay / l1 * 1023.f)) : 0u;
     uint32_t m = 0;
     for (int b = 0; b < 10; ++b) m |= (((u >> b) & 1u) << (2 * b)) | (((v >> b) & 1u) << (2 * b + 1));
-    return (uint64_t(oct(s)) << 32) | m;
+    return (uint32_t(oct(s)) << 20) | m;  // 23 bits
   };
-  std::vector<uint64_t> keys(n);
-  for (uint32_t s = 0; s < n; ++s) { order[s] = s; keys[s] = key(s); }
-  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return keys[x] < keys[y]; });
+  std::vector<uint32_t> keys(n), tmp(n);
+  parallel_ranges(n, 1 << 16, [&](size_t b, size_t e) {
+    for (size_t s = b; s < e; ++s) keys[s] = key(uint32_t(s));
+  });
+  // stable LSD radix sort of the indices by key: 12 low bits, then 11 high
+  for (uint32_t s = 0; s < n; ++s) order[s] = s;
+  for (int pass = 0; pass < 2; ++pass) {
+    const int shift = pass ? 12 : 0;
+    std::vector<uint32_t> cnt(4097, 0);
+    for (uint32_t s = 0; s < n; ++s) ++cnt[((keys[order[s]] >> shift) & 4095u) + 1];
+    for (int b = 0; b < 4096; ++b) cnt[b + 1] += cnt[b];
+    for (uint32_t s = 0; s < n; ++s) tmp[cnt[(keys[order[s]] >> shift) & 4095u]++] = order[s];
+    order.swap(tmp);
+  }
   VLB_CUDA(ctx, cudaMalloc(&d->d_order, size_t(n) * 4));
   VLB_CUDA(ctx, cudaMemcpy(d->d_order, order.data(), size_t(n) * 4, cudaMemcpyHostToDevice));
   // BF16 basis for the tensor-core projection, transposed [32][pitch]: row k
   // the BF16 rounding of w_s Y_k, row 16 + k the BF16 rounding of the rest
   d->bt_pitch = (n + 7) / 8 * 8;
   std::vector<uint16_t> bt(size_t(32) * d->bt_pitch, 0);
-  for (uint32_t s = 0; s < n; ++s)
-    for (int k = 0; k < 16; ++k) {
-      const double b = d->h_basis[size_t(s) * 16 + k];
-      const uint16_t hi = bf16_rne(float(b));
-      bt[size_t(k) * d->bt_pitch + s] = hi;
-      bt[size_t(16 + k) * d->bt_pitch + s] = bf16_rne(float(b - double(bf16_to_float(hi))));
-    }
+  parallel_ranges(n, 1 << 16, [&](size_t sb, size_t se) {
+    for (size_t s = sb; s < se; ++s)
+      for (int k = 0; k < 16; ++k) {
+        const double b = d->h_basis[s * 16 + k];
+        const uint16_t hi = bf16_rne(float(b));
+        bt[size_t(k) * d->bt_pitch + s] = hi;
+        bt[size_t(16 + k) * d->bt_pitch + s] = bf16_rne(float(b - double(bf16_to_float(hi))));
+      }
+  });
   VLB_CUDA(ctx, cudaMalloc(&d->d_bt, bt.size() * 2));
   VLB_CUDA(ctx, cudaMemcpy(d->d_bt, bt.data(), bt.size() * 2, cudaMemcpyHostToDevice));
   return VLB_OK;
@@ -620,17 +663,19 @@ vlb_status vlb_dirset_create_fibonacci(vlb_ctx* ctx, uint32_t n, vlb_frame frame
   d->h_dirs.resize(size_t(n) * 3);
   std::vector<double> bd(size_t(n) * 3), w(n, 4.0 * kPi / double(n));
   const double g = 0.6180339887498949, two_pi = 6.283185307179586;
-  for (uint32_t i = 0; i < n; ++i) {
-    const double z = 1.0 - (2.0 * i + 1.0) / double(n);
-    const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
-    double fr = double(i) * g;
-    fr -= std::floor(fr);
-    const double phi = two_pi * fr;
-    const float f[3] = {float(r * std::cos(phi)), float(r * std::sin(phi)), float(z)};
-    for (int a = 0; a < 3; ++a) d->h_dirs[3 * i + a] = f[a];
-    if (frame == VLB_FRAME_WORLD) { bd[3 * i] = f[0]; bd[3 * i + 1] = f[1]; bd[3 * i + 2] = f[2]; }
-    else { bd[3 * i] = f[0]; bd[3 * i + 1] = f[2]; bd[3 * i + 2] = f[1]; }
-  }
+  parallel_ranges(n, 1 << 16, [&](size_t ib, size_t ie) {
+    for (size_t i = ib; i < ie; ++i) {
+      const double z = 1.0 - (2.0 * double(i) + 1.0) / double(n);
+      const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
+      double fr = double(i) * g;
+      fr -= std::floor(fr);
+      const double phi = two_pi * fr;
+      const float f[3] = {float(r * std::cos(phi)), float(r * std::sin(phi)), float(z)};
+      for (int a = 0; a < 3; ++a) d->h_dirs[3 * i + a] = f[a];
+      if (frame == VLB_FRAME_WORLD) { bd[3 * i] = f[0]; bd[3 * i + 1] = f[1]; bd[3 * i + 2] = f[2]; }
+      else { bd[3 * i] = f[0]; bd[3 * i + 1] = f[2]; bd[3 * i + 2] = f[1]; }
+    }
+  });
   vlb_status st = dirset_finish(ctx, d, bd, w);
   if (st) { vlb_dirset_destroy(d); return st; }
   *out = d;
@@ -647,19 +692,21 @@ vlb_status vlb_dirset_create_equirect(vlb_ctx* ctx, uint32_t w, uint32_t h, vlb_
   d->ctx = ctx; d->n = n;
   d->h_dirs.resize(size_t(n) * 3);
   std::vector<double> bd(size_t(n) * 3), wt(n);
-  for (uint32_t y = 0; y < h; ++y)
-    for (uint32_t x = 0; x < w; ++x) {
-      const size_t s = size_t(y) * w + x;
-      const double phi = 2.0 * kPiRef * (double(x) + 0.5) / double(w);
-      const double th = kPiRef * (double(y) + 0.5) / double(h);
-      const double r = std::sin(th);
-      double v[3] = {r * std::cos(phi), r * std::sin(phi), std::cos(th)};
-      const double nn = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-      for (int a = 0; a < 3; ++a) v[a] /= nn;
-      d->h_dirs[3 * s] = float(v[0]); d->h_dirs[3 * s + 1] = float(v[2]); d->h_dirs[3 * s + 2] = float(v[1]);
-      bd[3 * s] = v[0]; bd[3 * s + 1] = v[1]; bd[3 * s + 2] = v[2];
-      wt[s] = (2.0 * kPiRef / w) * (kPiRef / h) * std::sin(th);
-    }
+  parallel_ranges(h, std::max<size_t>(1, (1 << 16) / w), [&](size_t yb, size_t ye) {
+    for (size_t y = yb; y < ye; ++y)
+      for (uint32_t x = 0; x < w; ++x) {
+        const size_t s = y * w + x;
+        const double phi = 2.0 * kPiRef * (double(x) + 0.5) / double(w);
+        const double th = kPiRef * (double(y) + 0.5) / double(h);
+        const double r = std::sin(th);
+        double v[3] = {r * std::cos(phi), r * std::sin(phi), std::cos(th)};
+        const double nn = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int a = 0; a < 3; ++a) v[a] /= nn;
+        d->h_dirs[3 * s] = float(v[0]); d->h_dirs[3 * s + 1] = float(v[2]); d->h_dirs[3 * s + 2] = float(v[1]);
+        bd[3 * s] = v[0]; bd[3 * s + 1] = v[1]; bd[3 * s + 2] = v[2];
+        wt[s] = (2.0 * kPiRef / w) * (kPiRef / h) * std::sin(th);
+      }
+  });
   vlb_status st = dirset_finish(ctx, d, bd, wt);
   if (st) { vlb_dirset_destroy(d); return st; }
   *out = d;
