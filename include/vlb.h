@@ -30,7 +30,7 @@ extern "C" {
 
 /* Replaces the reference's C++ exceptions (std::runtime_error, vk::SystemError,
  * caught in src/baker/main.cpp:26-40) and the printed-only fence failure of
- * src/application.cpp:266-273. */
+ * src/application.cpp:265-273. */
 typedef enum vlb_status {
   VLB_OK = 0,
   VLB_ERR_INVALID = 1,     /* bad argument (message in vlb_last_error) */
@@ -47,7 +47,7 @@ typedef struct vlb_dirset vlb_dirset;
 typedef struct vlb_sky vlb_sky;
 
 /* ---- context ------------------------------------------------------------
- * Replaces Application::Application (src/application.cpp:540-560): device,
+ * Replaces Application::Application (src/application.cpp:540-556): device,
  * queues and command pools become one CUDA device + one stream. */
 uint32_t vlb_version(void);
 const char* vlb_status_string(vlb_status s);
@@ -79,7 +79,7 @@ uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx);
 
 /* ---- probe grid -----------------------------------------------------------
  * Replaces LightBaker::probePositionsFromBoudingBox
- * (src/baker/light_baker.cpp:138-159): same FP32 arithmetic, same order (the
+ * (src/baker/light_baker.cpp:80-101): same FP32 arithmetic, same order (the
  * grid is grown one axis at a time: x runs first, then each existing probe is
  * repeated along y, then along z).  bounds = {min xyz, max xyz}; out_xyz
  * holds counts[0]*counts[1]*counts[2]*3 floats; grid_step may be NULL. */
@@ -88,7 +88,7 @@ vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts
 
 /* ---- scene ------------------------------------------------------------------
  * Replaces SceneManager::pushScene + Scene_t::buildAccelerationStructures
- * (src/scene_manager.cpp:1013-1034, :339-443): the hardware BLAS/TLAS becomes
+ * (src/scene_manager.cpp:1013-1034, :339-442): the hardware BLAS/TLAS becomes
  * a Morton LBVH built on the device (bit-exact with a CPU build).
  * positions: nverts vertices, position_stride_bytes apart (12 for packed xyz,
  * 48 for the reference's shader::Vertex, shaders/structures.h:20-26).
@@ -106,7 +106,8 @@ vlb_status vlb_scene_create_ex(vlb_ctx* ctx, const float* positions, uint32_t po
                                uint32_t flags, vlb_scene** out);
 void vlb_scene_destroy(vlb_scene* scene);
 uint32_t vlb_scene_triangle_count(const vlb_scene* scene);
-/* Replaces Scene_t::getBounds (src/scene_manager.hpp:214, cpp:497-507).  The
+/* Replaces Scene_t::getBounds (src/scene_manager.cpp:214-217; the bounds are
+ * grown in Scene_t::loadNode, :496-506).  The
  * reference starts its bounds at the origin, so include_origin=1 reproduces
  * it; 0 gives the plain vertex bounds. */
 vlb_status vlb_scene_bounds(const vlb_scene* scene, int include_origin, float out[6]);
@@ -174,11 +175,13 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
  * library, held by every GPU that loads the library until the process exits.
  * One map per call; lmax 2 or 3; cubemap faces up to 256, panoramas up to
  * 8192 x 8192; texels and out must be device memory of the current device
- * (host pointers and larger sizes return VLB_ERR_INVALID).  stream: a
- * cudaStream_t or NULL; the call returns when the result is in out.  The
- * first call on a device looks up the array's device address, so make it
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race and must be serialised by the caller. */
+ * (host pointers, larger sizes and unknown flags return VLB_ERR_INVALID).
+ * stream: a cudaStream_t or NULL; the call synchronises that stream and
+ * returns when the result is in out.  The first call on a device looks up
+ * the array's device address and keeps it, so make it before any stream
+ * capture; calls after cudaDeviceReset are not supported (the array may
+ * move).  All calls share the array: calls whose work overlaps on the GPU
+ * race and must be serialised by the caller. */
 vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format fmt, vlb_sky_layout layout, uint32_t w,
                                  uint32_t h, uint32_t lmax, uint32_t flags, float* out, void* stream);
 
@@ -189,13 +192,13 @@ vlb_status vlb_sky_create(vlb_ctx* ctx, const float* cubemap_rgb, uint32_t n, vl
 void vlb_sky_destroy(vlb_sky* sky);
 
 /* ---- bake ---------------------------------------------------------------------
- * Replaces LightBaker::bake (src/baker/light_baker.cpp:345-386) with its
+ * Replaces LightBaker::bake (src/baker/light_baker.cpp:287-328) with its
  * per-probe EnvMapGenerator::getMap (src/baker/env_map_generator.cpp:325-359:
  * env_map.rgen -> traversal -> env_map.rchit / shadow.rmiss / main.rmiss)
  * and dispatchBakingKernel (sh.comp).  probe_xyz: nprobes*3.  out: nprobes x
  * K x 3 FP32, probe-major, coefficient k = l(l+1)+m, RGB innermost; with
  * lmax = 3 this is byte-for-byte the reference's 192-byte-per-probe layout
- * (light_baker.cpp:352-379), each probe's own sum (the reference never clears
+ * (light_baker.cpp:294-322), each probe's own sum (the reference never clears
  * its accumulator between probes; that carry-over is not reproduced). */
 typedef enum vlb_precision {
   VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 projection */
@@ -263,7 +266,7 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
 
 /* ---- batched bakes ------------------------------------------------------------
  * No single reference counterpart: the reference bakes one scene per
- * LightBaker (src/baker/light_baker.cpp:27-49, baker/main.cpp:22-24) and one
+ * LightBaker (src/baker/light_baker.cpp:20-74, src/baker/main.cpp:22-24) and one
  * probe per dispatch.  A batch bakes many (scene, probes) jobs at once: one
  * launch sorts every job's probes, ONE persistent trace launch has its warps
  * pull chunks of rays from all jobs (costliest jobs first) and hand them to
@@ -301,7 +304,7 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
 
 /* ---- bake service ------------------------------------------------------------
  * No reference counterpart (the reference bakes once per process,
- * baker/main.cpp:22-24).  A resident service over the scenes, direction sets
+ * src/baker/main.cpp:22-24).  A resident service over the scenes, direction sets
  * and skies of one context: requests are submitted from any thread, admitted
  * against a device-memory budget and baked by a worker thread in continuous
  * batches -- while one batch runs on the GPU the next is assembled from the
@@ -378,7 +381,7 @@ vlb_status vlb_sh_eval_envmap(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, 
 
 /* ---- baked-light glTF files ----------------------------------------------------
  * Host only (no GPU).  Replaces LightBaker::serialize
- * (src/baker/light_baker.cpp:372-401): the input glTF document plus one
+ * (src/baker/light_baker.cpp:375-401): the input glTF document plus one
  * buffer holding the coefficients as a base64 data URI, one bufferView over
  * it and the top-level "light" object {bufferView, gridStep {x, y, z},
  * lmax: coeff_count}, printed the way the reference's JSON library prints it
@@ -389,7 +392,7 @@ vlb_status vlb_sh_eval_envmap(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, 
 vlb_status vlb_gltf_write_light(const char* gltf_json, size_t json_len, const float* coeffs, uint32_t nprobes,
                                 uint32_t coeff_count, const float grid_step[3], char* out, size_t out_cap,
                                 size_t* out_len);
-/* Replaces Scene_t::loadBakedLight (src/scene_manager.cpp:614-648): reads
+/* Replaces Scene_t::loadBakedLight (src/scene_manager.cpp:613-648): reads
  * gridStep, lmax (the coefficient count) and the coefficient bytes
  * (byteLength of the light's buffer) back.  A document without "light"
  * gives zeros and *coeffs_bytes = 0.  coeffs NULL: only the sizes. */
@@ -398,7 +401,7 @@ vlb_status vlb_gltf_read_light(const char* gltf_json, size_t json_len, float gri
 /* Scene geometry from a .gltf (external .bin or data-URI buffers) or .glb file,
  * host only.  Replaces the geometry side of Scene_t::loadNodes / loadNode /
  * fetchVertices / fetchIndices / loadMatrix (src/scene_manager.cpp:257-337,
- * 445-538, 860-870): the triangles of glTF scene 0 in world space (node
+ * 445-533, 860-870): the triangles of glTF scene 0 in world space (node
  * local matrix T*R*S*M, multiplied along the parent chain as the reference's
  * TLAS instances are), u8/u16/u32 indices, per-triangle albedo = the
  * material's baseColorFactor RGB (1 without a material; textures are not
@@ -425,7 +428,7 @@ const char* vlb_gltf_last_error(void);
  * with E_p(n) = sum_k c_pk Y_k(n).  The reference's faults are not reproduced:
  * its cell index assumes the grid starts at the origin and 7 x 7 x 7
  * probes in x-major order (the bake writes them breadth-first,
- * light_baker.cpp:138-159), it strides by (16+1)^2 coefficients and sums 16
+ * src/baker/light_baker.cpp:80-101), it strides by (16+1)^2 coefficients and sums 16
  * bands of a 16-coefficient probe, and it divides 0 by 0 when no probe is
  * visible (here: 0).  coeffs: the bake's output for the grid, nprobes x K x 3
  * in the reference's breadth-first order (vlb_probe_grid_ref_order).
@@ -448,11 +451,12 @@ vlb_status vlb_sh_eval_dirs(vlb_ctx* ctx, const float* coeffs, uint32_t lmax, co
 /* ---- debug env-map images ---------------------------------------------------------
  * The reference writes, for every probe, its traced equirect env map as an
  * R8G8B8A8 UNORM image (src/baker/env_map_generator.hpp:39) to "<probe>.png"
- * (light_baker.cpp:306-307, EnvMapGenerator::saveImage
- * env_map_generator.cpp:73-112); texels are sRGB-encoded by the shaders
- * (env_map.rchit:82, main.rmiss:40, main.rchit:49-56) with alpha 1.
+ * (src/baker/light_baker.cpp:306-307, EnvMapGenerator::saveImage
+ * src/baker/env_map_generator.cpp:73-112); texels are sRGB-encoded by the shaders
+ * (shaders/env_map.rchit:101, shaders/main.rmiss:40,
+ * shaders/main.rchit:49-56) with alpha 1.
  * vlb_encode_rgba8: rgba[i] = UNORM8(srgb ? sRGB(scale*rgb[i]) : scale*rgb[i]),
- * alpha 255 (sh_sum.comp:51 is scale 1250 without sRGB).  Host or device. */
+ * alpha 255 (shaders/sh_sum.comp:51 is scale 1250 without sRGB).  Host or device. */
 vlb_status vlb_encode_rgba8(vlb_ctx* ctx, const float* rgb, uint32_t n, float scale, uint32_t srgb, uint8_t* rgba);
 /* One probe's env map as the reference's debug image: the probe's traced
  * radiance over params->dirs, which must be vlb_dirset_create_equirect(w, h)

@@ -13,7 +13,7 @@
 //   * per-probe projection, weights, k=l(l+1)+m ..... shaders/sh.comp:23-42
 //   * skybox projection (phi - PI/2, basis at .xzy) . shaders/skybox_sh.comp:23-42
 //   * SH reconstruction (x1250) ..................... shaders/sh_sum.comp:35-52
-//   * probe grid order .............................. src/baker/light_baker.cpp:138-159
+//   * probe grid order .............................. src/baker/light_baker.cpp:80-101
 //   * closest-hit + shadow ray structure ............ shaders/env_map.rchit:51-102,
 //                                                     shaders/shadow.rmiss:6-9
 // Pieces the reference does not have (cubemap solid angle, Fibonacci sphere
@@ -667,7 +667,7 @@ void orc_sh_eval_envmap(const double* coeffs, int lmax, uint32_t w, uint32_t h, 
     }
 }
 
-// ---- probe grid (light_baker.cpp:138-159), FP32 like glm::vec3 -------------
+// ---- probe grid (light_baker.cpp:80-101), FP32 like glm::vec3 -------------
 uint32_t orc_probe_grid_ref_order(const float* bounds, const uint32_t* counts, float* out, float* step) {
   float st[3];
   for (int a = 0; a < 3; ++a) {
@@ -747,7 +747,7 @@ void orc_bake(const void* scene, const float* probes, uint32_t np, const float* 
 // ---- probe evaluation (consumer side) ------------------------------------------
 // shaders/main.rchit:124-168 with shaders/sh.rmiss:23-39, intended math: the
 // grid starts at `origin` (the reference assumes 0), probes are indexed in the
-// bake's breadth-first order (light_baker.cpp:138-159; the reference indexes
+// bake's breadth-first order (light_baker.cpp:80-101; the reference indexes
 // x + 7y + 49z), each probe holds K = (lmax+1)^2 coefficients (the reference
 // strides by (16+1)^2 and sums 16 bands), and a point that sees no probe gets
 // 0 (the reference divides 0 by 0).  Per corner c (bits z, y, x of c as in

@@ -17,7 +17,7 @@ FP32 (as the shaders run them):
                are pinned exactly)
   * envmap:    the same for sh.comp:27-41 (no -PI/2, basis at dir)
   * sh_sum:    sh_sum.comp:39-51 reconstruction (x1250) of seeded coefficients
-  * grid:      the probe order of light_baker.cpp:138-159 for a 3x3x3 grid
+  * grid:      the probe order of light_baker.cpp:80-101 for a 3x3x3 grid
                over the unit box, written out from that loop by hand
 """
 from __future__ import annotations
@@ -102,7 +102,7 @@ def main() -> None:
                     c += coeffs[l * (l + 1) + m] * f32(ref.ref_sh(l, m, buf[0], buf[1], buf[2]))
             recon[y, x] = f32(1250.0) * c
 
-    # light_baker.cpp:138-159 for bounds [0,1]^3, counts 3x3x3: positions grow
+    # light_baker.cpp:80-101 for bounds [0,1]^3, counts 3x3x3: positions grow
     # one axis at a time (x run, then each existing probe stepped along y,
     # then along z); step (b1-b0)/(n-1) = 0.5 accumulated in FP32.
     grid = []

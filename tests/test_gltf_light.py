@@ -1,7 +1,7 @@
 """Baked-light glTF files (host only): vlb_gltf_write_light / vlb_gltf_read_light.
 
 The reference re-prints the whole glTF through its JSON library after adding
-the coefficient buffer (src/baker/light_baker.cpp:372-401): sorted keys,
+the coefficient buffer (src/baker/light_baker.cpp:375-401): sorted keys,
 4-space indentation, shortest round-trip doubles, UTF-8 passed through.
 Python's json module prints with the same conventions (sort_keys, indent=4,
 ensure_ascii=False, repr floats), so for documents without numbers in

@@ -1,6 +1,6 @@
 """glTF scene ingestion (vlb_gltf_mesh_*, host only) against a numpy
 restatement of the node transforms: world = parent chain of T * R * S * M
-(scene_manager.cpp:447-477), positions in FP64 rounded once to FP32,
+(scene_manager.cpp:463-477), positions in FP64 rounded once to FP32,
 triangles of scene 0, baseColorFactor albedo."""
 import base64
 import json

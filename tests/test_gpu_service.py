@@ -155,3 +155,29 @@ def test_service_destroy_finishes_pending(ctx, world):
     for i in range(6):
         svc.submit(sc, w["probes"](b, 500), _params(w, 64, vlb.synth_sun(i)))
     svc.close()  # must return after the six bakes, without error
+
+
+def test_context_close_with_requests_in_flight():
+    """Closing a context while its service still has submitted requests: the
+    service finishes them and stops before the scenes, direction sets and
+    skies those requests name are destroyed (no use after free)."""
+    c = vlb.Context(0)
+    pos, idx, alb = vlb.synth_box_scene(77, 300)
+    sc = c.scene(pos, idx, alb)
+    ds = c.fibonacci(256)
+    sky = c.sky(vlb.synth_cubemap(3, 32), 32)
+    svc = vlb.Service(c, lmax=2, precision=vlb.PREC_FP32, max_batch_probes=2000)
+    rng = np.random.default_rng(5)
+    b = sc.bounds()
+    for i in range(12):
+        p = vlb.bake_params(ds, 2, vlb.PREC_FP32, vlb.synth_sun(i), sky=sky)
+        svc.submit(sc, (b[:3] + rng.random((1500, 3)) * (b[3:] - b[:3])).astype(np.float32), p)
+    c.close()
+    assert svc.h is None and sc.h is None and ds.h is None and c.h is None
+    # the device is still usable afterwards
+    c2 = vlb.Context(0)
+    sc2 = c2.scene(pos, idx, alb)
+    out = c2.bake(sc2, np.float32([[0.5, 0.5, 0.5]]), vlb.bake_params(c2.fibonacci(64), 2, vlb.PREC_FP32,
+                                                                      vlb.synth_sun(1)))
+    assert np.isfinite(out).all()
+    c2.close()

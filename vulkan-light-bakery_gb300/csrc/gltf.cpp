@@ -1,16 +1,16 @@
 // gltf.cpp -- glTF entry points of include/vlb.h (host code):
 //   vlb_gltf_write_light  replaces LightBaker::serialize
-//                         (src/baker/light_baker.cpp:372-401)
+//                         (src/baker/light_baker.cpp:375-401)
 //   vlb_gltf_read_light   replaces Scene_t::loadBakedLight
-//                         (src/scene_manager.cpp:614-648)
+//                         (src/scene_manager.cpp:613-648)
 //   vlb_gltf_mesh_*       replace the geometry side of Scene_t::loadNodes /
 //                         loadNode / fetchVertices / fetchIndices / loadMatrix
-//                         (src/scene_manager.cpp:257-337, 445-538, 860-870)
+//                         (src/scene_manager.cpp:257-337, 445-533, 860-870)
 // The document model and its printing follow the reference's JSON library
 // (json.h); base64 is the standard alphabet with '=' padding
-// (light_baker.cpp:330-370), and decoding stops at the first '=' or
+// (light_baker.cpp:330-373), and decoding stops at the first '=' or
 // non-alphabet character as the reference's decoder does
-// (scene_manager.cpp:556-612).
+// (scene_manager.cpp:556-611).
 #include <cmath>
 #include <cstdio>
 #include <cstring>

@@ -1,8 +1,8 @@
 // json.h -- a small JSON document model for the glTF entry points.
 //
 // The reference reads and writes glTF with nlohmann::json (third-party,
-// nlohmann/json, header-only; src/baker/light_baker.cpp:372-401,
-// src/scene_manager.cpp:614-648).  Its observable behaviour is restated
+// nlohmann/json, header-only; src/baker/light_baker.cpp:375-401,
+// src/scene_manager.cpp:613-648).  Its observable behaviour is restated
 // here, not its code:
 //   * objects keep their keys sorted by byte value (nlohmann's default
 //     object type is std::map); a repeated key keeps its last value;

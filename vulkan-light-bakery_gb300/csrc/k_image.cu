@@ -1,7 +1,7 @@
 // k_image.cu -- RGBA8 encoding of radiance images (debug env maps).
 //
 // The reference stores every env-map texel into an R8G8B8A8 UNORM image
-// (src/baker/env_map_generator.hpp:39): env_map.rchit:82 and main.rmiss:40
+// (src/baker/env_map_generator.hpp:39): env_map.rchit:101 and main.rmiss:40
 // pass the radiance through sRGB() (main.rchit:49-56: 12.92 x below
 // 0.0031308, else 1.055 x^(1/2.4) - 0.055) and env_map.rgen:27 writes it with
 // alpha 1; sh_sum.comp:51 writes 1250 x the reconstruction without sRGB.

@@ -1,5 +1,5 @@
 // k_lbvh.cu -- device LBVH build, replacing the driver-built BLAS/TLAS of
-// Scene_t::buildAS / buildAccelerationStructures (src/scene_manager.cpp:339-443).
+// Scene_t::buildAS / buildAccelerationStructures (src/scene_manager.cpp:339-442).
 //
 // Karras 2012 ("Maximizing parallelism in the construction of BVHs, octrees
 // and k-d trees").  Every step is either integer arithmetic or an IEEE FP32

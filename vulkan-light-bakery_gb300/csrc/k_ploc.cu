@@ -2,7 +2,7 @@
 // Meister and Bittner 2018, "Parallel Locally-Ordered Clustering for Bounding
 // Volume Hierarchy Construction") over the Morton-sorted triangles of the LBVH
 // build.  Replaces, like the LBVH, the driver's BLAS/TLAS build
-// (src/scene_manager.cpp:339-443); the Karras LBVH stays as the exported,
+// (src/scene_manager.cpp:339-442); the Karras LBVH stays as the exported,
 // bit-exact build, this tree is what the trace kernels walk.
 //
 // Clusters start as the leaves in Morton order.  Each round:

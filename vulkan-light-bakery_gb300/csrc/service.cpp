@@ -1,7 +1,7 @@
 // service.cpp -- the resident bake service of include/vlb.h (vlb_service_*).
 //
 // No reference counterpart: the reference bakes one scene per process
-// (baker/main.cpp:22-24, LightBaker::bake light_baker.cpp:166-230).  This is
+// (baker/main.cpp:22-24, LightBaker::bake light_baker.cpp:287-328).  This is
 // the serving loop around the batched bake:
 //
 //   submit (any thread)  -> queue (FIFO, mutex)

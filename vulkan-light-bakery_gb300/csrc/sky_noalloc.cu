@@ -15,7 +15,12 @@
 // contents behind; the counters that must start at zero are cleared at the
 // start of each call, so calls whose work overlaps on the GPU (several host
 // threads, or several streams) race on the array and must be serialised by
-// the caller.
+// the caller.  The array's device address is looked up once per device and
+// kept: after cudaDeviceReset (or a release of the device's primary context)
+// the library's module is loaded again and the array may move, so calls
+// after a reset are not supported.  Each call waits for its own work on the
+// caller's stream (it reads the error counters back with an asynchronous
+// copy on that stream, then synchronises the stream) before it returns.
 #include <algorithm>
 #include <mutex>
 
@@ -95,6 +100,7 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
                                             void* stream) {
   if (!texels || !out) return VLB_ERR_INVALID;
   if (lmax != 2 && lmax != 3) return VLB_ERR_INVALID;
+  if (flags & ~uint32_t(VLB_SKY_REF_BGRA_SWAP)) return VLB_ERR_INVALID;
   if (fmt != VLB_TEXEL_RGB32F && fmt != VLB_TEXEL_RGBA8) return VLB_ERR_INVALID;
   if (layout != VLB_SKY_CUBEMAP && layout != VLB_SKY_PANORAMA && layout != VLB_SKY_ENVMAP) return VLB_ERR_INVALID;
   if (!w || !h) return VLB_ERR_INVALID;
@@ -113,6 +119,15 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
   float4* row = reinterpret_cast<float4*>(base + kPartialBytes + kTableBytes + kColBytes);
   int* err = reinterpret_cast<int*>(base + kPartialBytes + kTableBytes + kColBytes + kRowBytes);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // A launch error the caller left pending on this thread is not this call's:
+  // it is neither cleared nor reported here.
+  const cudaError_t prior = cudaPeekAtLastError();
+  auto launch_failed = [prior]() {
+    if (prior != cudaSuccess) return false;
+    if (cudaPeekAtLastError() == cudaSuccess) return false;
+    cudaGetLastError();  // this call's own launch error: clear it
+    return true;
+  };
 
   const uint32_t T = layout == VLB_SKY_CUBEMAP ? 6 * w * w : w * h;
   const uint32_t TB = fmt == VLB_TEXEL_RGB32F ? 12 : 4;
@@ -135,13 +150,16 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
     k_pano_tables<<<(n + 255) / 256, 256, 0, s>>>(col, row, w, h, layout == VLB_SKY_PANORAMA);
     a.col_tab = col; a.row_tab = row;
   }
+  if (launch_failed()) return VLB_ERR_CUDA;
   const bool tma = (reinterpret_cast<uintptr_t>(texels) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
   vlbk::launch_skybox_sh(a, tma, num_sms, s);
+  if (launch_failed()) return VLB_ERR_CUDA;
   vlbk::launch_sh_finalize(partial, 1, spm * vlbk::kSkyPartialsPerSlab, V, out, s);
-  if (cudaGetLastError() != cudaSuccess) return VLB_ERR_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return VLB_ERR_CUDA;
+  if (launch_failed()) return VLB_ERR_CUDA;
+  // the error counters come back on the caller's stream (no legacy-stream copy)
   int herr[vlbk::kErrSlots];
-  if (cudaMemcpy(herr, err, sizeof herr, cudaMemcpyDeviceToHost) != cudaSuccess) return VLB_ERR_CUDA;
+  if (cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s) != cudaSuccess) return VLB_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return VLB_ERR_CUDA;
   if (herr[vlbk::kErrTimeout]) return VLB_ERR_TIMEOUT;
   for (int i = 0; i < vlbk::kErrSlots; ++i)
     if (herr[i]) return VLB_ERR_INTERNAL;

@@ -492,7 +492,7 @@ vlb_status vlb_ctx_profile_reset(vlb_ctx* ctx) {
 
 uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
-// ---- probe grid (light_baker.cpp:138-159) ---------------------------------------
+// ---- probe grid (light_baker.cpp:80-101) ---------------------------------------
 vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts[3], float* out_xyz,
                                     float grid_step[3]) {
   if (!bounds || !counts || !out_xyz) return VLB_ERR_INVALID;

@@ -209,10 +209,18 @@ class Context:
 
     def close(self) -> None:
         """Destroys the context, after every object still open on it (the C ABI
-        wants a context's objects destroyed before the context)."""
+        wants a context's objects destroyed before the context).  Services go
+        first: destroying one finishes its submitted requests and joins its
+        worker, which may still be baking with the scenes, direction sets and
+        skies those requests name; those objects are destroyed after that."""
         if getattr(self, "h", None):
-            for obj in list(getattr(self, "_objects", ())):
-                obj.close()
+            objs = list(getattr(self, "_objects", ()))
+            for obj in objs:
+                if isinstance(obj, Service):
+                    obj.close()
+            for obj in objs:
+                if not isinstance(obj, Service):
+                    obj.close()
             lib.vlb_ctx_destroy(self.h)
             self.h = None
 

@@ -4,7 +4,10 @@ Each translation unit compiles in parallel; an object is rebuilt only when a
 source or header is newer.  Output: vulkan-light-bakery_gb300/_build/libvlb.so
 (git-ignored).  Also builds the oracle under oracle/_build (and the reference
 header shim under oracle/_ref when the reference checkout exists) -- those are
-test infrastructure, built here only so one call prepares a machine.
+test infrastructure, built here only so one call prepares a machine.  The
+shim needs the reference checkout: set VLB_REFERENCE_DIR to its root (no
+default; without it the shim is skipped and the tests use the committed
+fixtures alone).
 """
 from __future__ import annotations
 
@@ -21,7 +24,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libvlb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-REFERENCE = Path(os.environ.get("VLB_REFERENCE_DIR", "/root/reference"))
+_REF_DIR = os.environ.get("VLB_REFERENCE_DIR")
+REFERENCE = Path(_REF_DIR) if _REF_DIR else None
 
 
 def _nvcc() -> str:
@@ -88,8 +92,8 @@ def build_oracle(verbose: bool = False) -> Path:
     if _stale(out, [src]):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-shared", "-o", str(out),
               str(src)])
-    hdr = REFERENCE / "shaders" / "sh_common.h"
-    if hdr.exists():
+    hdr = REFERENCE / "shaders" / "sh_common.h" if REFERENCE else None
+    if hdr is not None and hdr.exists():
         shim = REPO / "oracle" / "ref_shim.cpp"
         ref = REPO / "oracle" / "_ref" / "libshref.so"
         ref.parent.mkdir(exist_ok=True)
