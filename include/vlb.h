@@ -201,10 +201,15 @@ void vlb_sky_destroy(vlb_sky* sky);
  * (light_baker.cpp:294-322), each probe's own sum (the reference never clears
  * its accumulator between probes; that carry-over is not reproduced). */
 typedef enum vlb_precision {
-  VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 projection */
-  VLB_PREC_FUSED = 1, /* FP32, fastest schedule: trace + projection in one kernel when the probe count
-                         is large enough to fill the GPU one packet per warp, else the tile schedule */
-  VLB_PREC_MIXED = 2  /* BF16 radiance tile, BF16 projection */
+  VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 CUDA-core projection (the drop-in) */
+  VLB_PREC_FUSED = 1, /* FP32, one kernel: each warp projects the rays it traced (FP32 sums in a
+                         fixed order, FP64 chunk sums); no radiance tile */
+  VLB_PREC_MIXED = 2, /* radiance stored as BF16 hi/lo pairs (4 bytes a sample), projected on the
+                         tensor cores with the hi/lo BF16 basis and FP32 accumulation: within 1e-4
+                         of FP64 like FP32 */
+  VLB_PREC_BF16 = 3   /* radiance stored as one BF16 (2 bytes a sample), tensor-core projection with
+                         the hi/lo basis: half the tile bytes, ~8 mantissa bits per sample (about
+                         2e-3 relative SH error on lit box scenes) */
 } vlb_precision;
 /* vlb_bake_params.flags: with VLB_PREC_FUSED, always run the one-kernel schedule. */
 #define VLB_BAKE_FORCE_FUSED_KERNEL 1u
@@ -272,8 +277,9 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
  * pull chunks of rays from all jobs (costliest jobs first) and hand them to
  * their lanes as the lanes free up, then one projection per direction set
  * writes all of that set's probes.  Each job's output is
- * bit-identical to vlb_bake of that job alone with the same parameters:
- * VLB_PREC_FP32 or VLB_PREC_MIXED (VLB_PREC_FUSED bakes as VLB_PREC_FP32).
+ * bit-identical to vlb_bake of that job alone with the same parameters, in
+ * every precision (VLB_PREC_FUSED: one persistent fused launch over all
+ * jobs' work items, no tile and no projection launch).
  * The device part of a batch is captured in a CUDA graph on the second call
  * with the same shape (job count, per-job probe counts, direction sets,
  * output placement) and replayed while the shape repeats. */
@@ -286,19 +292,28 @@ typedef struct vlb_bake_job {
 } vlb_bake_job;
 /* Schedule knobs of the batched trace (results do not depend on them). */
 typedef struct vlb_batch_schedule {
-  uint32_t dirs_per_item; /* rays per lane in a warp's chunk of a job's rays (chunk = 32 x this), 1..64;
-                             0 = library choice */
+  uint32_t dirs_per_item; /* tile walks: rays per lane in a warp's chunk of a job's rays (chunk = 32 x this),
+                             1..64; 0 = library choice */
   uint32_t cost_order;    /* 1: work items of the costliest jobs (rays x log2 triangles) first */
   uint32_t graph;         /* 1: capture and replay the device part as a CUDA graph */
+  uint32_t ctas_per_sm;   /* fused walk: resident 4-warp CTAs per SM its registers are sized for,
+                             7, 8 or 9 (fewer: more registers a thread); 0 = 8 */
+  uint32_t node_steps;    /* fused walk: inner-node steps of a lane turn before the leaf tests, 1..16;
+                             0 = 6 */
+  uint32_t refill_idle;   /* fused walk: idle lanes that make a warp hand out new rays, 1..32; 0 = 16 */
 } vlb_batch_schedule;
 /* sched NULL: the schedule vlb_batch_autotune stored in the context, else
- * the library default {0, 1, 1}. */
+ * the library default {0, 1, 1, 0, 0, 0}.  A VLB_PREC_FUSED vlb_bake uses
+ * the tuned fused-walk knobs too. */
 vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                           const vlb_batch_schedule* sched);
-/* Times the batch under each candidate schedule (rays per lane per chunk 1,
- * 2, 4, 8, 16 x job order, reps runs each, outputs written every run), stores the fastest in
- * the context for later vlb_bake_batch calls with sched NULL and returns it
- * with its mean milliseconds per batch. */
+/* Times the batch under candidate schedules (reps runs each, outputs written
+ * every run), stores the fastest in the context for later vlb_bake_batch calls
+ * with sched NULL and returns it with its mean milliseconds per batch.  Tile
+ * walks: rays per lane per chunk 1, 2, 4, 8, 16 x job order.  Fused walks
+ * (VLB_PREC_FUSED): one knob at a time from the default -- CTAs per SM 7, 8,
+ * 9; node steps 4, 6, 8, 12; refill threshold 8, 16, 24; job order -- each
+ * kept at its fastest value before the next is swept. */
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                               uint32_t reps, vlb_batch_schedule* best, float* best_ms);
 
@@ -320,7 +335,7 @@ typedef struct vlb_service vlb_service;
 typedef struct vlb_service_config {
   uint64_t hbm_budget_bytes; /* device bytes for batches in flight plus kept hits (0: 64 GiB) */
   uint32_t lmax;             /* 2 or 3, every request */
-  uint32_t precision;        /* VLB_PREC_FP32 or VLB_PREC_MIXED (VLB_PREC_FUSED bakes as FP32) */
+  uint32_t precision;        /* vlb_precision of every request */
   uint32_t max_batch_probes; /* probes per batch (0: 1,048,576) */
   uint32_t max_inflight;     /* batches queued on the GPU at once (0: 2) */
 } vlb_service_config;
@@ -370,7 +385,11 @@ vlb_status vlb_service_plan(const uint64_t* probes, const uint64_t* bytes, uint3
  * Replaces dispatchBakingKernel / shaders/sh.comp:23-42 for a radiance tile
  * laid out [nprobes][3][S] (S = the direction set's count): out nprobes x K x
  * 3.  dtype selects FP32 or BF16 radiance. */
-typedef enum vlb_dtype { VLB_DTYPE_F32 = 0, VLB_DTYPE_BF16 = 1 } vlb_dtype;
+typedef enum vlb_dtype {
+  VLB_DTYPE_F32 = 0,
+  VLB_DTYPE_BF16 = 1,       /* [nprobes][3][S] BF16 */
+  VLB_DTYPE_BF16_SPLIT = 2  /* [nprobes][3][2S] BF16 hi/lo pairs: S high parts, then S low parts */
+} vlb_dtype;
 vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint32_t nprobes, const vlb_dirset* dirs,
                        uint32_t lmax, float* out);
 /* Replaces shaders/sh_sum.comp:35-52: out[y][x] = scale * sum_k c_k

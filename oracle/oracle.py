@@ -44,6 +44,9 @@ def _load():
         "orc_shadow_margin": (D, [P, P, P, D, D]),
         "orc_closest_hit": (None, [P, P, P, D, D, P, P]),
         "orc_probe_eval": (None, [P, P, I32, P, P, P, P, P, U32, F, I32, P, P, P]),
+        "orc_synth_box_scene": (I32, [C.c_uint64, U32, P, P, P, C.POINTER(U32), C.POINTER(U32)]),
+        "orc_synth_cubemap": (None, [C.c_uint64, U32, P]),
+        "orc_synth_sun": (None, [C.c_uint64, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -158,6 +161,29 @@ def probe_grid_ref_order(bounds, counts):
     m = lib.orc_probe_grid_ref_order(_p(b), _p(c), _p(out), _p(step))
     assert m == n
     return out, step
+
+
+def synth_box_scene(seed, nboxes):
+    """The benchmark's seeded box scene (positions, indices, per-triangle albedo)."""
+    nv, nt = C.c_uint32(), C.c_uint32()
+    lib.orc_synth_box_scene(seed, nboxes, None, None, None, C.byref(nv), C.byref(nt))
+    pos = np.empty((nv.value, 3), np.float32)
+    idx = np.empty((nt.value, 3), np.uint32)
+    alb = np.empty((nt.value, 3), np.float32)
+    assert lib.orc_synth_box_scene(seed, nboxes, _p(pos), _p(idx), _p(alb), None, None) == 0
+    return pos, idx, alb
+
+
+def synth_cubemap(seed, n):
+    out = np.empty((6, n, n, 3), np.float32)
+    lib.orc_synth_cubemap(seed, n, _p(out))
+    return out
+
+
+def synth_sun(seed):
+    out = np.empty(3, np.float32)
+    lib.orc_synth_sun(seed, _p(out))
+    return out
 
 
 def lbvh_build(pos, idx):

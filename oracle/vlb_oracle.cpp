@@ -692,6 +692,113 @@ uint32_t orc_probe_grid_ref_order(const float* bounds, const uint32_t* counts, f
   return uint32_t(pos.size() / 3);
 }
 
+// ---- seeded workloads ------------------------------------------------------
+// The benchmark's synthetic inputs, restated here so that the CPU baseline
+// builds them without the product library: SplitMix64 (Steele, Lea and
+// Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014; the
+// published constants), 24-bit uniform floats, rejection-sampled unit
+// directions.  Scene: the unit room open at +Y (5 quads, albedo 0.5) and
+// boxes with centres uniform in [0.1,0.9]^3, edges in [0.05,0.2], albedo in
+// [0.2,0.8] per channel; cubemap: 0.3 + three spherical Gaussian lobes;
+// sun: a unit direction on the upper (+Y) hemisphere.  The stream layout
+// (seed salts, draw order, corner and quad order) defines the workload and
+// is checked against the library's generators bit for bit by the tests.
+struct Rng {
+  uint64_t s;
+  explicit Rng(uint64_t seed) : s(seed) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  float unit() { return float(next() >> 40) * 0x1p-24f; }
+  float in(float lo, float hi) {
+    volatile float w = hi - lo;
+    volatile float t = w * unit();
+    return lo + t;
+  }
+  void dir(double* d, bool upper) {
+    for (;;) {
+      const double x = 2.0 * unit() - 1.0, y = 2.0 * unit() - 1.0, z = 2.0 * unit() - 1.0;
+      const double r2 = x * x + y * y + z * z;
+      if (r2 > 1.0 || r2 < 1e-6) continue;
+      if (upper && y <= 0.0) continue;
+      const double r = std::sqrt(r2);
+      d[0] = x / r; d[1] = y / r; d[2] = z / r;
+      return;
+    }
+  }
+};
+
+int orc_synth_box_scene(uint64_t seed, uint32_t nboxes, float* pos, uint32_t* idx, float* alb, uint32_t* nverts,
+                        uint32_t* ntris) {
+  if (nboxes > (1u << 24)) return 1;
+  if (nverts) *nverts = 8 + 8 * nboxes;
+  if (ntris) *ntris = 10 + 12 * nboxes;
+  if (!pos || !idx || !alb) return 0;
+  // corner c of a box: bit 0 x, bit 1 y, bit 2 z; quads wound outward
+  static const uint32_t room[5][4] = {{0, 4, 5, 1}, {0, 2, 6, 4}, {1, 5, 7, 3}, {0, 1, 3, 2}, {4, 6, 7, 5}};
+  static const uint32_t box[6][4] = {{0, 4, 5, 1}, {2, 3, 7, 6}, {0, 2, 6, 4}, {1, 5, 7, 3}, {0, 1, 3, 2}, {4, 6, 7, 5}};
+  uint32_t v = 0, t = 0;
+  auto put_box = [&](const float* lo, const float* hi, const uint32_t (*quads)[4], int nq, const float* rgb) {
+    for (uint32_t c = 0; c < 8; ++c)
+      for (int a = 0; a < 3; ++a) pos[3 * (v + c) + a] = ((c >> a) & 1) ? hi[a] : lo[a];
+    for (int q = 0; q < nq; ++q) {
+      const uint32_t tri[2][3] = {{quads[q][0], quads[q][1], quads[q][2]}, {quads[q][0], quads[q][2], quads[q][3]}};
+      for (int i = 0; i < 2; ++i, ++t)
+        for (int k = 0; k < 3; ++k) { idx[3 * t + k] = v + tri[i][k]; alb[3 * t + k] = rgb[k]; }
+    }
+    v += 8;
+  };
+  const float z0[3] = {0.f, 0.f, 0.f}, o1[3] = {1.f, 1.f, 1.f}, grey[3] = {0.5f, 0.5f, 0.5f};
+  put_box(z0, o1, room, 5, grey);
+  Rng r(seed ^ 0x5CE9E5CE9E5CE9EULL);
+  for (uint32_t b = 0; b < nboxes; ++b) {
+    float c[3], e[3], rgb[3], lo[3], hi[3];
+    for (float& x : c) x = r.in(0.1f, 0.9f);
+    for (float& x : e) x = r.in(0.05f, 0.2f);
+    for (float& x : rgb) x = r.in(0.2f, 0.8f);
+    for (int a = 0; a < 3; ++a) {
+      volatile float h = e[a] * 0.5f;
+      lo[a] = c[a] - h;
+      hi[a] = c[a] + h;
+    }
+    put_box(lo, hi, box, 6, rgb);
+  }
+  return 0;
+}
+
+void orc_synth_cubemap(uint64_t seed, uint32_t n, float* out) {
+  Rng r(seed ^ 0xC0BE0C0BE0C0BEULL);
+  double mu[3][3], k[3], I[3][3];
+  for (int j = 0; j < 3; ++j) {
+    r.dir(mu[j], false);
+    k[j] = 20.0 + 180.0 * r.unit();
+    for (int c = 0; c < 3; ++c) I[j][c] = 1.0 + 49.0 * r.unit();
+  }
+  for (int f = 0; f < 6; ++f)
+    for (uint32_t y = 0; y < n; ++y)
+      for (uint32_t x = 0; x < n; ++x) {
+        double d[3];
+        cube_face_dir(f, 2.0 * (x + 0.5) / n - 1.0, 2.0 * (y + 0.5) / n - 1.0, d);
+        double L[3] = {0.3, 0.3, 0.3};
+        for (int j = 0; j < 3; ++j) {
+          const double g = std::exp(k[j] * (d[0] * mu[j][0] + d[1] * mu[j][1] + d[2] * mu[j][2] - 1.0));
+          for (int c = 0; c < 3; ++c) L[c] += I[j][c] * g;
+        }
+        float* o = out + ((size_t(f) * n + y) * n + x) * 3;
+        for (int c = 0; c < 3; ++c) o[c] = float(L[c]);
+      }
+}
+
+void orc_synth_sun(uint64_t seed, float* out) {
+  Rng r(seed ^ 0x5E45E45E45E45EULL);
+  double d[3];
+  r.dir(d, true);
+  for (int a = 0; a < 3; ++a) out[a] = float(d[a]);
+}
+
 // ---- LBVH -----------------------------------------------------------------
 int orc_lbvh_build(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, uint32_t* codes,
                    uint32_t* order, int32_t* child, float* box) {

@@ -72,13 +72,30 @@ def test_paths_agree(ctx, lmax):
     # the one-kernel schedule is deterministic and independent of the batch
     kernel2 = ctx.bake(scene, probes[::-1].copy(), pk)[::-1]
     assert np.array_equal(kernel, kernel2)
-    mixed = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_MIXED, sun, sky=skyh))
     assert parity.per_probe_rel(fused, plain).max() < 1e-5
+    # the fused lane walk is deterministic, independent of the probe order and
+    # of the per-ray debug outputs
+    fused2 = ctx.bake(scene, probes[::-1].copy(), vlb.bake_params(ds, lmax, vlb.PREC_FUSED, sun, sky=skyh))[::-1]
+    assert np.array_equal(fused, fused2)
+    fused_dbg, hit, vis, rad = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FUSED, sun, sky=skyh),
+                                        debug=True)
+    assert np.array_equal(fused, fused_dbg)
+    _, hit_p, vis_p, rad_p = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_FP32, sun, sky=skyh),
+                                      debug=True)
+    assert np.array_equal(hit, hit_p) and np.array_equal(vis, vis_p) and np.array_equal(rad, rad_p)
+    # mixed precision: BF16 hi/lo radiance pairs on the tensor cores, within
+    # the FP32 tolerance (hi + lo keeps ~16 mantissa bits of every sample)
+    mixed = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_MIXED, sun, sky=skyh))
     e = parity.per_probe_rel(mixed, plain)
-    print(f"mixed (BF16 radiance tile) vs fp32: max {e.max():.3e} mean {e.mean():.3e}")
-    # BF16 keeps 8 mantissa bits per radiance sample (relative rounding up to
-    # 2^-9).  Samples on one flat lit face share one radiance value, so their
-    # rounding errors are equal and do not average out: ~1e-3 per probe.
+    print(f"mixed (BF16 hi/lo tile) vs fp32: max {e.max():.3e} mean {e.mean():.3e}")
+    assert e.max() < 2e-5, e.max()
+    # the half-size form: one BF16 per sample, its stated error.  BF16 keeps 8
+    # mantissa bits per radiance sample (relative rounding up to 2^-9); samples
+    # on one flat lit face share one radiance value, so their rounding errors
+    # are equal and do not average out: ~1e-3 per probe.
+    bf16 = ctx.bake(scene, probes, vlb.bake_params(ds, lmax, vlb.PREC_BF16, sun, sky=skyh))
+    e = parity.per_probe_rel(bf16, plain)
+    print(f"bf16 (one BF16 a sample) vs fp32: max {e.max():.3e} mean {e.mean():.3e}")
     assert e.max() < 5e-3 and e.mean() < 2e-3
 
 

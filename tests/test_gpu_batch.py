@@ -48,7 +48,8 @@ def _singles(ctx, w, plist):
             for j, p in zip(w["jobs"], plist)]
 
 
-@pytest.mark.parametrize("precision,lmax", [(vlb.PREC_MIXED, 2), (vlb.PREC_FP32, 2), (vlb.PREC_MIXED, 3)])
+@pytest.mark.parametrize("precision,lmax", [(vlb.PREC_MIXED, 2), (vlb.PREC_FP32, 2), (vlb.PREC_MIXED, 3),
+                                            (vlb.PREC_FUSED, 2), (vlb.PREC_FUSED, 3), (vlb.PREC_BF16, 2)])
 def test_batch_matches_single_bakes(ctx, batch_world, precision, lmax):
     w = batch_world
     plist = [_job_params(w, j, lmax, precision) for j in w["jobs"]]
@@ -106,6 +107,42 @@ def test_batch_autotune(ctx, batch_world):
         assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
 
 
+def test_fused_batch_schedule_and_graph_invariance(ctx, batch_world):
+    """The fused walk's launch knobs (register budget, node steps per turn,
+    refill threshold, job order) and graph replay change no bit of any job."""
+    import torch
+
+    w = batch_world
+    plist = [_job_params(w, j, 3, vlb.PREC_FUSED) for j in w["jobs"]]
+    ref = _singles(ctx, w, plist)
+    jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
+    for occ, steps, refill, order in ((7, 1, 1, 0), (8, 6, 16, 1), (9, 16, 32, 1), (9, 4, 8, 0), (7, 12, 24, 1)):
+        outs = ctx.bake_batch(jobs, plist[0], vlb.BatchSchedule(0, order, 0, occ, steps, refill))
+        assert all(np.array_equal(a, b) for a, b in zip(outs, ref)), (occ, steps, refill, order)
+    djobs = []
+    for k, (j, p) in enumerate(zip(w["jobs"], plist)):
+        n = len(j["probes"])
+        o = torch.empty((n, 16, 3), dtype=torch.float32, device="cuda") if k % 2 == 0 else None
+        djobs.append((j["scene"], j["probes"], o, p))
+    for _ in range(3):  # direct, capture + replay, replay
+        outs = ctx.bake_batch(djobs, plist[0], vlb.BatchSchedule(0, 1, 1, 8, 6, 16))
+        torch.cuda.synchronize()
+        for a, b in zip(outs, ref):
+            a = a.cpu().numpy() if hasattr(a, "cpu") else a
+            assert np.array_equal(a, b)
+    with pytest.raises(vlb.VlbError):
+        ctx.bake_batch(jobs, plist[0], vlb.BatchSchedule(0, 1, 0, 5, 6, 16))
+    # the autotuner sweeps the fused knobs and keeps a schedule that bakes the same bits
+    sched, ms = ctx.batch_autotune(jobs, plist[0], reps=1)
+    assert sched.ctas_per_sm in (7, 8, 9) and sched.node_steps in (4, 6, 8, 12) and ms > 0
+    assert sched.refill_idle in (8, 16, 24) and sched.graph == 1
+    outs = ctx.bake_batch(jobs, plist[0])
+    assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
+    # a single fused bake with the tuned knobs bakes the same bits too
+    j = w["jobs"][1]
+    assert np.array_equal(ctx.bake(j["scene"], j["probes"], plist[1]), ref[1])
+
+
 def test_batch_job_vs_oracle(ctx, batch_world):
     """One batched job (300 boxes, 33 probes) against the FP64 oracle, FP32 path."""
     w = batch_world
@@ -135,8 +172,8 @@ def test_batch_invalid(ctx, batch_world):
     with pytest.raises(vlb.VlbError):
         ctx.bake_batch([(j["scene"], j["probes"], None, pf)], p2)
     assert ctx.bake_batch([], p2) == []
-    # FUSED bakes as FP32 in a batch
+    # a FUSED batch of one job is the fused single bake
     pu = _job_params(w, j, 2, vlb.PREC_FUSED)
     a = ctx.bake_batch([(j["scene"], j["probes"], None)], pu)[0]
-    b = ctx.bake(j["scene"], j["probes"], _job_params(w, j, 2, vlb.PREC_FP32))
+    b = ctx.bake(j["scene"], j["probes"], pu)
     assert np.array_equal(a, b)

@@ -105,6 +105,37 @@ def test_project_bf16_tensor_core_matches_oracle(ctx, lmax, nprobes, S):
     assert np.isfinite(got).all()
 
 
+def _split_bf16(torch, rad):
+    """FP32 samples [n, 3, S] -> hi/lo BF16 pairs [n, 3, 2S] (hi, then the rounding of the remainder)."""
+    hi = rad.to(torch.bfloat16)
+    lo = (rad - hi.float()).to(torch.bfloat16)
+    return torch.cat([hi, lo], dim=2).contiguous()
+
+
+@pytest.mark.parametrize("lmax", [2, 3])
+@pytest.mark.parametrize("nprobes,S", [(1, 64), (300, 1024), (5, 100), (7, 30001), (50_000, 256)])
+def test_project_bf16_split_matches_fp32_oracle(ctx, lmax, nprobes, S):
+    """Hi/lo BF16 pairs (the mixed-precision tile): tensor cores for S % 4 == 0
+    (K = 2S against the split basis), CUDA cores otherwise.  The pair keeps
+    ~16 mantissa bits of each FP32 sample, so the result is within 2e-5 of the
+    FP64 projection of the FP32 samples themselves."""
+    torch = pytest.importorskip("torch")
+    ds = ctx.fibonacci(S)
+    d, w = O.dirs_fibonacci(S)
+    B = O.basis_matrix(d.astype(np.float64), w, lmax)
+    g = torch.Generator().manual_seed(3 * nprobes + S + lmax)
+    rad = torch.rand((nprobes, 3, S), generator=g) * 5
+    dev = _split_bf16(torch, rad).cuda().view(torch.int16)
+    out = torch.empty((nprobes, vlb.k_of(lmax), 3), dtype=torch.float32, device="cuda")
+    ctx.project(dev, nprobes, ds, lmax, dtype=vlb.DTYPE_BF16_SPLIT, out=out)
+    ctx.synchronize()
+    got = out.cpu().numpy()
+    m = min(nprobes, 2000)
+    ref = O.project(rad[:m].numpy(), m, S, B)
+    assert rel(got[:m], ref) < 2e-5
+    assert np.isfinite(got).all()
+
+
 def test_sh_eval_matches_reference_golden(ctx, golden):
     w, h = (int(v) for v in golden["recon_wh"])
     got = ctx.sh_eval_envmap(golden["coeffs"], 3, w, h, 1250.0)

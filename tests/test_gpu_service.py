@@ -37,7 +37,7 @@ def _params(w, S, sun, prec=vlb.PREC_MIXED, lmax=2, intensity=5.0):
     return vlb.bake_params(w["dsets"][S], lmax, prec, sun, sun_intensity=intensity, sky=w["sky"])
 
 
-@pytest.mark.parametrize("prec", [vlb.PREC_MIXED, vlb.PREC_FP32])
+@pytest.mark.parametrize("prec", [vlb.PREC_MIXED, vlb.PREC_FP32, vlb.PREC_FUSED, vlb.PREC_BF16])
 def test_service_matches_bake(ctx, world, prec):
     w = world
     svc = vlb.Service(ctx, lmax=2, precision=prec, max_batch_probes=3000)

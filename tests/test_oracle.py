@@ -245,3 +245,16 @@ def test_probe_eval_oracle_indexes_the_bake_grid_order():
                 den += w
             exp[i] = num / den
         assert np.allclose(out[:, 0], exp, rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("seed,nboxes", [(1, 64), (1, 4096), (7, 0), (31, 700)])
+def test_oracle_workload_generators_match_library(seed, nboxes):
+    """The oracle's restated seeded generators (the CPU baseline builds its
+    inputs with them, without the product library) give the library's inputs
+    bit for bit."""
+    import vlb
+
+    for a, b in zip(O.synth_box_scene(seed, nboxes), vlb.synth_box_scene(seed, nboxes)):
+        assert a.dtype == b.dtype and np.array_equal(a.reshape(b.shape), b)
+    assert np.array_equal(O.synth_cubemap(seed, 32).reshape(-1), vlb.synth_cubemap(seed, 32).reshape(-1))
+    assert np.array_equal(O.synth_sun(seed), vlb.synth_sun(seed))

@@ -19,7 +19,7 @@
 //   --lmax 2|3           coefficients 9 or 16 (default 3, the file's layout)
 //   --sun X Y Z          direction toward the sun (default 0 1 0)
 //   --intensity I        sun intensity (default 5)
-//   --precision fp32|fused|mixed   (default fused: FP32 arithmetic, fastest schedule)
+//   --precision fp32|fused|mixed|bf16   (default fused: FP32 arithmetic, one kernel)
 //   --out PATH           output file (default baked_<name> next to the input)
 //   --device N           CUDA device (default 0)
 #include <cstdio>
@@ -78,7 +78,8 @@ int main(int argc, char** argv) {
     if (fib ? std::sscanf(dirs.c_str() + 4, "%u", &dw) != 1
             : dirs.rfind("equirect:", 0) != 0 || std::sscanf(dirs.c_str() + 9, "%ux%u", &dw, &dh) != 2)
       throw std::runtime_error("bad --dirs " + dirs);
-    if (prec != "fp32" && prec != "fused" && prec != "mixed") throw std::runtime_error("bad --precision " + prec);
+    if (prec != "fp32" && prec != "fused" && prec != "mixed" && prec != "bf16")
+      throw std::runtime_error("bad --precision " + prec);
     const std::string src = read_text(in);  // the document re-written after the bake
     if (src.compare(0, 4, "glTF") == 0)
       throw std::runtime_error("binary glTF input: the baked file is written from a JSON .gltf document");
@@ -110,7 +111,10 @@ int main(int argc, char** argv) {
     vlb_bake_params p;
     vlb_bake_params_default(&p);
     p.lmax = lmax;
-    p.precision = prec == "fp32" ? VLB_PREC_FP32 : prec == "mixed" ? VLB_PREC_MIXED : VLB_PREC_FUSED;
+    p.precision = prec == "fp32"    ? VLB_PREC_FP32
+                  : prec == "mixed" ? VLB_PREC_MIXED
+                  : prec == "bf16"  ? VLB_PREC_BF16
+                                    : VLB_PREC_FUSED;
     for (int a = 0; a < 3; ++a) p.sun_dir[a] = sun[a];
     p.sun_intensity = intensity;
     p.dirs = ds;

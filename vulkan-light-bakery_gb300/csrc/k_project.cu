@@ -2,8 +2,9 @@
 // (shaders/sh.comp:23-42 for a sample set shared by all probes) and the
 // reconstruction of shaders/sh_sum.comp:35-52.
 //
-// Tile layout: row r = probe*3 + channel, S samples contiguous per row.  The
-// basis table is S x 16 FP32 with the sample weight folded in.  One thread
+// Tile layout: row r = probe*3 + channel, S samples contiguous per row (a
+// BF16 tile of hi/lo pairs holds 2S per row: S high parts, then S low parts;
+// the sample is their sum).  The basis table is S x 16 FP32 with the sample weight folded in.  One thread
 // owns one row; a CTA stages a [128 rows x 64 samples] block of the tile in
 // shared memory with coalesced row-segment copies (cp.async for FP32, so a
 // thread's copies are all in flight at once; rows padded to 65 words so the
@@ -54,7 +55,7 @@ static_assert(kProjTileWords % 4 == 0, "basis block must stay 16-byte aligned");
 template <typename T>
 __device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_t rows, uint32_t S, uint32_t s_end,
                                               const float* __restrict__ basis16, uint32_t row0, uint32_t s0,
-                                              float* stage) {
+                                              float* stage, uint32_t split) {
   float(*tile)[kProjCols + 1] = reinterpret_cast<float(*)[kProjCols + 1]>(stage);
   float(*bas)[16] = reinterpret_cast<float(*)[16]>(stage + kProjTileWords);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -82,7 +83,14 @@ __device__ __forceinline__ void project_stage(const T* __restrict__ rad, uint32_
       for (int h = 0; h < kProjCols / 32; ++h) {
         const uint32_t c = h * 32 + lane;
         float v = 0.f;
-        if (gr < rows && c < ns) v = to_f32<T>(rad[size_t(gr) * S + s0 + c]);
+        if (gr < rows && c < ns) {
+          if (split) {  // hi/lo pair: [rows][2S]
+            const size_t r0 = size_t(gr) * 2 * S;
+            v = to_f32<T>(rad[r0 + s0 + c]) + to_f32<T>(rad[r0 + S + s0 + c]);
+          } else {
+            v = to_f32<T>(rad[size_t(gr) * S + s0 + c]);
+          }
+        }
         tile[rr][c] = v;
       }
     }
@@ -124,7 +132,8 @@ size_t project_partial_bytes(uint32_t nprobes, uint32_t S, uint32_t K) {
 template <typename T, int K>
 __global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad, uint32_t rows, uint32_t S,
                                                        uint32_t per, const float* __restrict__ basis16,
-                                                       float* __restrict__ out, float* __restrict__ partial) {
+                                                       float* __restrict__ out, float* __restrict__ partial,
+                                                       uint32_t split) {
   __shared__ __align__(16) float stage[kProjStageWords];
   const float(*tile)[kProjCols + 1] = reinterpret_cast<const float(*)[kProjCols + 1]>(stage);
   const float(*bas)[16] = reinterpret_cast<const float(*)[16]>(stage + kProjTileWords);
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(kProjRows) k_project(const T* __restrict__ rad
   for (int k = 0; k < K; ++k) acc[k] = 0.f;
 
   for (uint32_t s0 = s_begin; s0 < s_end; s0 += kProjCols) {
-    project_stage<T>(rad, rows, S, s_end, basis16, row0, s0, stage);
+    project_stage<T>(rad, rows, S, s_end, basis16, row0, s0, stage, split);
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 #pragma unroll 4
@@ -180,7 +189,7 @@ __global__ void k_project_reduce(const float* __restrict__ partial, uint32_t spl
 
 template <typename T>
 static void launch_project(const T* rad, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K, float* out,
-                           float* partial, cudaStream_t s) {
+                           float* partial, uint32_t split, cudaStream_t s) {
   const uint32_t rows = nprobes * 3;
   const uint32_t tiles = (rows + kProjRows - 1) / kProjRows;
   if (tiles == 0) return;
@@ -188,19 +197,19 @@ static void launch_project(const T* rad, uint32_t nprobes, uint32_t S, const flo
   const uint32_t splits = S ? project_splits(rows, S, &per) : 1;
   if (!S) per = 0;
   const dim3 grid(tiles, splits);
-  if (K == 9) k_project<T, 9><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial);
-  else k_project<T, 16><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial);
+  if (K == 9) k_project<T, 9><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial, split);
+  else k_project<T, 16><<<grid, kProjRows, 0, s>>>(rad, rows, S, per, basis16, out, partial, split);
   if (splits > 1) k_project_reduce<<<(rows * K + 255) / 256, 256, 0, s>>>(partial, splits, rows, K, out);
 }
 
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
                         float* out, float* partial, cudaStream_t s) {
-  launch_project<float>(radiance, nprobes, S, basis16, K, out, partial, s);
+  launch_project<float>(radiance, nprobes, S, basis16, K, out, partial, 0, s);
 }
 
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
-                              uint32_t K, float* out, float* partial, cudaStream_t s) {
-  launch_project<uint16_t>(radiance, nprobes, S, basis16, K, out, partial, s);
+                              uint32_t K, float* out, float* partial, uint32_t split, cudaStream_t s) {
+  launch_project<uint16_t>(radiance, nprobes, S, basis16, K, out, partial, split, s);
 }
 
 // sh_sum.comp:35-52 -- one thread per pixel, direction from the per-column

@@ -22,8 +22,9 @@
 // used when a batch needs room; the host copy of the probes stays, so a
 // relight of an evicted set bakes in full with the same result.
 //
-// Budget accounting: device bytes of the batches in flight (radiance tile,
-// outputs, probe and sort scratch) plus the resident kept sets.
+// Budget accounting: device bytes of the batches in flight (radiance tile or
+// fused chunk partials, outputs, probe and sort scratch) plus the resident
+// kept sets.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,9 +58,18 @@ vlb_status sfail(vlb_status st, const std::string& msg) {
   return st;
 }
 
-// Device bytes a batch holds for one request while it runs.
-uint64_t transient_bytes(uint64_t n, uint64_t S, uint32_t K, bool bf16) {
-  return n * S * 3 * (bf16 ? 2 : 4) + n * (12 + 4 + 16 + uint64_t(K) * 12);
+// Device bytes a batch holds for one request while it runs: the radiance
+// tile (FP32, BF16 hi/lo pairs or one BF16), or for the fused walk its chunk
+// partials and tickets.
+uint64_t transient_bytes(uint64_t n, uint64_t S, uint32_t K, uint32_t prec) {
+  uint64_t work;
+  if (prec == VLB_PREC_FUSED) {
+    const uint64_t D = vlbk::fused_chunk_rays(uint32_t(S)), C = (S + D - 1) / D;
+    work = n * ((C > 1 ? C * 3 * K * 4 : 0) + 4);
+  } else {
+    work = n * S * 3 * (prec == VLB_PREC_BF16 ? 2 : 4);
+  }
+  return work + n * (12 + 4 + 16 + uint64_t(K) * 12);
 }
 // Device bytes of a kept-hit set.
 uint64_t hitset_bytes(uint64_t n, uint64_t S) { return n * S * 8 + n * 12; }
@@ -119,7 +129,6 @@ struct vlb_service {
   vlb_ctx* user = nullptr;
   vlb_ctx* ctx = nullptr;  // private context: own stream, accepts the user's objects
   vlb_service_config cfg{};
-  bool bf16 = false;
   uint32_t K = 9;
 
   std::mutex mu;
@@ -189,7 +198,7 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
     }
     const uint32_t n = src ? src->n : r->n;
     const uint32_t S = src ? src->dirs->n : r->params.dirs->n;
-    uint64_t b = transient_bytes(n, S, K, bf16);
+    uint64_t b = transient_bytes(n, S, K, cfg.precision);
     if (r->keep && !r->relight_of) b += hitset_bytes(n, S);
     // room: budget minus what is held; evict unused kept sets (LRU) if the head does not fit
     auto room = [&]() { return budget > set_bytes + flight_bytes ? budget - set_bytes - flight_bytes : 0; };
@@ -438,8 +447,7 @@ vlb_status vlb_service_create(vlb_ctx* ctx, const vlb_service_config* cfg, vlb_s
   vlb_service_config c = cfg ? *cfg : vlb_service_config{};
   if (c.lmax == 0) c.lmax = 2;
   if (c.lmax != 2 && c.lmax != 3) return sfail(VLB_ERR_INVALID, "service lmax must be 2 or 3");
-  if (c.precision > VLB_PREC_MIXED) return sfail(VLB_ERR_INVALID, "service precision must be FP32, FUSED or MIXED");
-  if (c.precision == VLB_PREC_FUSED) c.precision = VLB_PREC_FP32;
+  if (c.precision > VLB_PREC_BF16) return sfail(VLB_ERR_INVALID, "service precision must be a vlb_precision");
   if (!c.hbm_budget_bytes) c.hbm_budget_bytes = kDefaultBudget;
   if (!c.max_batch_probes) c.max_batch_probes = kDefaultMaxProbes;
   if (!c.max_inflight) c.max_inflight = kDefaultInflight;
@@ -452,7 +460,6 @@ vlb_status vlb_service_create(vlb_ctx* ctx, const vlb_service_config* cfg, vlb_s
   s->user = ctx;
   s->ctx = priv;
   s->cfg = c;
-  s->bf16 = c.precision == VLB_PREC_MIXED;
   s->K = svc_k(c.lmax);
   s->worker = std::thread([s] { s->run(); });
   *out = s;
@@ -510,7 +517,7 @@ vlb_status vlb_service_submit(vlb_service* s, const vlb_request* q, uint64_t* ti
   const double sl = double(r->params.sun_dir[0]) * r->params.sun_dir[0] +
                     double(r->params.sun_dir[1]) * r->params.sun_dir[1] + double(r->params.sun_dir[2]) * r->params.sun_dir[2];
   if (!(sl > 0.0)) return sfail(VLB_ERR_INVALID, "sun direction must be non-zero");
-  uint64_t need = transient_bytes(n, S, s->K, s->bf16) + (r->keep ? hitset_bytes(n, S) : 0);
+  uint64_t need = transient_bytes(n, S, s->K, s->cfg.precision) + (r->keep ? hitset_bytes(n, S) : 0);
   if (need > s->cfg.hbm_budget_bytes) {
     return sfail(VLB_ERR_OOM, "request exceeds the service's device-memory budget");
   }

@@ -1,0 +1,553 @@
+// trace_common.cuh -- device pieces shared by the trace kernels (k_trace.cu,
+// k_trace_fused.cu): ray setup, box and triangle tests, the packet and
+// per-lane BVH walks, shading of a primary hit, and the per-lane ray state
+// machine of the lane walks.  See k_trace.cu for the traversal rules (the
+// pruning margin, the tie rule) that make every ray's result independent of
+// the walk that finds it.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include <climits>
+
+#include "vlb_device.cuh"
+#include "vlb_internal.h"
+
+namespace vlbk {
+constexpr int kTraceThreads = kTraceWarps * 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct RayCtx {
+  float ox, oy, oz, dx, dy, dz;
+  float ix, iy, iz;     // 1 / d (zero components nudged to 1e-30)
+  float oix, oiy, oiz;  // o * inv
+};
+
+struct Work {
+  uint32_t wnodes = 0, wtris = 0, shadow = 0, lnodes = 0;
+};
+
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+__device__ __forceinline__ float safe_inv(float d) {
+  return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
+}
+
+__device__ __forceinline__ void make_ray(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz) {
+  r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
+  r.ix = safe_inv(dx); r.iy = safe_inv(dy); r.iz = safe_inv(dz);
+  r.oix = ox * r.ix; r.oiy = oy * r.iy; r.oiz = oz * r.iz;
+}
+
+// make_ray with the reciprocals of d precomputed (host_safe_inv: the same bits).
+__device__ __forceinline__ void make_ray_inv(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz,
+                                             float ix, float iy, float iz) {
+  r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
+  r.ix = ix; r.iy = iy; r.iz = iz;
+  r.oix = ox * ix; r.oiy = oy * iy; r.oiz = oz * iz;
+}
+
+// Slab test for a ray in octant OCT (bit a set: 1/d_a < 0).  The octant is
+// the same for every lane of a packet (one direction per packet), so the
+// entry and exit planes of each axis are chosen at compile time and no
+// per-axis min/max is needed.
+template <int OCT>
+__device__ __forceinline__ bool slab(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                     float tmin, float tmax, float* tnear) {
+  const float tnx = fmaf((OCT & 1) ? hx : lx, r.ix, -r.oix), tfx = fmaf((OCT & 1) ? lx : hx, r.ix, -r.oix);
+  const float tny = fmaf((OCT & 2) ? hy : ly, r.iy, -r.oiy), tfy = fmaf((OCT & 2) ? ly : hy, r.iy, -r.oiy);
+  const float tnz = fmaf((OCT & 4) ? hz : lz, r.iz, -r.oiz), tfz = fmaf((OCT & 4) ? lz : hz, r.iz, -r.oiz);
+  const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
+  const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
+  *tnear = tn;
+  return tn <= tf;
+}
+
+__device__ __forceinline__ int octant_of(float dx, float dy, float dz) {
+  return (safe_inv(dx) < 0.f ? 1 : 0) | (safe_inv(dy) < 0.f ? 2 : 0) | (safe_inv(dz) < 0.f ? 4 : 0);
+}
+
+// Moller-Trumbore, inclusive edges; returns t or -1.
+__device__ __forceinline__ float tri_hit(const RayCtx& r, const float4 v0, const float4 e1, const float4 e2) {
+  const float px = r.dy * e2.z - r.dz * e2.y, py = r.dz * e2.x - r.dx * e2.z, pz = r.dx * e2.y - r.dy * e2.x;
+  const float det = e1.x * px + e1.y * py + e1.z * pz;
+  if (det == 0.f) return -1.f;
+  const float inv = 1.0f / det;
+  const float sx = r.ox - v0.x, sy = r.oy - v0.y, sz = r.oz - v0.z;
+  const float u = (sx * px + sy * py + sz * pz) * inv;
+  if (u < 0.f || u > 1.f) return -1.f;
+  const float qx = sy * e1.z - sz * e1.y, qy = sz * e1.x - sx * e1.z, qz = sx * e1.y - sy * e1.x;
+  const float v = (r.dx * qx + r.dy * qy + r.dz * qz) * inv;
+  if (v < 0.f || u + v > 1.f) return -1.f;
+  return (e2.x * qx + e2.y * qy + e2.z * qz) * inv;
+}
+
+// Far limit of the box tests: the best distance so far plus a relative 2^-12.
+__device__ __forceinline__ float prune_limit(float tbest) { return fmaf(tbest, 0x1p-12f, tbest); }
+
+// Warp-uniform stack of up to kTraceStack (64) node references held in two
+// registers per lane: entry i sits in lane i % 32, register i / 32, together
+// with the ballot of the lanes whose own box test accepted that subtree.
+struct WarpStack {
+  int r0 = 0, r1 = 0, sp = 0;
+  unsigned m0 = 0, m1 = 0;
+  __device__ __forceinline__ void push(int v, unsigned lanes, uint32_t lane, int* err) {
+    if (sp >= kTraceStack) {
+      if (lane == 0) atomicAdd(err + kErrStackOverflow, 1);
+      return;
+    }
+    if (lane == uint32_t(sp & 31)) {
+      if (sp < 32) { r0 = v; m0 = lanes; } else { r1 = v; m1 = lanes; }
+    }
+    ++sp;
+  }
+  __device__ __forceinline__ int pop(bool& mine, uint32_t lane) {
+    --sp;
+    const bool lo = sp < 32;
+    const int v = __shfl_sync(kFull, lo ? r0 : r1, sp & 31);
+    const unsigned m = __shfl_sync(kFull, lo ? m0 : m1, sp & 31);
+    mine = (m >> lane) & 1u;
+    return v;
+  }
+};
+
+// Warp-cooperative traversal.  ANY = false: closest hit in (tmin, tbest)
+// with ties to the lower triangle id; ANY = true: a lane stops (active =
+// false, best_slot >= 0) at its first hit in (tmin, tbest).  Must be called
+// by all 32 lanes; lanes with active == false only vote "no".  OCT is the
+// packet's (warp-uniform) ray octant.  A lane tests a node or triangle only
+// inside subtrees its own box tests accepted (`in`), so it visits exactly the
+// nodes its own walk would, in the warp's order: its result does not depend
+// on the other rays of the packet.
+template <int OCT, bool ANY, bool COUNT>
+__device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, const float4* __restrict__ nodes,
+                                                const float4* __restrict__ tris, uint32_t ntris, float tmin,
+                                                float& tbest, int& best_slot, int& best_id, int* err, Work& w) {
+  if (ntris == 0 || !__any_sync(kFull, active)) return;
+  const uint32_t lane = threadIdx.x & 31;
+  WarpStack st;
+  int cur = ntris > 1 ? 0 : ~0;
+  bool in = true;
+  for (;;) {
+    const bool test = active && in;
+    if (cur >= 0) {
+      if constexpr (COUNT) { w.wnodes += lane == 0; w.lnodes += test; }
+      const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
+                   n3 = __ldg(nodes + 4 * cur + 3);
+      bool h0 = false, h1 = false;
+      float tn0 = 0.f, tn1 = 0.f;
+      if (test) {
+        const float lim = prune_limit(tbest);
+        h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
+        h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
+      }
+      const unsigned b0 = __ballot_sync(kFull, h0), b1 = __ballot_sync(kFull, h1);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (b0 && b1) {
+        bool first0 = true;
+        if constexpr (!ANY) {
+          // visit first the child most lanes reach first (efficiency only)
+          const unsigned pref0 = __ballot_sync(kFull, h0 && (!h1 || tn0 <= tn1));
+          first0 = 2 * __popc(pref0) >= __popc(b0 | b1);
+        }
+        st.push(first0 ? c1 : c0, first0 ? b1 : b0, lane, err);
+        cur = first0 ? c0 : c1;
+        in = first0 ? h0 : h1;
+        continue;
+      }
+      if (b0) { cur = c0; in = h0; continue; }
+      if (b1) { cur = c1; in = h1; continue; }
+    } else {
+      if constexpr (COUNT) w.wtris += lane == 0;
+      const int slot = ~cur;
+      const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
+      if (test) {
+        const float t = tri_hit(r, v0, e1, e2);
+        if (t > tmin) {
+          if constexpr (ANY) {
+            if (t < tbest) { best_slot = slot; active = false; }
+          } else {
+            const int id = __float_as_int(v0.w);
+            if (t < tbest || (t == tbest && best_slot >= 0 && id < best_id)) { tbest = t; best_slot = slot; best_id = id; }
+          }
+        }
+      }
+      if constexpr (ANY) {
+        if (!__any_sync(kFull, active)) break;
+      }
+    }
+    if (st.sp == 0) break;
+    cur = st.pop(in, lane);
+  }
+}
+
+// Per-lane traversal (lane mode): the same tests and tie rule as the packet
+// walk, the lane's own stack (local memory), nearer child first.  Lanes with
+// active == false return at once; no warp collectives.
+template <int OCT, bool ANY, bool COUNT>
+__device__ __forceinline__ void lane_traverse(const RayCtx& r, bool& active, const float4* __restrict__ nodes,
+                                              const float4* __restrict__ tris, uint32_t ntris, float tmin,
+                                              float& tbest, int& best_slot, int& best_id, int* err, Work& w) {
+  if (ntris == 0 || !active) return;
+  int stack[kTraceStack];
+  int sp = 0;
+  int cur = ntris > 1 ? 0 : ~0;
+  for (;;) {
+    if (cur >= 0) {
+      if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+      const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
+                   n3 = __ldg(nodes + 4 * cur + 3);
+      float tn0, tn1;
+      const float lim = prune_limit(tbest);
+      const bool h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
+      const bool h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
+      const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+      if (h0 && h1) {
+        const bool first0 = tn0 <= tn1;
+        if (sp < kTraceStack) stack[sp++] = first0 ? c1 : c0;
+        else atomicAdd(err + kErrStackOverflow, 1);
+        cur = first0 ? c0 : c1;
+        continue;
+      }
+      if (h0) { cur = c0; continue; }
+      if (h1) { cur = c1; continue; }
+    } else {
+      if constexpr (COUNT) ++w.wtris;
+      const int slot = ~cur;
+      const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
+      const float t = tri_hit(r, v0, e1, e2);
+      if (t > tmin) {
+        if constexpr (ANY) {
+          if (t < tbest) { best_slot = slot; active = false; return; }
+        } else {
+          const int id = __float_as_int(v0.w);
+          if (t < tbest || (t == tbest && best_slot >= 0 && id < best_id)) { tbest = t; best_slot = slot; best_id = id; }
+        }
+      }
+    }
+    if (sp == 0) break;
+    cur = stack[--sp];
+  }
+}
+
+// Dispatch on the packet's octant (a warp-uniform branch) and the mode.
+template <bool ANY, bool COUNT, bool LANE>
+__device__ __forceinline__ void traverse(int oct, const RayCtx& r, bool& active, const float4* __restrict__ nodes,
+                                         const float4* __restrict__ tris, uint32_t ntris, float tmin, float& tbest,
+                                         int& best_slot, int& best_id, int* err, Work& w) {
+#define VLB_OCT(o)                                                                                                \
+  case o:                                                                                                         \
+    if constexpr (LANE) lane_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot,       \
+                                                     best_id, err, w);                                            \
+    else packet_traverse<o, ANY, COUNT>(r, active, nodes, tris, ntris, tmin, tbest, best_slot, best_id, err, w); \
+    break;
+  switch (oct) {
+    VLB_OCT(0) VLB_OCT(1) VLB_OCT(2) VLB_OCT(3) VLB_OCT(4) VLB_OCT(5) VLB_OCT(6) VLB_OCT(7)
+  }
+#undef VLB_OCT
+}
+
+// Nearest cubemap texel; each step one IEEE FP32 operation (matches the
+// oracle's texel choice exactly).
+__device__ __forceinline__ uint32_t cube_texel(float x, float y, float z, uint32_t n) {
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  float sc, tc, ma;
+  uint32_t f;
+  if (ax >= ay && ax >= az) {
+    if (x >= 0.f) { f = 0; sc = -z; tc = -y; } else { f = 1; sc = z; tc = -y; }
+    ma = ax;
+  } else if (ay >= az) {
+    if (y >= 0.f) { f = 2; sc = x; tc = z; } else { f = 3; sc = x; tc = -z; }
+    ma = ay;
+  } else {
+    if (z >= 0.f) { f = 4; sc = x; tc = -y; } else { f = 5; sc = -x; tc = -y; }
+    ma = az;
+  }
+  const float fn = float(n);
+  const float fu = __fmul_rn(__fmul_rn(__fadd_rn(__fdiv_rn(sc, ma), 1.0f), 0.5f), fn);
+  const float fv = __fmul_rn(__fmul_rn(__fadd_rn(__fdiv_rn(tc, ma), 1.0f), 0.5f), fn);
+  const int ix = min(max(int(floorf(fu)), 0), int(n) - 1);
+  const int iy = min(max(int(floorf(fv)), 0), int(n) - 1);
+  return (f * n + uint32_t(iy)) * n + uint32_t(ix);
+}
+
+// One radiance sample into a BF16 tile row.  Plain: [rows][S], the BF16
+// rounding of v.  Split (hi/lo): [rows][2S], the rounding hi at column s and
+// the rounding of the remainder v - hi at column S + s; hi + lo carries ~16
+// mantissa bits of v.
+__device__ __forceinline__ void store_bf16(uint16_t* __restrict__ t, size_t row, uint32_t S, uint32_t s, float v,
+                                           uint32_t split) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  if (!split) {
+    t[row * S + s] = __bfloat16_as_ushort(hi);
+    return;
+  }
+  const size_t r0 = row * 2 * size_t(S);
+  t[r0 + s] = __bfloat16_as_ushort(hi);
+  t[r0 + S + s] = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(hi)));
+}
+
+struct Shaded {
+  float r, g, b;
+  int tri;      // original triangle id or -1
+  uint8_t vis;  // 0 occluded, 1 lit, 2 no shadow ray
+};
+
+// One sample for the whole warp: primary packet, shading, shadow packet.
+// A: any type with the scene and shading fields of TraceArgs (nodes, tris,
+// albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
+// Primary ray: closest hit -> (slot, id, t); slot -1 on a miss.
+template <bool COUNT, bool LANE, class A>
+__device__ __forceinline__ void primary_hit(const A& a, bool valid, const RayCtx& ray, const float4 d, int& slot,
+                                            int& id, float& tb, Work& w) {
+  bool act = valid;
+  tb = a.tmax;
+  slot = -1;
+  id = -1;
+  traverse<false, COUNT, LANE>(octant_of(d.x, d.y, d.z), ray, act, a.nodes, a.tris, a.ntris, a.tmin, tb, slot, id,
+                               a.err, w);
+}
+
+// Shading of a primary result: sky on a miss; at a hit the sun shadow ray
+// (any hit) and Lambert.  Called by all 32 lanes (the shadow walk may be a
+// packet walk).
+template <bool COUNT, bool LANE, class A>
+__device__ __forceinline__ Shaded shade_hit(const A& a, bool valid, const RayCtx& ray, float ox, float oy, float oz,
+                                            const float4 d, int slot, int id, float tb, Work& w) {
+  Shaded o{0.f, 0.f, 0.f, -1, 2};
+  RayCtx sh = ray;
+  bool need = false;
+  float ndl = 0.f;
+  if (valid) {
+    if (slot < 0) {
+      if (a.sky) {
+        const float* tx = a.sky + 3 * size_t(cube_texel(d.x, d.y, d.z, a.sky_n));
+        o.r = __ldg(tx); o.g = __ldg(tx + 1); o.b = __ldg(tx + 2);
+      }
+    } else {
+      const float4 e1 = __ldg(a.tris + 3 * slot + 1), e2 = __ldg(a.tris + 3 * slot + 2);
+      o.tri = id;
+      float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+      const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
+      nx *= rn; ny *= rn; nz *= rn;
+      if (nx * d.x + ny * d.y + nz * d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
+      ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
+      if (ndl > 0.f) {
+        need = true;
+        make_ray(sh, fmaf(tb, d.x, ox) + a.bias * nx, fmaf(tb, d.y, oy) + a.bias * ny, fmaf(tb, d.z, oz) + a.bias * nz,
+                 a.sun.x, a.sun.y, a.sun.z);
+      }
+    }
+  }
+  if constexpr (COUNT) w.shadow += need;
+  bool sact = need;
+  float stb = a.tmax;
+  int sslot = -1, sid = -1;
+  // inactive lanes keep their primary ray: the octant comes from the sun, uniform
+  traverse<true, COUNT, LANE>(octant_of(a.sun.x, a.sun.y, a.sun.z), sh, sact, a.nodes, a.tris, a.ntris, 0.0f, stb,
+                              sslot, sid, a.err, w);
+  if (need) {
+    const bool occ = sslot >= 0;
+    o.vis = occ ? 0 : 1;
+    if (!occ) {
+      const float k = a.sun_scale * ndl;
+      const float4 alb = __ldg(a.albedo + o.tri);
+      o.r = alb.x * k; o.g = alb.y * k; o.b = alb.z * k;
+    }
+  }
+  return o;
+}
+
+// One sample for the whole warp: primary walk, shading, shadow walk.
+// A: any type with the scene and shading fields of TraceArgs (nodes, tris,
+// albedo, ntris, tmin, tmax, bias, sun, sun_scale, sky, sky_n, err).
+template <bool COUNT, bool LANE, class A>
+__device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox, float oy, float oz, const float4 d,
+                                               Work& w) {
+  RayCtx ray;
+  make_ray(ray, ox, oy, oz, d.x, d.y, d.z);
+  int slot, id;
+  float tb;
+  primary_hit<COUNT, LANE>(a, valid, ray, d, slot, id, tb, w);
+  return shade_hit<COUNT, LANE>(a, valid, ray, ox, oy, oz, d, slot, id, tb, w);
+}
+
+
+// ---- per-lane ray state machine (the lane walks) ------------------------------------
+// Box test with the octant taken per lane at run time (the lane walks mix
+// directions within a warp).
+__device__ __forceinline__ bool slab_rt(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                        float tmin, float tmax, float* tnear) {
+  const float ax = fmaf(lx, r.ix, -r.oix), bx = fmaf(hx, r.ix, -r.oix);
+  const float ay = fmaf(ly, r.iy, -r.oiy), by = fmaf(hy, r.iy, -r.oiy);
+  const float az = fmaf(lz, r.iz, -r.oiz), bz = fmaf(hz, r.iz, -r.oiz);
+  const float tn = fmax3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
+  const float tf = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+  *tnear = tn;
+  return tn <= tf;
+}
+
+__device__ __forceinline__ uint32_t lane_lt_mask() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// One lane's ray: its walk and the pending shading of its primary hit.
+// cur: the next node (>= 0), triangle slot ~cur, or kWalkEnd; leaf: a
+// triangle slot parked for the next leaf phase (-1 none).
+constexpr int kWalkEnd = INT_MIN;
+// First step of a walk: the root node, the one triangle of a one-triangle
+// scene, or nothing in an empty scene.
+__device__ __forceinline__ int walk_root(uint32_t ntris) { return ntris > 1 ? 0 : (ntris == 1 ? ~0 : kWalkEnd); }
+struct LaneRay {
+  bool has = false, shadow = false;
+  uint32_t p = 0, s = 0;
+  float ox = 0.f, oy = 0.f, oz = 0.f;
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  RayCtx ray;
+  int cur = 0, sp = 0, slot = -1, id = -1, leaf = -1;
+  float tb = 0.f, lit = 0.f;
+};
+
+// A: TraceArgs or BakeJobDev (scene, shading, probes and dirs fields).
+template <class A>
+__device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uint32_t s) {
+  L.p = p;
+  L.s = s;
+  L.d = __ldg(a.dirs + s);
+  L.ox = a.probes[3 * size_t(p)];
+  L.oy = a.probes[3 * size_t(p) + 1];
+  L.oz = a.probes[3 * size_t(p) + 2];
+  const float4 inv = __ldg(a.dinv + s);
+  make_ray_inv(L.ray, L.ox, L.oy, L.oz, L.d.x, L.d.y, L.d.z, inv.x, inv.y, inv.z);
+  L.has = true;
+  L.shadow = false;
+  L.cur = walk_root(a.ntris);
+  L.sp = 0;
+  L.slot = -1;
+  L.id = -1;
+  L.leaf = -1;
+  L.tb = a.tmax;
+}
+
+// After a walk.  A finished primary walk is shaded: a miss takes the sky, a
+// lit-facing hit starts its shadow walk (returns false: the lane walks on,
+// the triangle id and sun term wait in id / lit), anything else is done.  A
+// finished shadow walk gives the Lambert term or 0.  Returns true with the
+// sample in `o` when the ray is complete.
+template <bool COUNT, class A>
+__device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Work& w) {
+  o = Shaded{0.f, 0.f, 0.f, -1, 2};
+  if (!L.shadow) {
+    if (L.slot < 0) {
+      if (a.sky) {
+        const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
+        o.r = __ldg(tx); o.g = __ldg(tx + 1); o.b = __ldg(tx + 2);
+      }
+      return true;
+    }
+    const float4 e1 = __ldg(a.tris + 3 * L.slot + 1), e2 = __ldg(a.tris + 3 * L.slot + 2);
+    o.tri = L.id;
+    float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+    const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
+    nx *= rn; ny *= rn; nz *= rn;
+    if (nx * L.d.x + ny * L.d.y + nz * L.d.z > 0.f) { nx = -nx; ny = -ny; nz = -nz; }
+    const float ndl = nx * a.sun.x + ny * a.sun.y + nz * a.sun.z;
+    if (!(ndl > 0.f)) return true;
+    if constexpr (COUNT) ++w.shadow;
+    make_ray_inv(L.ray, fmaf(L.tb, L.d.x, L.ox) + a.bias * nx, fmaf(L.tb, L.d.y, L.oy) + a.bias * ny,
+                 fmaf(L.tb, L.d.z, L.oz) + a.bias * nz, a.sun.x, a.sun.y, a.sun.z, a.sun_inv.x, a.sun_inv.y,
+                 a.sun_inv.z);
+    L.lit = a.sun_scale * ndl;
+    L.shadow = true;
+    L.cur = walk_root(a.ntris);
+    L.sp = 0;
+    L.slot = -1;
+    L.tb = a.tmax;
+    return false;
+  }
+  o.tri = L.id;
+  const bool occ = L.slot >= 0;
+  o.vis = occ ? 0 : 1;
+  if (!occ) {
+    const float4 alb = __ldg(a.albedo + L.id);
+    o.r = alb.x * L.lit; o.g = alb.y * L.lit; o.b = alb.z * L.lit;
+  }
+  return true;
+}
+
+// Speculative while-while walk.  Run one step per turn, a warp's lanes at an
+// inner node and its lanes at a (single-triangle) leaf take different
+// branches nearly every turn.  Here a turn has a node phase -- every lane
+// walks inner nodes until it meets a leaf, parks it (one slot), and walks on
+// past it while other lanes of the warp still look for theirs -- and then a
+// leaf phase in which all parked triangles are tested together.  Only the
+// visiting order changes: box tests are conservative, pruning keeps a margin
+// and ties go to the lower triangle id, so every ray's result is unchanged.
+__device__ __forceinline__ bool lr_is_tri(int cur) { return cur < 0 && cur != kWalkEnd; }
+
+__device__ __forceinline__ void lr_park(LaneRay& L, const int* stack) {
+  if (L.has && L.leaf < 0 && lr_is_tri(L.cur)) {
+    L.leaf = ~L.cur;
+    L.cur = L.sp ? stack[--L.sp] : kWalkEnd;
+  }
+}
+
+// One inner node: nearer hit child next, the farther one on the stack.
+template <bool COUNT, class A>
+__device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work& w) {
+  if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
+               n2 = __ldg(a.nodes + 4 * L.cur + 2), n3 = __ldg(a.nodes + 4 * L.cur + 3);
+  float tn0, tn1;
+  const float lim = prune_limit(L.tb);
+  const bool h0 = slab_rt(L.ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
+  const bool h1 = slab_rt(L.ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
+  const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+  if (h0 && h1) {
+    const bool first0 = tn0 <= tn1;
+    if (L.sp < kTraceStack) stack[L.sp++] = first0 ? c1 : c0;
+    else atomicAdd(a.err + kErrStackOverflow, 1);
+    L.cur = first0 ? c0 : c1;
+  } else if (h0) {
+    L.cur = c0;
+  } else if (h1) {
+    L.cur = c1;
+  } else {
+    L.cur = L.sp ? stack[--L.sp] : kWalkEnd;
+  }
+}
+
+// The parked triangle; an occluder ends a shadow walk.
+template <bool COUNT, class A>
+__device__ __forceinline__ void lr_leaf(const A& a, LaneRay& L, Work& w) {
+  if constexpr (COUNT) ++w.wtris;
+  const int ts = L.leaf;
+  L.leaf = -1;
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
+  const float t = tri_hit(L.ray, v0, e1, e2);
+  if (!(t > tlo)) return;
+  if (L.shadow) {
+    if (t < L.tb) { L.slot = ts; L.cur = kWalkEnd; L.sp = 0; }
+    return;
+  }
+  const int tid = __float_as_int(v0.w);
+  if (t < L.tb || (t == L.tb && L.slot >= 0 && tid < L.id)) { L.tb = t; L.slot = ts; L.id = tid; }
+}
+
+constexpr int kNodeSteps = 6;   // bound on one turn's node phase
+constexpr int kRefillIdle = 16; // idle lanes that trigger a refill (all idle always does)
+
+}  // namespace vlbk

@@ -739,6 +739,7 @@ void vlb_dirset_destroy(vlb_dirset* d) {
   cudaFree(d->d_basis16);
   cudaFree(d->d_order);
   cudaFree(d->d_bt);
+  cudaFree(d->d_bt2);
   delete d;
 }
 
@@ -894,18 +895,52 @@ void vlb_bake_params_default(vlb_bake_params* p) {
   p->shadow_bias = 0.005f;
 }
 
+// The BF16 basis of a direction set for hi/lo split tiles ([32][2S]): built
+// on the host from the FP64 basis on first use (synchronous; never inside a
+// stream capture: callers make it before they enqueue).
+static vlb_status dirset_split_basis(vlb_ctx* ctx, const vlb_dirset* d) {
+  std::lock_guard<std::mutex> g(d->bt2_mu);
+  if (d->d_bt2) return VLB_OK;
+  const uint32_t n = d->n;
+  const uint32_t pitch = (2 * n + 7) / 8 * 8;
+  std::vector<uint16_t> bt(size_t(32) * pitch, 0);
+  parallel_ranges(n, 1 << 16, [&](size_t sb, size_t se) {
+    for (size_t s = sb; s < se; ++s)
+      for (int k = 0; k < 16; ++k) {
+        const double b = d->h_basis[s * 16 + k];
+        const uint16_t hi = bf16_rne(float(b));
+        const uint16_t lo = bf16_rne(float(b - double(bf16_to_float(hi))));
+        bt[size_t(k) * pitch + s] = hi;       // x radiance hi
+        bt[size_t(k) * pitch + n + s] = hi;   // x radiance lo
+        bt[size_t(16 + k) * pitch + s] = lo;  // x radiance hi (lo x lo is dropped)
+      }
+  });
+  uint16_t* dev = nullptr;
+  VLB_CUDA(ctx, cudaMalloc(&dev, bt.size() * 2));
+  const cudaError_t e = cudaMemcpy(dev, bt.data(), bt.size() * 2, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(dev); return cuda_fail(ctx, e, "split basis upload"); }
+  d->bt2_pitch = pitch;
+  d->d_bt2 = dev;
+  return VLB_OK;
+}
+
 // BF16 tile projection: the tcgen05 kernel when the tile meets its alignment
-// (S a multiple of 8, 16-byte aligned), else the CUDA-core kernel.
+// (columns a multiple of 8, 16-byte aligned), else the CUDA-core kernel.
+// split: the tile holds hi/lo pairs ([rows][2S]); the tensor-core form then
+// runs K = 2S against the split basis, so out = hi*bhi + lo*bhi + hi*blo.
 // `part_name`: the scratch for split partials (the batch path, whose launches
-// a CUDA graph may replay, keeps its own).
+// a CUDA graph may replay, keeps its own).  Split tiles need
+// dirset_split_basis first.
 static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprobes, const vlb_dirset* dirs,
-                               uint32_t K, float* out, const char* part_name = "project_partial") {
+                               uint32_t K, float* out, bool split, const char* part_name = "project_partial") {
   const uint32_t S = dirs->n;
-  if (vlbk::project_tc_supported(rad, S)) {
-    KScope k(ctx, "project_tc");
-    if (vlbk::launch_project_tc(rad, nprobes, S, dirs->d_bt, dirs->bt_pitch, K, out, ctx->d_err, ctx->num_sms,
-                                ctx->stream) < 0)
-      return fail(ctx, VLB_ERR_CUDA, "tensor map encoding failed for the BF16 projection");
+  if (vlbk::project_tc_supported(rad, split ? 2 * S : S) && (!split || dirs->d_bt2)) {
+    KScope k(ctx, split ? "project_tc_split" : "project_tc");
+    const int r = split ? vlbk::launch_project_tc(rad, nprobes, 2 * S, dirs->d_bt2, dirs->bt2_pitch, K, out,
+                                                  ctx->d_err, ctx->num_sms, ctx->stream)
+                        : vlbk::launch_project_tc(rad, nprobes, S, dirs->d_bt, dirs->bt_pitch, K, out, ctx->d_err,
+                                                  ctx->num_sms, ctx->stream);
+    if (r < 0) return fail(ctx, VLB_ERR_CUDA, "tensor map encoding failed for the BF16 projection");
     return VLB_OK;
   }
   void* part = nullptr;
@@ -915,7 +950,8 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
     if (st) return st;
   }
   KScope k(ctx, "project_bf16", pb ? 2 : 1);
-  vlbk::launch_project_bf16_simt(rad, nprobes, S, dirs->d_basis16, K, out, static_cast<float*>(part), ctx->stream);
+  vlbk::launch_project_bf16_simt(rad, nprobes, S, dirs->d_basis16, K, out, static_cast<float*>(part), split ? 1 : 0,
+                                 ctx->stream);
   return VLB_OK;
 }
 
@@ -969,7 +1005,7 @@ static vlb_status check_params(vlb_ctx* ctx, const vlb_scene* scene, const vlb_b
   if (!mine(scene->ctx) || !mine(p->dirs->ctx) || (p->sky && !mine(p->sky->ctx)))
     return fail(ctx, VLB_ERR_INVALID, "handles belong to another context");
   if (p->lmax != 2 && p->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", p->lmax);
-  if (p->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
+  if (p->precision > VLB_PREC_BF16) return fail(ctx, VLB_ERR_INVALID, "precision %u", p->precision);
   const double sl = std::sqrt(double(p->sun_dir[0]) * p->sun_dir[0] + double(p->sun_dir[1]) * p->sun_dir[1] +
                               double(p->sun_dir[2]) * p->sun_dir[2]);
   if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
@@ -1040,6 +1076,28 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   return VLB_OK;
 }
 
+// The fused walk's launch knobs of a schedule (0: the library default).
+static vlbk::FusedSched fused_sched(const vlb_batch_schedule& sc) {
+  vlbk::FusedSched f;
+  if (sc.ctas_per_sm) f.ctas_per_sm = sc.ctas_per_sm;
+  if (sc.node_steps) f.node_steps = sc.node_steps;
+  if (sc.refill_idle) f.refill_idle = sc.refill_idle;
+  return f;
+}
+
+// The scene, shading, probe and direction fields of one bake as a job of the
+// fused lane walk (the fused-projection fields are set by the caller).
+static void job_from_trace(const vlbk::TraceArgs& a, vlbk::BakeJobDev* j) {
+  j->nodes = a.nodes; j->tris = a.tris; j->albedo = a.albedo; j->ntris = a.ntris;
+  j->tmin = a.tmin; j->tmax = a.tmax; j->bias = a.bias;
+  j->sun = a.sun; j->sun_inv = a.sun_inv; j->sun_scale = a.sun_scale;
+  j->sky = a.sky; j->sky_n = a.sky_n; j->err = a.err;
+  j->probes = a.probes; j->order = const_cast<uint32_t*>(a.order); j->nprobes = a.nprobes;
+  j->dirs = a.dirs; j->dinv = a.dinv; j->dir_order = a.dir_order; j->S = a.S;
+  j->basis16 = a.basis16;
+  j->item_begin = 0;
+}
+
 vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_xyz, uint32_t nprobes,
                        const vlb_bake_params* p, float* out, const vlb_bake_debug* dbg) {
   if (!ctx) return VLB_ERR_INVALID;
@@ -1062,16 +1120,43 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     a.shadow = static_cast<uint8_t*>(os.dev);
     a.dbg_radiance = static_cast<float*>(orad.dev);
   }
-  // VLB_PREC_FUSED runs the one-kernel schedule for packet walks whose
-  // directions fit at most two work items per packet (large probe counts);
-  // lane walks (the default) and smaller bakes are faster through the
-  // radiance tile, which then stays in L2.
-  bool fused = p->precision == VLB_PREC_FUSED && !a.lane && a.chunks <= 2 && !a.dbg_radiance && !a.grid_hdr;
-  if (p->precision == VLB_PREC_FUSED && (p->flags & VLB_BAKE_FORCE_FUSED_KERNEL)) {
+  // VLB_PREC_FUSED: the lane walk with the projection in the same kernel
+  // (k_trace_fused.cu), no radiance tile.  Packet walks (on request) keep the
+  // packet kernel's fused mode when the directions fit at most two work items
+  // per packet (large probe counts), else the tile; grid walks use the tile.
+  const bool prec_fused = p->precision == VLB_PREC_FUSED;
+  if (prec_fused && a.lane && !a.grid_hdr && !(p->flags & VLB_BAKE_FORCE_FUSED_KERNEL)) {
+    vlbk::BakeJobDev j{};
+    job_from_trace(a, &j);
+    j.out = static_cast<float*>(ob.dev);
+    j.chunk_rays = vlbk::fused_chunk_rays(S);
+    j.chunks = (S + j.chunk_rays - 1) / j.chunk_rays;
+    j.hit_tri = a.hit_tri; j.shadow = a.shadow; j.dbg_radiance = a.dbg_radiance;
+    if (j.chunks > 1) {
+      void *part, *done;
+      if ((st = scratch(ctx, "bake_partial", size_t(nprobes) * j.chunks * V * 4, &part)) ||
+          (st = scratch(ctx, "bake_chunk_done", size_t(nprobes) * 4, &done)))
+        return st;
+      VLB_CUDA(ctx, cudaMemsetAsync(done, 0, size_t(nprobes) * 4, ctx->stream));
+      j.partial = static_cast<float*>(part);
+      j.done = static_cast<uint32_t*>(done);
+    }
+    const uint64_t items = uint64_t(nprobes) * j.chunks;
+    if (items >= (1ull << 32) - (1ull << 20)) return fail(ctx, VLB_ERR_INVALID, "too many probes for one bake");
+    KScope k(ctx, "trace_fused_lane");
+    vlbk::launch_trace_fused_lane(nullptr, j, 1, uint32_t(items), K, a.work_counter, fused_sched(ctx->batch_sched),
+                                  ctx->num_sms, ctx->stream);
+    if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) ||
+        (st = copy_out(ctx, orad)))
+      return st;
+    return finish(ctx, ob.host || oh.host || os.host || orad.host);
+  }
+  bool fused = prec_fused && !a.lane && a.chunks <= 2 && !a.dbg_radiance && !a.grid_hdr;
+  if (prec_fused && (p->flags & VLB_BAKE_FORCE_FUSED_KERNEL)) {
     if (a.dbg_radiance) return fail(ctx, VLB_ERR_UNSUPPORTED, "the fused kernel keeps no per-ray radiance");
     fused = true;
   }
-  if (p->precision == VLB_PREC_FUSED && !fused) vlbk::plan_trace(a, ctx->num_sms, false);
+  if (prec_fused && !fused) vlbk::plan_trace(a, ctx->num_sms, false);
   if (fused) {
     a.out = static_cast<float*>(ob.dev);
     if (a.chunks > 1) {
@@ -1087,17 +1172,21 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     KScope k(ctx, "trace_fused");
     vlbk::launch_trace_fused(a, ctx->num_sms, ctx->stream);
   } else {
-    const bool bf16 = p->precision == VLB_PREC_MIXED;
+    const bool bf16 = p->precision == VLB_PREC_MIXED || p->precision == VLB_PREC_BF16;
+    const bool split = p->precision == VLB_PREC_MIXED;
+    if (split && (st = dirset_split_basis(ctx, p->dirs))) return st;
     void* tile;
-    if ((st = scratch(ctx, "bake_tile", rays * 3 * (bf16 ? 2 : 4), &tile))) return st;
+    if ((st = scratch(ctx, "bake_tile", rays * 3 * (bf16 && !split ? 2 : 4), &tile))) return st;
     if (bf16) a.radiance_bf16 = static_cast<uint16_t*>(tile);
     else a.radiance = static_cast<float*>(tile);
+    a.bf16_split = split ? 1 : 0;
     {
       KScope k(ctx, "trace_tile");
       vlbk::launch_trace_tile(a, ctx->num_sms, ctx->stream);
     }
     if (bf16) {
-      if ((st = project_bf16(ctx, a.radiance_bf16, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) return st;
+      if ((st = project_bf16(ctx, a.radiance_bf16, nprobes, p->dirs, K, static_cast<float*>(ob.dev), split)))
+        return st;
     } else if ((st = project_f32(ctx, a.radiance, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) {
       return st;
     }
@@ -1181,9 +1270,10 @@ struct BatchPlan {
   uint32_t K = 0;
   uint32_t max_probes = 0;  // largest job
   bool bf16 = false;
+  bool split = false;         // VLB_PREC_MIXED: BF16 hi/lo pairs
+  bool fused = false;         // VLB_PREC_FUSED: the fused lane walk, no tile
+  size_t partial_floats = 0;  // fused: chunk partials of all jobs
 };
-
-uint32_t batch_prec(uint32_t p) { return p == VLB_PREC_MIXED ? VLB_PREC_MIXED : VLB_PREC_FP32; }
 
 // Device buffers of one batch (context scratch, allocated before any launch
 // so that the launch sequence can be captured).
@@ -1193,6 +1283,8 @@ struct BatchBufs {
   uint32_t* sort;      // 4 x rows
   uint8_t* tile;
   float* out;          // rows x V
+  float* partial;      // fused: chunk partials
+  uint32_t* done;      // fused: rows chunk tickets
   uint8_t* meta;       // job table + scatter arrays
   uint32_t* counter;
   size_t table_bytes, dst_off, p0_off, np_off;
@@ -1206,20 +1298,26 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
   if (!params) return fail(ctx, VLB_ERR_INVALID, "null batch params");
   if (!jobs && njobs) return fail(ctx, VLB_ERR_INVALID, "null job array");
   if (params->lmax != 2 && params->lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", params->lmax);
-  if (params->precision > VLB_PREC_MIXED) return fail(ctx, VLB_ERR_INVALID, "precision %u", params->precision);
+  if (params->precision > VLB_PREC_BF16) return fail(ctx, VLB_ERR_INVALID, "precision %u", params->precision);
   pl->K = k_of(params->lmax);
-  pl->bf16 = batch_prec(params->precision) == VLB_PREC_MIXED;
+  pl->bf16 = params->precision == VLB_PREC_MIXED || params->precision == VLB_PREC_BF16;
+  pl->split = params->precision == VLB_PREC_MIXED;
+  pl->fused = params->precision == VLB_PREC_FUSED;
   for (uint32_t i = 0; i < njobs; ++i) {
     const vlb_bake_job& j = jobs[i];
     const vlb_bake_params* p = j.params ? j.params : params;
     BatchJob b{};
     vlb_status st = check_params(ctx, j.scene, p, &b.sun_len);
     if (st) return fail(ctx, st, "job %u: %s", i, ctx->err.c_str());
-    if (p->lmax != params->lmax || batch_prec(p->precision) != batch_prec(params->precision))
+    if (p->lmax != params->lmax || p->precision != params->precision)
       return fail(ctx, VLB_ERR_INVALID, "job %u: lmax and precision must equal the batch's", i);
     if (j.nprobes == 0) continue;
     if (!j.probe_xyz || !j.out) return fail(ctx, VLB_ERR_INVALID, "job %u: null probes or output", i);
     b.idx = i; b.p = p; b.nprobes = j.nprobes; b.S = p->dirs->n;
+    if (pl->fused) {
+      const uint32_t D = vlbk::fused_chunk_rays(b.S), C = (b.S + D - 1) / D;
+      if (C > 1) pl->partial_floats += size_t(j.nprobes) * C * 3 * pl->K;
+    }
     pl->max_probes = std::max(pl->max_probes, j.nprobes);
     b.cost = double(j.nprobes) * b.S * std::log2(double(j.scene->ntris) + 2.0);
     uint32_t g = 0;
@@ -1230,12 +1328,12 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
     if (!is_device_ptr(j.probe_xyz)) pl->host_probe_bytes += (size_t(j.nprobes) * 12 + 15) / 16 * 16;
     pl->jobs.push_back(b);
   }
-  const size_t esz = pl->bf16 ? 2 : 4;
+  const size_t esz = pl->bf16 && !pl->split ? 2 : 4;  // bytes a sample (hi/lo pairs: 4)
   for (auto& g : pl->groups) {
     g.row0 = pl->rows;
     pl->rows += g.rows;
     g.tile_off = pl->tile_bytes;
-    pl->tile_bytes += (size_t(g.rows) * 3 * g.dirs->n * esz + 255) / 256 * 256;
+    if (!pl->fused) pl->tile_bytes += (size_t(g.rows) * 3 * g.dirs->n * esz + 255) / 256 * 256;
     g.rows = 0;  // reused below as the running row
   }
   for (auto& b : pl->jobs) {
@@ -1251,24 +1349,30 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
 // The device work of a batch on ctx->stream (capturable: no allocation, no
 // synchronisation).
 static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBufs& bb, uint32_t ntable,
-                                uint32_t total_rays, uint32_t chunk) {
+                                uint32_t total_rays, uint32_t chunk, const vlbk::FusedSched& fs) {
   const uint32_t V = 3 * pl.K;
   const auto* table = reinterpret_cast<const vlbk::BakeJobDev*>(bb.meta);
   VLB_CUDA(ctx, cudaMemsetAsync(bb.counter, 0, 4, ctx->stream));
+  if (pl.fused) VLB_CUDA(ctx, cudaMemsetAsync(bb.done, 0, pl.rows * 4, ctx->stream));
   {
     KScope k(ctx, "probe_order_batch");
     vlbk::launch_probe_order_batch(table, ntable, ctx->stream);
   }
-  {
+  if (pl.fused) {
+    KScope k(ctx, "trace_fused_batch");
+    vlbk::launch_trace_fused_lane(table, ctx->batch_table[0], ntable, total_rays, pl.K, bb.counter, fs,
+                                  ctx->num_sms, ctx->stream);
+  } else {
     KScope k(ctx, "trace_batch");
     vlbk::launch_trace_batch(table, ntable, total_rays, chunk, bb.counter, ctx->num_sms, ctx->stream);
   }
   for (const auto& g : pl.groups) {
+    if (pl.fused) break;  // the fused walk wrote the projected rows
     float* out = bb.out + g.row0 * V;
     const uint32_t n = uint32_t(g.rows);
     if (pl.bf16) {
       vlb_status st = project_bf16(ctx, reinterpret_cast<const uint16_t*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out,
-                                   "batch_project_partial");
+                                   pl.split, "batch_project_partial");
       if (st) return st;
     } else {
       vlb_status st = project_f32(ctx, reinterpret_cast<const float*>(bb.tile + g.tile_off), n, g.dirs, pl.K, out,
@@ -1314,21 +1418,24 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
   bb.np_off = bb.p0_off + size_t(ndev_out) * 4;
   bb.ndev_out = ndev_out;
   const size_t meta_bytes = bb.np_off + size_t(ndev_out) * 4;
-  void *probes = nullptr, *order, *sort, *tile, *out, *meta, *counter;
+  void *probes = nullptr, *order, *sort, *tile = nullptr, *out, *meta, *counter, *part = nullptr, *done = nullptr;
   if ((pl.host_probe_bytes && (st = scratch(ctx, "batch_probes", pl.host_probe_bytes, &probes))) ||
       (st = scratch(ctx, "batch_order", pl.rows * 4, &order)) ||
       (st = scratch(ctx, "batch_sort", pl.rows * 16, &sort)) ||
-      (st = scratch(ctx, "batch_tile", pl.tile_bytes, &tile)) ||
+      (pl.tile_bytes && (st = scratch(ctx, "batch_tile", pl.tile_bytes, &tile))) ||
       (st = scratch(ctx, "batch_out", pl.rows * V * 4, &out)) ||
       (st = scratch(ctx, "batch_meta", meta_bytes, &meta)) ||
-      (st = scratch(ctx, "batch_counter", 256, &counter)))
+      (st = scratch(ctx, "batch_counter", 256, &counter)) ||
+      (pl.partial_floats && (st = scratch(ctx, "batch_partial", pl.partial_floats * 4, &part))) ||
+      (pl.fused && (st = scratch(ctx, "batch_done", pl.rows * 4, &done))))
     return st;
+  bb.partial = static_cast<float*>(part); bb.done = static_cast<uint32_t*>(done);
   bb.probes = static_cast<float*>(probes); bb.order = static_cast<uint32_t*>(order);
   bb.sort = static_cast<uint32_t*>(sort); bb.tile = static_cast<uint8_t*>(tile); bb.out = static_cast<float*>(out);
   bb.meta = static_cast<uint8_t*>(meta); bb.counter = static_cast<uint32_t*>(counter);
 
   // stage host probes, build the job table
-  const size_t esz = pl.bf16 ? 2 : 4;
+  const size_t esz = pl.bf16 && !pl.split ? 2 : 4;
   uint64_t warp_rays = 0;
   for (const auto& b : pl.jobs) warp_rays += (uint64_t(b.nprobes) + 31) / 32 * b.S;
   // rays per lane per chunk (a warp takes 32 x that many rays at a time):
@@ -1341,9 +1448,12 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     dpw = uint32_t(std::min<uint64_t>(8, std::max<uint64_t>(1, rays / target)));
   }
   const uint32_t chunk = 32 * dpw;
+  if (pl.split)  // the split basis is built before anything is enqueued (or captured)
+    for (const auto& g : pl.groups)
+      if ((st = dirset_split_basis(ctx, g.dirs))) return st;
   auto& table = ctx->batch_table;
   table.assign(ntable, vlbk::BakeJobDev{});
-  size_t poff = 0;
+  size_t poff = 0, part_off = 0;
   uint64_t items = 0;
   for (uint32_t t = 0; t < ntable; ++t) {
     const BatchJob& b = pl.jobs[ord[t]];
@@ -1372,16 +1482,33 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     d.order = bb.order + b.row0;
     d.nprobes = b.nprobes;
     d.dirs = p->dirs->d_dirs; d.dinv = p->dirs->d_dinv; d.dir_order = p->dirs->d_order; d.S = b.S;
-    uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
-    if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
-    else d.radiance = reinterpret_cast<float*>(rad);
-    d.ray_begin = uint32_t(items);
-    items += ((uint64_t(b.nprobes) + 31) / 32 * 32 * b.S + chunk - 1) / chunk * chunk;
+    if (pl.fused) {
+      d.basis16 = p->dirs->d_basis16;
+      d.out = bb.out + b.row0 * V;
+      d.chunk_rays = vlbk::fused_chunk_rays(b.S);
+      d.chunks = (b.S + d.chunk_rays - 1) / d.chunk_rays;
+      if (d.chunks > 1) {
+        d.partial = bb.partial + part_off;
+        part_off += size_t(b.nprobes) * d.chunks * V;
+      }
+      d.done = bb.done + b.row0;
+      d.item_begin = uint32_t(items);
+      items += uint64_t(b.nprobes) * d.chunks;
+    } else {
+      uint8_t* rad = bb.tile + g.tile_off + (b.row0 - g.row0) * 3 * b.S * esz;
+      d.bf16_split = pl.split ? 1 : 0;
+      if (pl.bf16) d.radiance_bf16 = reinterpret_cast<uint16_t*>(rad);
+      else d.radiance = reinterpret_cast<float*>(rad);
+      d.ray_begin = uint32_t(items);
+      items += ((uint64_t(b.nprobes) + 31) / 32 * 32 * b.S + chunk - 1) / chunk * chunk;
+    }
     for (int a = 0; a < 6; ++a) d.bounds[a] = j.scene->bounds[a];
     d.sort_scratch = bb.sort + 4 * b.row0;
     if (ext) { d.hits_out = ext[b.idx].hits_out; d.hits_in = ext[b.idx].hits_in; }
   }
-  if (items >= (1ull << 31)) return fail(ctx, VLB_ERR_INVALID, "batch has 2^31 rays or more; split it");
+  if (items >= (1ull << 31))
+    return fail(ctx, VLB_ERR_INVALID, pl.fused ? "batch has 2^31 work items or more; split it"
+                                               : "batch has 2^31 rays or more; split it");
   auto& meta_h = ctx->batch_meta;
   meta_h.assign(meta_bytes, 0);
   std::memcpy(meta_h.data(), table.data(), table.size() * sizeof(vlbk::BakeJobDev));
@@ -1400,9 +1527,15 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
   VLB_CUDA(ctx, cudaMemcpyAsync(meta, meta_h.data(), meta_bytes, cudaMemcpyHostToDevice, ctx->stream));
 
   // shape key: everything the captured launches bake in as parameters
-  std::vector<uint64_t> key = {ntable, uint64_t(items), dpw, pl.bf16, K, ndev_out, pl.max_probes, uint64_t(uintptr_t(tile)),
-                               uint64_t(uintptr_t(out)), uint64_t(uintptr_t(meta)), uint64_t(uintptr_t(counter)),
-                               uint64_t(ctx->num_sms)};
+  std::vector<uint64_t> key = {ntable, uint64_t(items), dpw, pl.bf16 + 2u * pl.split, K, ndev_out, pl.max_probes,
+                               uint64_t(uintptr_t(tile)), uint64_t(uintptr_t(out)), uint64_t(uintptr_t(meta)),
+                               uint64_t(uintptr_t(counter)), uint64_t(ctx->num_sms), pl.fused,
+                               uint64_t(uintptr_t(part)), uint64_t(uintptr_t(done)), pl.rows, sc.ctas_per_sm,
+                               sc.node_steps, sc.refill_idle};
+  if (pl.fused && ntable == 1) {  // one job goes to the kernel by value: its fields are part of the shape
+    const auto* w = reinterpret_cast<const uint64_t*>(table.data());
+    key.insert(key.end(), w, w + sizeof(vlbk::BakeJobDev) / 8);
+  }
   for (const auto& g : pl.groups) {
     key.push_back(uint64_t(uintptr_t(g.dirs)));
     key.push_back(g.row0); key.push_back(g.rows); key.push_back(g.tile_off);
@@ -1419,7 +1552,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
       ctx->profiling = false;
       cudaGraph_t g = nullptr;
       VLB_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk);
+      st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk, fused_sched(sc));
       const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       ctx->profiling = prof;
       ctx->batch_graph_kernels = uint32_t(ctx->launches - l0);
@@ -1432,7 +1565,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     }
     KScope k(ctx, "bake_batch_graph", int(ctx->batch_graph_kernels));
     VLB_CUDA(ctx, cudaGraphLaunch(ctx->batch_exec, ctx->stream));
-  } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk))) {
+  } else if ((st = batch_enqueue(ctx, pl, bb, ntable, uint32_t(items), chunk, fused_sched(sc)))) {
     return st;
   }
   for (const auto& b : pl.jobs) {
@@ -1469,6 +1602,11 @@ vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs
   cudaSetDevice(ctx->device);
   vlb_batch_schedule sc = sched ? *sched : ctx->batch_sched;
   if (sc.dirs_per_item > 64) return fail(ctx, VLB_ERR_INVALID, "dirs_per_item %u > 64", sc.dirs_per_item);
+  if (sc.ctas_per_sm && (sc.ctas_per_sm < 7 || sc.ctas_per_sm > 9))
+    return fail(ctx, VLB_ERR_INVALID, "ctas_per_sm %u: 7, 8 or 9", sc.ctas_per_sm);
+  if (sc.node_steps > 16 || sc.refill_idle > 32)
+    return fail(ctx, VLB_ERR_INVALID, "node_steps %u (<= 16) or refill_idle %u (<= 32)", sc.node_steps,
+                sc.refill_idle);
   return batch_run(ctx, jobs, njobs, params, sc);
 }
 
@@ -1476,29 +1614,58 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
                               uint32_t reps, vlb_batch_schedule* best, float* best_ms) {
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
+  if (!params) return fail(ctx, VLB_ERR_INVALID, "null batch params");
   if (reps == 0) reps = 1;
-  const uint32_t dpws[] = {1, 2, 4, 8, 16};
   cudaEvent_t e0, e1;
   VLB_CUDA(ctx, cudaEventCreate(&e0));
   VLB_CUDA(ctx, cudaEventCreate(&e1));
-  vlb_batch_schedule win{0, 1, 1};
-  float win_ms = -1.f;
+  // mean ms per batch of one schedule (after one warm-up run), or < 0 on error
   vlb_status st = VLB_OK;
-  for (uint32_t order = 0; order < 2 && !st; ++order) {
-    for (uint32_t dpw : dpws) {
-      const vlb_batch_schedule sc{dpw, order, 0};
-      if ((st = batch_run(ctx, jobs, njobs, params, sc))) break;  // warm-up
-      cudaEventRecord(e0, ctx->stream);
-      for (uint32_t r = 0; r < reps && !st; ++r) st = batch_run(ctx, jobs, njobs, params, sc);
-      cudaEventRecord(e1, ctx->stream);
-      if (st) break;
-      if (cudaEventSynchronize(e1) != cudaSuccess) { st = cuda_fail(ctx, cudaGetLastError(), "autotune timing"); break; }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      ms /= float(reps);
-      if (win_ms < 0.f || ms < win_ms) { win_ms = ms; win = {dpw, order, 1}; }
+  auto time_one = [&](const vlb_batch_schedule& sc) -> float {
+    if ((st = batch_run(ctx, jobs, njobs, params, sc))) return -1.f;
+    cudaEventRecord(e0, ctx->stream);
+    for (uint32_t r = 0; r < reps && !st; ++r) st = batch_run(ctx, jobs, njobs, params, sc);
+    cudaEventRecord(e1, ctx->stream);
+    if (st) return -1.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      st = cuda_fail(ctx, cudaGetLastError(), "autotune timing");
+      return -1.f;
     }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / float(reps);
+  };
+  vlb_batch_schedule win{0, 1, 1, 0, 0, 0};
+  float win_ms = -1.f;
+  if (params->precision == VLB_PREC_FUSED) {
+    // one knob at a time from the default, each kept at its fastest value
+    const vlb_batch_schedule start{0, 1, 0, 8, 6, 16};
+    win_ms = time_one(start);
+    win = start;
+    auto sweep = [&](uint32_t vlb_batch_schedule::*knob, std::initializer_list<uint32_t> vals) {
+      for (uint32_t v : vals) {
+        if (st) return;
+        vlb_batch_schedule c = win;
+        c.*knob = v;
+        const float ms = time_one(c);
+        if (ms >= 0.f && ms < win_ms) { win_ms = ms; win = c; }
+      }
+    };
+    sweep(&vlb_batch_schedule::ctas_per_sm, {7, 9});
+    sweep(&vlb_batch_schedule::node_steps, {4, 8, 12});
+    sweep(&vlb_batch_schedule::refill_idle, {8, 24});
+    sweep(&vlb_batch_schedule::cost_order, {0});
+  } else {
+    const uint32_t dpws[] = {1, 2, 4, 8, 16};
+    for (uint32_t order = 0; order < 2 && !st; ++order)
+      for (uint32_t dpw : dpws) {
+        const vlb_batch_schedule sc{dpw, order, 0, 0, 0, 0};
+        const float ms = time_one(sc);
+        if (st) break;
+        if (win_ms < 0.f || ms < win_ms) { win_ms = ms; win = sc; }
+      }
   }
+  win.graph = 1;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st) return st;
@@ -1631,12 +1798,15 @@ vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint
   cudaSetDevice(ctx->device);
   if (!dirs || dirs->ctx != ctx) return fail(ctx, VLB_ERR_INVALID, "direction set missing or from another context");
   if (lmax != 2 && lmax != 3) return fail(ctx, VLB_ERR_INVALID, "lmax must be 2 or 3 (got %u)", lmax);
-  if (dtype != VLB_DTYPE_F32 && dtype != VLB_DTYPE_BF16) return fail(ctx, VLB_ERR_INVALID, "dtype %d", dtype);
+  if (dtype != VLB_DTYPE_F32 && dtype != VLB_DTYPE_BF16 && dtype != VLB_DTYPE_BF16_SPLIT)
+    return fail(ctx, VLB_ERR_INVALID, "dtype %d", dtype);
   if (nprobes == 0) return VLB_OK;
   if (!radiance || !out) return fail(ctx, VLB_ERR_INVALID, "null radiance or output");
   const uint32_t S = dirs->n, K = k_of(lmax);
-  const size_t eb = dtype == VLB_DTYPE_F32 ? 4 : 2;
+  const size_t eb = dtype == VLB_DTYPE_BF16 ? 2 : 4;  // bytes a sample (hi/lo pairs: 4)
+  const bool split = dtype == VLB_DTYPE_BF16_SPLIT;
   vlb_status st;
+  if (split && (st = dirset_split_basis(ctx, dirs))) return st;
   const void* drad;
   if ((st = stage_in(ctx, radiance, size_t(nprobes) * 3 * S * eb, "proj_in", &drad))) return st;
   OutBuf ob;
@@ -1645,7 +1815,7 @@ vlb_status vlb_project(vlb_ctx* ctx, const void* radiance, vlb_dtype dtype, uint
     if ((st = project_f32(ctx, static_cast<const float*>(drad), nprobes, dirs, K, static_cast<float*>(ob.dev))))
       return st;
   } else if ((st = project_bf16(ctx, static_cast<const uint16_t*>(drad), nprobes, dirs, K,
-                                static_cast<float*>(ob.dev)))) {
+                                static_cast<float*>(ob.dev), split))) {
     return st;
   }
   if ((st = copy_out(ctx, ob))) return st;

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -69,8 +70,9 @@ void launch_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, ui
 size_t project_partial_bytes(uint32_t nprobes, uint32_t S, uint32_t K);
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
                         float* out, float* partial, cudaStream_t s);
+// split: the tile is [rows][2S] hi/lo BF16 pairs (the sample is hi + lo).
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
-                              uint32_t K, float* out, float* partial, cudaStream_t s);
+                              uint32_t K, float* out, float* partial, uint32_t split, cudaStream_t s);
 // tcgen05 projection of a BF16 tile (k_project_tc.cu).  basis_bt: [32][bt_pitch]
 // BF16, rows 0..15 the high and 16..31 the low part of the weighted basis.
 // Needs S % 8 == 0 and a 16-byte aligned tile; returns -1 if the tensor maps
@@ -140,7 +142,8 @@ struct TraceArgs {
   uint32_t sky_n;
   // outputs
   float* radiance;        // [nprobes][3][S] fp32 or null
-  uint16_t* radiance_bf16;  // [nprobes][3][S] bf16 or null
+  uint16_t* radiance_bf16;  // [nprobes][3][S] bf16, or [nprobes][3][2S] hi/lo split, or null
+  uint32_t bf16_split;    // 1: radiance_bf16 holds hi/lo pairs (store_bf16)
   int32_t* hit_tri;       // [nprobes*S] or null
   uint8_t* shadow;        // [nprobes*S] or null
   float* dbg_radiance;    // [nprobes*S*3] or null
@@ -212,6 +215,7 @@ struct BakeJobDev {
   // this job's rows of its direction set's radiance tile
   float* radiance;
   uint16_t* radiance_bf16;
+  uint32_t bf16_split;    // 1: hi/lo pairs, rows of 2S
   // rays [ray_begin, ray_begin + P * S) of the batch's numbering (P: nprobes
   // rounded up to 32), the range rounded up to whole chunks
   uint32_t ray_begin;
@@ -223,7 +227,45 @@ struct BakeJobDev {
   // skipped and the kept hit shaded (relight)
   int2* hits_out;
   const int2* hits_in;
+  // fused projection (no radiance tile): a work item is one probe and one
+  // chunk of chunk_rays consecutive positions of the trace order
+  const float* basis16;   // S x 16 FP32 weighted basis
+  float* out;             // [nprobes][K][3], this job's rows
+  float* partial;         // [nprobes][chunks][K*3] FP32 chunk sums (chunks > 1)
+  uint32_t* done;         // [nprobes] chunk tickets, zero before the launch
+  uint32_t chunks, chunk_rays;
+  uint32_t item_begin;    // first work item of this job in the launch's numbering
+  // per-ray debug outputs of the fused walk (null: none), ray r = probe * S + s
+  int32_t* hit_tri;
+  uint8_t* shadow;
+  float* dbg_radiance;
 };
+// Fused lane walk: chunk size for S directions, a multiple of 64 rays, at
+// most 16 chunks per probe while a chunk holds at most 4096 rays (larger
+// sets, such as the 3141 x 1000 equirect set, get more chunks).  A function
+// of S alone, so a probe's sums have the same order in a single bake and in
+// any batch.
+constexpr uint32_t kFusedSubRays = 64;
+constexpr uint32_t kFusedMaxChunks = 16;
+constexpr uint32_t kFusedMaxChunkRays = 4096;
+inline uint32_t fused_chunk_rays(uint32_t S) {
+  const uint32_t per = (S + kFusedMaxChunks - 1) / kFusedMaxChunks;
+  const uint32_t d = (per + kFusedSubRays - 1) / kFusedSubRays * kFusedSubRays;
+  return d < kFusedMaxChunkRays ? d : kFusedMaxChunkRays;
+}
+// Launch knobs of the fused walk (vlb_batch_schedule; results do not depend on them).
+struct FusedSched {
+  uint32_t ctas_per_sm = 8;  // register budget: 7, 8 or 9 resident 4-warp CTAs per SM
+  uint32_t node_steps = 6;   // inner-node steps per turn
+  uint32_t refill_idle = 16; // idle lanes that trigger a refill
+};
+// One persistent launch: warps pull work items (job, probe, direction chunk)
+// from *counter (zero before the launch), trace them per lane and project
+// each chunk's radiance in the warp (FP32 sums in a fixed order, chunk sums
+// added in FP64 in chunk order by the chunk that finishes last).  njobs == 1
+// passes the job by value (jobs may be null).
+void launch_trace_fused_lane(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njobs, uint32_t total_items,
+                             uint32_t K, uint32_t* counter, const FusedSched& sc, int num_sms, cudaStream_t s);
 // One CTA per job: spatial order of each job's probes into job.order
 // (counting sort on a 12-bit Morton prefix up to 16,384 probes, the CTA
 // radix sort in the job's sort scratch above).
@@ -307,7 +349,7 @@ struct vlb_ctx {
   std::vector<vlbk::BakeJobDev> batch_table;  // host copy of the job table
   std::vector<uint8_t> batch_meta;             // job table + scatter arrays, uploaded each call
   bool batch_tuned = false;
-  vlb_batch_schedule batch_sched{0, 1, 1};
+  vlb_batch_schedule batch_sched{0, 1, 1, 0, 0, 0};
 };
 
 struct vlb_scene {
@@ -332,6 +374,12 @@ struct vlb_dirset {
   uint32_t* d_order = nullptr;  // n direction indices sorted by ray octant (stable)
   uint16_t* d_bt = nullptr;     // [32][bt_pitch] BF16 weighted basis, high rows 0..15, low rows 16..31
   uint32_t bt_pitch = 0;
+  // BF16 basis for hi/lo split tiles over 2S columns (built on first use):
+  // rows 0..15 the high basis under both halves, rows 16..31 the low basis
+  // under the high half and zero under the low half
+  mutable std::mutex bt2_mu;
+  mutable uint16_t* d_bt2 = nullptr;
+  mutable uint32_t bt2_pitch = 0;
   float* d_basis16 = nullptr;   // n x 16 weighted basis, FP32
   std::vector<float> h_dirs;    // n*3
   std::vector<double> h_basis;  // n*16 FP64 weighted basis

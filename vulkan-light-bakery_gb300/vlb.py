@@ -23,11 +23,11 @@ FRAME_WORLD, FRAME_XZY = 0, 1
 SKY_CUBEMAP, SKY_PANORAMA, SKY_ENVMAP = 0, 1, 2
 TEXEL_RGB32F, TEXEL_RGBA8 = 0, 1
 SKY_REF_BGRA_SWAP = 1
-PREC_FP32, PREC_FUSED, PREC_MIXED = 0, 1, 2
+PREC_FP32, PREC_FUSED, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
 BAKE_FORCE_FUSED_KERNEL = 1
 BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE, BAKE_TRAVERSAL_GRID = 2, 4, 8
 SCENE_TRAVERSAL_LBVH = 1
-DTYPE_F32, DTYPE_BF16 = 0, 1
+DTYPE_F32, DTYPE_BF16, DTYPE_BF16_SPLIT = 0, 1, 2
 
 
 class VlbError(RuntimeError):
@@ -64,7 +64,8 @@ class BakeJob(C.Structure):
 
 
 class BatchSchedule(C.Structure):
-    _fields_ = [("dirs_per_item", C.c_uint32), ("cost_order", C.c_uint32), ("graph", C.c_uint32)]
+    _fields_ = [("dirs_per_item", C.c_uint32), ("cost_order", C.c_uint32), ("graph", C.c_uint32),
+                ("ctas_per_sm", C.c_uint32), ("node_steps", C.c_uint32), ("refill_idle", C.c_uint32)]
 
 
 class ServiceConfig(C.Structure):
@@ -319,7 +320,8 @@ class Context:
         S = params_dirs_count(params)
         hit = np.empty(n * S, np.int32)
         vis = np.empty(n * S, np.uint8)
-        rad = np.empty(n * S * 3, np.float32) if params.precision != PREC_FUSED else None
+        packet_fused = params.precision == PREC_FUSED and params.flags & BAKE_FORCE_FUSED_KERNEL
+        rad = None if packet_fused else np.empty(n * S * 3, np.float32)
         dbg = BakeDebug(_ptr(hit), _ptr(vis), _ptr(rad))
         self.check(lib.vlb_bake_ex(self.h, scene.h, _ptr(probes), n, C.byref(params), _ptr(ret), C.byref(dbg)))
         return ret, hit.reshape(n, S), vis.reshape(n, S), (None if rad is None else rad.reshape(n, S, 3))
