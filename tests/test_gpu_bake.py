@@ -197,25 +197,72 @@ def test_grid_mode_agrees(ctx, case):
 
 @pytest.mark.parametrize("nboxes,counts", [(64, (16, 16, 16)), (4000, (6, 6, 6))])
 def test_traversal_trees_agree(ctx, nboxes, counts):
-    """The clustered traversal tree and the Karras LBVH give the same per-ray
-    decisions and radiance, bit for bit, and the clustered tree visits fewer
-    nodes."""
+    """The clustered traversal tree and the Karras LBVH, each walked as the
+    binary tree or as the 8-wide quantised tree collapsed from it, give the
+    same per-ray decisions and radiance, bit for bit; the clustered tree visits
+    fewer nodes than the LBVH, and the wide trees fewer than the binary ones."""
     pos, idx, alb, sky, sun, probes, S = c1_inputs(seed=13, nboxes=nboxes, counts=counts)
     skyh = ctx.sky(sky, 128)
     ds = ctx.fibonacci(S)
     res, work = [], []
-    for flags in (0, vlb.SCENE_TRAVERSAL_LBVH):
+    trees = (vlb.SCENE_TRAVERSAL_WIDE, vlb.SCENE_TRAVERSAL_LBVH | vlb.SCENE_TRAVERSAL_WIDE, 0,
+             vlb.SCENE_TRAVERSAL_LBVH)
+    for flags in trees:
         scene = ctx.scene(pos, idx, alb, flags=flags)
         p = vlb.bake_params(ds, 2, vlb.PREC_FP32, sun, sky=skyh)
-        p.flags = vlb.BAKE_TRAVERSAL_LANE  # a tree walk in both
+        p.flags = vlb.BAKE_TRAVERSAL_LANE  # a tree walk in all four
         res.append(ctx.bake(scene, probes, p, debug=True))
         st = vlb.trace_stats(ctx, scene, probes, p)
         work.append(st["node_tests"] / (st["rays"] + st["shadow_rays"]))
-    (sa, ha, va, ra), (sb, hb, vb, rb) = res
-    print(f"node tests per ray: clustered {work[0]:.1f}, LBVH {work[1]:.1f}")
-    assert np.array_equal(ha, hb) and np.array_equal(va, vb)
-    assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
-    assert work[0] < work[1]
+    print("node visits per ray (clustered wide, LBVH wide, clustered binary, LBVH binary):",
+          [f"{w:.1f}" for w in work])
+    sa, ha, va, ra = res[0]
+    for sb, hb, vb, rb in res[1:]:
+        assert np.array_equal(ha, hb) and np.array_equal(va, vb)
+        assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+    assert work[2] < work[3] and work[0] < work[2] and work[1] < work[3]
+
+
+def _wide_edge_scenes():
+    """Scenes that stress the quantised boxes: far from the origin, flat (zero
+    extent on an axis), coincident and overlapping triangles, two triangles."""
+    rng = np.random.default_rng(17)
+    out = {}
+    pos, idx, alb = vlb.synth_box_scene(19, 300)
+    out["offset_1000"] = (pos + np.float32([1000.0, -1000.0, 250.0]), idx, alb)
+    p = rng.random((3 * 400, 3)).astype(np.float32)
+    p[:, 1] = 0.5  # every triangle in the plane y = 0.5
+    out["flat"] = (p, np.arange(3 * 400, dtype=np.uint32).reshape(-1, 3), rng.uniform(0.2, 0.8, (400, 3)))
+    t = rng.random((3, 3)).astype(np.float32)
+    out["coincident"] = (np.tile(t, (64, 1)), np.arange(3 * 64, dtype=np.uint32).reshape(-1, 3),
+                         rng.uniform(0.2, 0.8, (64, 3)))
+    p = (rng.random((3 * 500, 3)) * 2 - 0.5).astype(np.float32)
+    out["big_overlap"] = (p, np.arange(3 * 500, dtype=np.uint32).reshape(-1, 3), rng.uniform(0.2, 0.8, (500, 3)))
+    out["two"] = (np.float32([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 0.5], [1, 0, 0.5], [0, 1, 0.5]]),
+                  np.arange(6, dtype=np.uint32).reshape(2, 3), np.float32([[0.5] * 3, [0.7] * 3]))
+    return out
+
+
+@pytest.mark.parametrize("case", ["offset_1000", "flat", "coincident", "big_overlap", "two"])
+def test_wide_tree_edge_scenes(ctx, case):
+    """The wide walk equals the binary walk bit for bit on scenes that stress
+    the quantisation, for grid and random probes, in the tile and fused walks."""
+    pos, idx, alb = _wide_edge_scenes()[case]
+    alb = np.asarray(alb, np.float32)
+    lo, hi = pos.min(0), pos.max(0)
+    rng = np.random.default_rng(3)
+    probes = np.concatenate([vlb.probe_grid_ref_order(np.concatenate([lo, hi]).astype(np.float32), (5, 5, 5))[0],
+                             (lo + rng.random((100, 3)) * (hi - lo)).astype(np.float32)])
+    ds = ctx.fibonacci(256)
+    sun = vlb.synth_sun(5)
+    wide = ctx.scene(pos, idx, alb, flags=vlb.SCENE_TRAVERSAL_WIDE)
+    binary = ctx.scene(pos, idx, alb)
+    for prec in (vlb.PREC_FP32, vlb.PREC_FUSED):
+        p = vlb.bake_params(ds, 2, prec, sun)
+        a = ctx.bake(wide, probes, p, debug=True)
+        b = ctx.bake(binary, probes, p, debug=True)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), (case, prec)
 
 
 def test_empty_scene_sees_sky(ctx):

@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
   const uint32_t R = P * a.S;
   Work w;
-  int stack[kTraceStack];
+  int stack[kLaneStack];
   LaneRay L;
   make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
   bool exhausted = false;
@@ -706,7 +706,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
                                                                uint32_t total, uint32_t chunk, uint32_t* counter) {
   const uint32_t lane = threadIdx.x & 31;
   Work w;
-  int stack[kTraceStack];
+  int stack[kLaneStack];
   LaneRay L;
   make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
   for (;;) {

@@ -8,12 +8,12 @@
 // Morton-sorted probes, so neighbouring items share a probe or a Morton
 // neighbour.  Persistent warps take items from one counter.
 //
-// Sub-batches.  A warp cuts its items into sub-batches of up to 64 rays and
-// keeps up to four in flight in a shared-memory ring (radiance and direction
-// index per ray).  Idle lanes take the oldest sub-batch's unissued rays
-// first, then the next one's, so lanes that finish early run ahead into the
+// Sub-batches.  A warp cuts its items into sub-batches of up to kSubRays rays
+// and keeps up to kSubBufs in flight in a shared-memory ring (the RGB of each
+// ray).  Idle lanes take the oldest sub-batch's unissued rays first, then the
+// next one's, so lanes that finish early run ahead into the
 // next sub-batch (or the next item) while others finish their walks: a warp
-// waits for a slow ray only when four sub-batches are behind it.  Each lane
+// waits for a slow ray only when kSubBufs sub-batches are behind it.  Each lane
 // runs the per-lane state machine of the lane walk (primary walk, shading,
 // shadow walk) and writes its ray's RGB into the ring when done.  As in the
 // tile lane walk, a warp does this bookkeeping only when enough of its lanes
@@ -31,10 +31,11 @@
 #include "trace_common.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace vlbk {
 
-constexpr int kSubRays = int(kFusedSubRays);
+constexpr int kSubRays = 32;
 constexpr int kSubBufs = 4;
 constexpr uint32_t kSubFirst = 1, kSubLast = 2;
 
@@ -49,9 +50,8 @@ struct SubBatch {
 // lane 0 only, read by every lane after a __syncwarp.
 struct FusedWarp {
   float rad[kSubBufs][3][kSubRays];    // RGB of each ray, channel-major
-  uint32_t dir[kSubBufs][kSubRays];    // direction index of each ray
   SubBatch q[kSubBufs];
-  double acc[64];                      // the current item's running FP64 sums, output v at acc[v]
+  double acc[48];                      // the current item's running FP64 sums, output v at acc[v]
   uint32_t head, n;                    // ring: oldest slot, sub-batches in flight
   uint32_t ij, ip, ic, itn, ite, it0;  // the item being cut: job, probe, chunk, next/end/first ray
   uint32_t have_item, exhausted;
@@ -83,11 +83,13 @@ __device__ __forceinline__ void retire_head(FusedWarp& fw, const BakeJobDev* __r
   const uint32_t e = fw.head;
   const SubBatch q = fw.q[e];
   const BakeJobDev& J = job_of<MULTI>(jobs, one, q.job);
+  const uint32_t* dord = J.dir_order + q.t0;
   for (int v = int(lane); v < V; v += 32) {
     const int k = v / 3, ch = v - 3 * k;
     float s = 0.f;
 #pragma unroll 4
-    for (uint32_t i = 0; i < q.cnt; ++i) s = fmaf(__ldg(J.basis16 + size_t(fw.dir[e][i]) * 16 + k), fw.rad[e][ch][i], s);
+    for (uint32_t i = 0; i < q.cnt; ++i)
+      s = fmaf(__ldg(J.basis16 + size_t(__ldg(dord + i)) * 16 + k), fw.rad[e][ch][i], s);
     fw.acc[v] = ((q.flags & kSubFirst) ? 0.0 : fw.acc[v]) + double(s);
   }
   if (q.flags & kSubLast) {
@@ -202,7 +204,7 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
   }
   __syncwarp();
   Work w;
-  int stack[kTraceStack];
+  int stack[kLaneStack];
   LaneRay L;
   make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
   uint32_t lslot = 0;  // the lane's ray: ring slot << 8 | position
@@ -225,7 +227,6 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
           const uint32_t pos = issued + rank;
           const BakeJobDev& J = job_of<MULTI>(jobs, one, fw.q[e].job);
           const uint32_t s = __ldg(J.dir_order + fw.q[e].t0 + pos);
-          fw.dir[e][pos] = s;
           lslot = (e << 8) | pos;
           lr_start(J, L, fw.q[e].p, s);
           if (J.hits_in) {  // relight: the kept primary hit, only the shadow walk remains
@@ -296,6 +297,22 @@ static void launch_k(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njo
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
+  }
+  // Shared memory and the L1 cache share one array per SM: ask for no more
+  // shared memory than the resident CTAs' rings need, so the walk's node and
+  // triangle fetches keep the largest L1 (the carveout is a percentage of the
+  // 228 KiB maximum; the hardware rounds it up to a supported size).
+  static std::atomic<uint64_t> carved{0};
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+    if (bit && !(carved.load(std::memory_order_relaxed) & bit)) {
+      const size_t need = sizeof(FusedWarp) * kTraceWarps * size_t(per_sm);
+      const int pct = int(std::min<size_t>(100, (need * 100 + 228 * 1024 - 1) / (228 * 1024)));
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+      carved.fetch_or(bit, std::memory_order_relaxed);
+    }
   }
   const uint64_t ctas = std::min<uint64_t>((uint64_t(total) + kTraceWarps - 1) / kTraceWarps,
                                            uint64_t(num_sms) * per_sm);

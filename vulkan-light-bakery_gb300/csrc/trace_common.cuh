@@ -503,9 +503,78 @@ __device__ __forceinline__ void lr_park(LaneRay& L, const int* stack) {
   }
 }
 
+// Byte c (0..3) of a word as an exact float.
+__device__ __forceinline__ float q8(uint32_t word, int c) {
+  return __uint_as_float(0x4B000000u | ((word >> (8 * c)) & 255u)) - 8388608.0f;
+}
+
+// One node of the 8-wide quantised tree (layout in wide_bvh.cpp): every valid
+// child's box is dequantised with the build's FP32 expression fmaf(q, 2^e,
+// origin) -- a box that contains the binary tree's box for that subtree --
+// and slab-tested as in the binary walk; the nearest hit child is next, the
+// other hit children go on the stack.  The children are tested four at a
+// time (their bound bytes are six words) and a child's reference is read only
+// when its box is hit, to keep the walk's registers few.
+template <bool COUNT, class A>
+__device__ __forceinline__ void lr_node_wide(const A& a, LaneRay& L, int* stack, Work& w) {
+  if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
+  const float tlo = L.shadow ? 0.0f : a.tmin;
+  const float4* nd = a.wnodes + 6 * size_t(L.cur);
+  const float4 h = __ldg(nd);
+  const int* refs = reinterpret_cast<const int*>(nd + 4);
+  const uint32_t meta = __float_as_uint(h.w);
+  const float sx = __uint_as_float((meta & 255u) << 23), sy = __uint_as_float(((meta >> 8) & 255u) << 23),
+              sz = __uint_as_float(((meta >> 16) & 255u) << 23);
+  const int nc = int(meta >> 24);
+  const float lim = prune_limit(L.tb);
+  int next = kWalkEnd;
+  float tnext = INFINITY;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    if (4 * half >= nc) break;
+    uint32_t q[6];  // lo x, hi x, lo y, hi y, lo z, hi z: one byte per child
+    if (half == 0) {
+      const uint4 u = __ldg(reinterpret_cast<const uint4*>(nd + 1));
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(nd + 2));
+      q[0] = u.x; q[1] = u.y; q[2] = u.z; q[3] = u.w; q[4] = v.x; q[5] = v.y;
+    } else {
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(nd + 2) + 1);
+      const uint4 u = __ldg(reinterpret_cast<const uint4*>(nd + 3));
+      q[0] = v.x; q[1] = v.y; q[2] = u.x; q[3] = u.y; q[4] = u.z; q[5] = u.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if (4 * half + c < nc) {
+        const float lx = fmaf(q8(q[0], c), sx, h.x), hx = fmaf(q8(q[1], c), sx, h.x);
+        const float ly = fmaf(q8(q[2], c), sy, h.y), hy = fmaf(q8(q[3], c), sy, h.y);
+        const float lz = fmaf(q8(q[4], c), sz, h.z), hz = fmaf(q8(q[5], c), sz, h.z);
+        float tn;
+        if (slab_rt(L.ray, lx, ly, lz, hx, hy, hz, tlo, lim, &tn)) {
+          const int ref = __ldg(refs + 4 * half + c);
+          int push = ref;
+          if (tn < tnext) {
+            push = next;
+            next = ref;
+            tnext = tn;
+          }
+          if (push != kWalkEnd) {
+            if (L.sp < kLaneStack) stack[L.sp++] = push;
+            else atomicAdd(a.err + kErrStackOverflow, 1);
+          }
+        }
+      }
+    }
+  }
+  L.cur = next != kWalkEnd ? next : (L.sp ? stack[--L.sp] : kWalkEnd);
+}
+
 // One inner node: nearer hit child next, the farther one on the stack.
 template <bool COUNT, class A>
 __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work& w) {
+  if (a.wnodes) {
+    lr_node_wide<COUNT>(a, L, stack, w);
+    return;
+  }
   if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
   const float tlo = L.shadow ? 0.0f : a.tmin;
   const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
@@ -517,7 +586,7 @@ __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work
   const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
   if (h0 && h1) {
     const bool first0 = tn0 <= tn1;
-    if (L.sp < kTraceStack) stack[L.sp++] = first0 ? c1 : c0;
+    if (L.sp < kLaneStack) stack[L.sp++] = first0 ? c1 : c0;
     else atomicAdd(a.err + kErrStackOverflow, 1);
     L.cur = first0 ? c0 : c1;
   } else if (h0) {

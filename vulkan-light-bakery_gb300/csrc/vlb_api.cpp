@@ -610,6 +610,7 @@ vlb_status vlb_scene_create_ex(vlb_ctx* ctx, const float* positions, uint32_t st
       }
     }
     if (st == VLB_OK) st = finish(ctx, true);
+    if (st == VLB_OK && (flags & VLB_SCENE_TRAVERSAL_WIDE)) st = vlbh::build_wide(ctx, sc);
   }
   cudaFree(dpos); cudaFree(didx); if (dalb) cudaFree(dalb); cudaFree(scr);
   if (st != VLB_OK) { vlb_scene_destroy(sc); return st; }
@@ -621,7 +622,7 @@ void vlb_scene_destroy(vlb_scene* s) {
   if (!s) return;
   if (s->ctx) { cudaSetDevice(s->ctx->device); cudaStreamSynchronize(s->ctx->stream); }
   cudaFree(s->codes); cudaFree(s->order); cudaFree(s->child); cudaFree(s->box);
-  cudaFree(s->nodes); cudaFree(s->tris); cudaFree(s->albedo);
+  cudaFree(s->nodes); cudaFree(s->wnodes); cudaFree(s->tris); cudaFree(s->albedo);
   delete s;
 }
 
@@ -1038,6 +1039,7 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   vlbk::TraceArgs& a = *out;
   a = vlbk::TraceArgs{};
   a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
+  a.wnodes = scene->wnodes;
   a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
   a.order = static_cast<const uint32_t*>(order);
   a.dirs = p->dirs->d_dirs; a.dir_order = p->dirs->d_order; a.S = p->dirs->n;
@@ -1088,7 +1090,7 @@ static vlbk::FusedSched fused_sched(const vlb_batch_schedule& sc) {
 // The scene, shading, probe and direction fields of one bake as a job of the
 // fused lane walk (the fused-projection fields are set by the caller).
 static void job_from_trace(const vlbk::TraceArgs& a, vlbk::BakeJobDev* j) {
-  j->nodes = a.nodes; j->tris = a.tris; j->albedo = a.albedo; j->ntris = a.ntris;
+  j->nodes = a.nodes; j->wnodes = a.wnodes; j->tris = a.tris; j->albedo = a.albedo; j->ntris = a.ntris;
   j->tmin = a.tmin; j->tmax = a.tmax; j->bias = a.bias;
   j->sun = a.sun; j->sun_inv = a.sun_inv; j->sun_scale = a.sun_scale;
   j->sky = a.sky; j->sky_n = a.sky_n; j->err = a.err;
@@ -1240,7 +1242,7 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
   out[2] = h[0];
   out[3] = h[1];
   out[4] = h[3];
-  out[5] = 0;
+  out[5] = a.lane && a.wnodes && !a.grid_hdr ? 96 : 64;
   return VLB_OK;
 }
 
@@ -1462,6 +1464,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     const BatchGroup& g = pl.groups[b.group];
     vlbk::BakeJobDev& d = table[t];
     d.nodes = j.scene->nodes; d.tris = j.scene->tris; d.albedo = j.scene->albedo; d.ntris = j.scene->ntris;
+    d.wnodes = j.scene->wnodes;
     d.tmin = p->tmin; d.tmax = p->tmax; d.bias = p->shadow_bias;
     d.sun = make_float3(float(p->sun_dir[0] / b.sun_len), float(p->sun_dir[1] / b.sun_len),
                         float(p->sun_dir[2] / b.sun_len));

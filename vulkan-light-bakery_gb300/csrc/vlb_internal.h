@@ -23,8 +23,10 @@ enum ErrSlot : int {
   kErrSlots = 8
 };
 
-// Sizes of the bake's trace kernels.
+// Sizes of the bake's trace kernels: the warp stack of the packet walk and
+// the per-lane stacks of the lane walks (a wide node pushes up to 7 children).
 constexpr int kTraceStack = 64;
+constexpr int kLaneStack = 96;
 
 // ---- skybox projection ------------------------------------------------------
 struct SkyboxArgs {
@@ -124,6 +126,7 @@ int launch_probe_order(const float* probes, uint32_t n, const float bounds[6], u
 // ---- trace + shade --------------------------------------------------------------
 struct TraceArgs {
   const float4* nodes;
+  const float4* wnodes;   // 8-wide quantised tree: the lane walks use it when set (same results)
   const float4* tris;
   const float4* albedo;
   uint32_t ntris;
@@ -194,6 +197,7 @@ void launch_trace_fused(const TraceArgs& a, int num_sms, cudaStream_t s);
 struct BakeJobDev {
   // scene and shading (the fields trace_sample reads)
   const float4* nodes;
+  const float4* wnodes;   // 8-wide quantised tree or null
   const float4* tris;
   const float4* albedo;
   uint32_t ntris;
@@ -316,6 +320,9 @@ vlb_status batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const JobExt* ex
                         const vlb_bake_params* params, const vlb_batch_schedule& sc, bool* host_out_any);
 // Launch-error check, and (sync) stream synchronisation + device error counters.
 vlb_status ctx_finish(vlb_ctx* ctx, bool sync);
+// Collapses the scene's binary traversal tree into the 8-wide quantised tree
+// (sc->wnodes, sc->nwide; wide_bvh.cpp).  Synchronous.
+vlb_status build_wide(vlb_ctx* ctx, vlb_scene* sc);
 vlb_status ctx_fail(vlb_ctx* ctx, vlb_status s, const char* msg);
 }  // namespace vlbh
 
@@ -361,6 +368,8 @@ struct vlb_scene {
   int32_t* child = nullptr;
   float* box = nullptr;
   float4* nodes = nullptr;
+  float4* wnodes = nullptr;  // 8-wide quantised traversal tree (wide_bvh.cpp), or null
+  uint32_t nwide = 0;
   float4* tris = nullptr;
   float4* albedo = nullptr;
   uint64_t bytes = 0;

@@ -26,7 +26,7 @@ SKY_REF_BGRA_SWAP = 1
 PREC_FP32, PREC_FUSED, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
 BAKE_FORCE_FUSED_KERNEL = 1
 BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE, BAKE_TRAVERSAL_GRID = 2, 4, 8
-SCENE_TRAVERSAL_LBVH = 1
+SCENE_TRAVERSAL_LBVH, SCENE_TRAVERSAL_WIDE = 1, 2
 DTYPE_F32, DTYPE_BF16, DTYPE_BF16_SPLIT = 0, 1, 2
 
 
@@ -574,7 +574,7 @@ def trace_stats(ctx: Context, scene: "Scene", probes, params: BakeParams) -> dic
     out = np.zeros(6, np.uint64)
     ctx.check(lib.vlb_bake_trace_stats(ctx.h, scene.h, _ptr(pr), n, C.byref(params), _ptr(out)))
     return {"rays": int(out[0]), "shadow_rays": int(out[1]), "node_fetches": int(out[2]),
-            "tri_fetches": int(out[3]), "node_tests": int(out[4])}
+            "tri_fetches": int(out[3]), "node_tests": int(out[4]), "node_bytes": int(out[5])}
 
 
 class Scene:
