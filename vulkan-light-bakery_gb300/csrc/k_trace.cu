@@ -226,7 +226,7 @@ __device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, 
   }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool WIDE>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
       lr_park(L, stack);
       const bool at_node = L.has && L.cur >= 0;
       if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
-      if (at_node) lr_node<COUNT>(a, L, stack, w);
+      if (at_node) lr_node<COUNT, TraceArgs, WIDE>(a, L, stack, w);
     }
     lr_park(L, stack);
     if (!L.has) continue;
@@ -282,9 +282,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
   }
 }
 
-template <bool COUNT>
+template <bool COUNT, bool WIDE>
 static void launch_dyn(const TraceArgs& a, int num_sms, cudaStream_t s) {
-  auto kern = k_trace_dyn<COUNT>;
+  auto kern = k_trace_dyn<COUNT, WIDE>;
   static int per_sm = 0;
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0);
@@ -666,8 +666,13 @@ void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
     return;
   }
   if (trace_dyn_supported(a)) {
-    if (a.counters) launch_dyn<true>(a, num_sms, s);
-    else launch_dyn<false>(a, num_sms, s);
+    if (a.wnodes) {
+      if (a.counters) launch_dyn<true, true>(a, num_sms, s);
+      else launch_dyn<false, true>(a, num_sms, s);
+    } else {
+      if (a.counters) launch_dyn<true, false>(a, num_sms, s);
+      else launch_dyn<false, false>(a, num_sms, s);
+    }
     return;
   }
   if (a.counters) launch<0, 1, true>(a, num_sms, s);

@@ -417,7 +417,26 @@ struct LaneRay {
   RayCtx ray;
   int cur = 0, sp = 0, slot = -1, id = -1, leaf = -1;
   float tb = 0.f, lit = 0.f;
+  // the lane's previous primary hit and shadow occluder (triangle slots or
+  // -1): tested first by its next rays (see lr_start)
+  int hprev = -1, oprev = -1;
 };
+
+// Warm start.  A lane's consecutive rays mostly share a probe and take
+// neighbouring directions, so they often hit the same triangle, and shadow
+// rays from nearby points toward the sun are often blocked by the same
+// occluder.  Testing that triangle before the walk starts only tightens the
+// best distance (or ends an occluded shadow walk at once): the closest hit is
+// the minimum over all triangles with the same tie rule whatever order they
+// are tested in, and an occluded shadow ray is occluded by any occluder, so
+// every ray's result is unchanged.  A slot is tested only if it is a slot of
+// the current scene (a lane of a batch may change scenes between rays).
+template <class A>
+__device__ __forceinline__ float lr_try(const A& a, const LaneRay& L, int ts, int* id) {
+  const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
+  *id = __float_as_int(v0.w);
+  return tri_hit(L.ray, v0, e1, e2);
+}
 
 // A: TraceArgs or BakeJobDev (scene, shading, probes and dirs fields).
 template <class A>
@@ -438,6 +457,11 @@ __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uin
   L.id = -1;
   L.leaf = -1;
   L.tb = a.tmax;
+  if (L.hprev >= 0 && uint32_t(L.hprev) < a.ntris) {
+    int id;
+    const float t = lr_try(a, L, L.hprev, &id);
+    if (t > a.tmin && t < L.tb) { L.tb = t; L.slot = L.hprev; L.id = id; }
+  }
 }
 
 // After a walk.  A finished primary walk is shaded: a miss takes the sky, a
@@ -449,6 +473,7 @@ template <bool COUNT, class A>
 __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Work& w) {
   o = Shaded{0.f, 0.f, 0.f, -1, 2};
   if (!L.shadow) {
+    L.hprev = L.slot;
     if (L.slot < 0) {
       if (a.sky) {
         const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
@@ -474,10 +499,16 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
     L.sp = 0;
     L.slot = -1;
     L.tb = a.tmax;
+    if (L.oprev >= 0 && uint32_t(L.oprev) < a.ntris) {
+      int id;
+      const float t = lr_try(a, L, L.oprev, &id);
+      if (t > 0.0f && t < L.tb) { L.slot = L.oprev; L.cur = kWalkEnd; }
+    }
     return false;
   }
   o.tri = L.id;
   const bool occ = L.slot >= 0;
+  if (occ) L.oprev = L.slot;
   o.vis = occ ? 0 : 1;
   if (!occ) {
     const float4 alb = __ldg(a.albedo + L.id);
@@ -568,10 +599,12 @@ __device__ __forceinline__ void lr_node_wide(const A& a, LaneRay& L, int* stack,
   L.cur = next != kWalkEnd ? next : (L.sp ? stack[--L.sp] : kWalkEnd);
 }
 
-// One inner node: nearer hit child next, the farther one on the stack.
-template <bool COUNT, class A>
+// One inner node: nearer hit child next, the farther one on the stack.  WIDE:
+// the node is a node of the 8-wide tree (kernels built for it walk it when
+// the scene has one; the others walk the binary tree, with the same results).
+template <bool COUNT, class A, bool WIDE = false>
 __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work& w) {
-  if (a.wnodes) {
+  if constexpr (WIDE) {
     lr_node_wide<COUNT>(a, L, stack, w);
     return;
   }

@@ -1242,7 +1242,7 @@ vlb_status vlb_bake_trace_stats(vlb_ctx* ctx, const vlb_scene* scene, const floa
   out[2] = h[0];
   out[3] = h[1];
   out[4] = h[3];
-  out[5] = a.lane && a.wnodes && !a.grid_hdr ? 96 : 64;
+  out[5] = a.lane && a.wnodes && !a.grid_hdr ? 96 : 64;  // the tile lane walk walks the wide tree
   return VLB_OK;
 }
 
