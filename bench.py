@@ -54,8 +54,8 @@ METRIC_FULL = "probes/s, Grays/s, p99 bake latency: chosen vs plain FP32, <=1e-4
 # The headline kernel's per-launch figures from one ncu capture of the same
 # workload (profiles/trace_fused_c2.md gives the command): DRAM bytes read +
 # written, warp instructions issued, ncu's L1 and issue utilisation.
-TRACE_NCU = {"capture": "profiles/trace_fused_c2.md", "dram_bytes": None, "warp_instructions": None,
-             "l1tex_throughput_pct": None, "issue_active_pct": None}
+TRACE_NCU = {"capture": "profiles/trace_fused_c2.md", "dram_bytes": 490277888, "warp_instructions": 156708407819,
+             "l1tex_throughput_pct": 84.5, "issue_active_pct": 70.5}
 
 
 def parse():
@@ -684,7 +684,7 @@ def refbake_measure(ctx, torch, stream, steps, hbm_peak, reps=3):
     probes and output, L2 flushed before each bake."""
     import vlb
 
-    pos, idx, alb, sky, sun, _ = workload_inputs()
+    pos, idx, alb, sky, sun, _ = grid_probes(vlb, 64, (16, 16, 16))  # the config-1 scene
     scene = ctx.scene(pos, idx, alb)
     probes, _ = vlb.probe_grid_ref_order(scene.bounds(include_origin=True), (7, 7, 7))
     P, W, H = probes.shape[0], 3141, 1000
