@@ -76,6 +76,18 @@ vlb_status vlb_ctx_profile_read(vlb_ctx* ctx, vlb_kernel_time* out, uint32_t cap
 vlb_status vlb_ctx_profile_reset(vlb_ctx* ctx);
 /* Kernels launched by the library on this context since creation. */
 uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx);
+/* Test hook (no reference counterpart; the reference's only failure path is
+ * an unbounded fence wait whose result is printed, src/application.cpp:
+ * 265-273).  Makes the bounded device waits give up on purpose without
+ * faulting the GPU: with VLB_HOOK_HOLD_PRODUCER the copy-issuing thread of
+ * the TMA pipelines (the skybox projection's producer warp, the tcgen05
+ * projection's TMA thread) issues nothing, so no copy is ever in flight;
+ * each waiting thread gives up after `wait_polls` mbarrier polls (0: the
+ * library's bound), the kernel stops (the tcgen05 kernel frees its tensor
+ * memory) and the call returns VLB_ERR_TIMEOUT.  hook 0 clears it; the
+ * context stays usable and the next call succeeds. */
+#define VLB_HOOK_HOLD_PRODUCER 1u
+vlb_status vlb_ctx_test_hook(vlb_ctx* ctx, uint32_t hook, uint32_t wait_polls);
 
 /* ---- probe grid -----------------------------------------------------------
  * Replaces LightBaker::probePositionsFromBoudingBox
@@ -219,7 +231,8 @@ typedef enum vlb_precision {
                          the hi/lo basis: half the tile bytes, ~8 mantissa bits per sample (about
                          2e-3 relative SH error on lit box scenes) */
 } vlb_precision;
-/* vlb_bake_params.flags: with VLB_PREC_FUSED, always run the one-kernel schedule. */
+/* vlb_bake_params.flags: with VLB_PREC_FUSED, always run the one-kernel packet
+ * schedule (sun shading only: VLB_ERR_UNSUPPORTED with VLB_SHADE_REF_PHONG). */
 #define VLB_BAKE_FORCE_FUSED_KERNEL 1u
 /* vlb_bake_params.flags: traversal mode.  Packet: a warp walks the union of
  * its 32 probes' BVH paths once (coherent probes); lane: every ray walks its
@@ -243,7 +256,36 @@ typedef struct vlb_bake_params {
   float shadow_bias;      /* shadow origin offset along the normal; shaders/env_map.rchit:81 uses .005 */
   const vlb_dirset* dirs; /* required */
   const vlb_sky* sky;     /* NULL: black sky */
+  uint32_t shading;       /* vlb_shading */
+  float light_pos[3];     /* VLB_SHADE_REF_PHONG: the point light (default 1, 10, 1: env_map.rchit:25) */
 } vlb_bake_params;
+/* vlb_bake_params.shading.
+ * VLB_SHADE_LAMBERT_SUN (the benchmark configs): closest hit; the geometric
+ * normal facing the ray; radiance = albedo * sun_intensity/pi * max(0, n.l) *
+ * visibility of a shadow ray from hit + bias*n toward the sun; a miss takes
+ * the sky cubemap (nearest texel) or black.
+ * VLB_SHADE_REF_PHONG (the reference baker's own shading, replaces
+ * shaders/env_map.rchit:51-102 with shaders/shadow.rmiss:6-9 and
+ * shaders/main.rmiss:37-41): the normal of the triangle's winding (not turned
+ * toward the ray; the reference interpolates the glTF vertex normals, which
+ * equal it on flat-shaded geometry), L = normalize(light_pos - hit), a
+ * shadow ray from hit + bias*n along L, any hit in (0, |light_pos - hit|),
+ * traced only when n.L > 0; if it is not occluded, diffuse = 0.5 n.L and
+ * specular = 0.5 max(0, reflect(L, n).d)^16 (ambient 0); the sample is
+ * sRGB(albedo * (diffuse + specular)), and a miss sRGB(sky texel) or black
+ * (the reference's bake binds no sky); every sample is then stored as
+ * 8-bit UNORM (round(clamp(x, 0, 1) * 255) / 255) as the reference's
+ * R8G8B8A8 env map (src/baker/env_map_generator.hpp:39) stores it, and the
+ * projection reads the stored value.  The tile walks only (packet and grid
+ * requests walk per lane). */
+typedef enum vlb_shading { VLB_SHADE_LAMBERT_SUN = 0, VLB_SHADE_REF_PHONG = 1 } vlb_shading;
+/* vlb_bake_params.flags: the reference's carry-over accumulator.  The
+ * reference never clears its coefficient buffer between probes
+ * (src/baker/light_baker.cpp:110-121, :298-322), so it writes for probe i
+ * the sum of probes 0..i.  With this flag out[i] is that running sum, in the
+ * order of probe_xyz, added in FP64 and rounded once (the reference's is a
+ * racy FP32 sum); vlb_bake only (not batches or the service). */
+#define VLB_BAKE_REF_ACCUMULATE 16u
 void vlb_bake_params_default(vlb_bake_params* p);
 
 /* Per-ray outputs for parity checks (any may be NULL; host or device):

@@ -39,7 +39,7 @@ def _load():
         "orc_lbvh_build": (I32, [P, U32, P, U32, P, P, P, P]),
         "orc_scene_create": (P, [P, U32, P, U32, P]),
         "orc_scene_destroy": (None, [P]),
-        "orc_bake": (None, [P, P, U32, P, U32, P, I32, P, F, F, F, F, P, U32, P, P, I32, P, P, P, P, P]),
+        "orc_bake": (None, [P, P, U32, P, U32, P, I32, P, F, F, F, F, P, U32, P, P, I32, P, P, P, P, P, I32, P]),
         "orc_ray_tri": (I32, [P, P, P, I32, P, P, P, P]),
         "orc_shadow_margin": (D, [P, P, P, D, D]),
         "orc_closest_hit": (None, [P, P, P, D, D, P, P]),
@@ -212,7 +212,9 @@ class Scene:
             self.h = None
 
     def bake(self, probes, dirs32, basis, sun, sun_intensity=5.0, tmin=1e-3, tmax=1e4, bias=5e-3, sky=None,
-             sky_n=0, force_hit=None, force_vis=None, per_ray=False, nthreads=None):
+             sky_n=0, force_hit=None, force_vis=None, per_ray=False, nthreads=None, shading=0, light=(1.0, 10.0, 1.0)):
+        """shading 0: Lambert + sun (the configs); 1: the reference baker's
+        Phong + sRGB + 8-bit UNORM samples with the point light `light`."""
         pr = _c(probes, np.float32).reshape(-1, 3)
         d = _c(dirs32, np.float32).reshape(-1, 3)
         B = _c(basis, np.float64)
@@ -229,7 +231,8 @@ class Scene:
             edge = np.empty((np_, S), np.float64)
             rad = np.empty((np_, S, 3), np.float32)
         lib.orc_bake(self.h, _p(pr), np_, _p(d), S, _p(B), K, _p(sunv), sun_intensity, tmin, tmax, bias, _p(skyv),
-                     sky_n, _p(fh), _p(fv), nthreads or NTHREADS, _p(out), _p(hit), _p(vis), _p(edge), _p(rad))
+                     sky_n, _p(fh), _p(fv), nthreads or NTHREADS, _p(out), _p(hit), _p(vis), _p(edge), _p(rad),
+                     int(shading), _p(_c(light, np.float32)))
         if per_ray:
             return out, hit, vis, edge, rad
         return out

@@ -414,7 +414,49 @@ struct BakeCfg {
   const float* sky; uint32_t sky_n;  // cubemap 6*n*n*3 or null
   const int32_t* force_hit;          // optional per-ray decisions to replay (np*ns) or null
   const uint8_t* force_vis;
+  int shading;                       // 0 Lambert + sun, 1 the reference's Phong + sRGB + UNORM8
+  double light[3];                   // shading 1: the point light
 };
+
+// The reference baker's sample encoding: sRGB (shaders/env_map.rchit:27-34,
+// main.rmiss:9-16), then the 8-bit UNORM store of its R8G8B8A8 env map
+// (src/baker/env_map_generator.hpp:39), read back as k/255 by sh.comp.
+double ref_srgb(double c) { return c < 0.0031308 ? c * 12.92 : 1.055 * std::pow(c, 1.0 / 2.4) - 0.055; }
+double ref_unorm8(double c) { return std::nearbyint(std::min(1.0, std::max(0.0, c)) * 255.0) / 255.0; }
+
+// shaders/env_map.rchit:51-102 with shadow.rmiss:6-9 (shading 1).  The normal
+// is the triangle's winding normal (the mesh's flat vertex normal), not turned
+// toward the ray; L = normalize(light - hit); a shadow ray from hit + bias*n
+// along L, any hit in (0, |light - hit|), traced only when n.L > 0; lit:
+// diffuse 0.5 n.L + specular 0.5 max(0, reflect(L, n).d)^16 (ambient 0).
+void shade_ref(const Scene& sc, const BakeCfg& c, size_t r, const double* o, const double* d, const Hit& h,
+               double* L, uint8_t* vis_out) {
+  const Tri& tr = sc.tris[h.tri];
+  double n[3]; cross3(tr.e1, tr.e2, n);
+  const double nl = std::sqrt(dot3(n, n));
+  n[0] /= nl; n[1] /= nl; n[2] /= nl;
+  const double P[3] = {o[0] + h.t * d[0], o[1] + h.t * d[1], o[2] + h.t * d[2]};
+  double S[3] = {c.light[0] - P[0], c.light[1] - P[1], c.light[2] - P[2]};
+  const double len = std::sqrt(dot3(S, S));
+  const double Ld[3] = {S[0] / len, S[1] / len, S[2] / len};
+  const double sdn = std::max(dot3(Ld, n), 0.0);
+  L[0] = L[1] = L[2] = 0.0;
+  if (!(sdn > 0.0)) {
+    if (vis_out) *vis_out = 2;
+    return;
+  }
+  const double Q[3] = {P[0] + c.bias * n[0], P[1] + c.bias * n[1], P[2] + c.bias * n[2]};
+  bool lit;
+  if (c.force_vis && c.force_vis[r] != 2) lit = c.force_vis[r] == 1;
+  else lit = !any_hit(sc, Q, Ld, 0.0, len);
+  if (vis_out) *vis_out = lit ? 1 : 0;
+  if (!lit) return;
+  const double rd = 2.0 * dot3(n, Ld);
+  const double R[3] = {Ld[0] - rd * n[0], Ld[1] - rd * n[1], Ld[2] - rd * n[2]};
+  const double sp = std::pow(std::max(dot3(R, d), 0.0), 16.0);
+  const double k = 0.5 * sdn + 0.5 * sp;
+  for (int ch = 0; ch < 3; ++ch) L[ch] = ref_unorm8(ref_srgb(sc.albedo[3 * h.tri + ch] * k));
+}
 
 void sky_radiance(const BakeCfg& c, const float* d, double* L) {
   if (!c.sky) { L[0] = L[1] = L[2] = 0.0; return; }
@@ -441,12 +483,18 @@ void shade_ray(const Scene& sc, const BakeCfg& c, uint32_t p, uint32_t s, double
   if (hit_out) *hit_out = h.tri;
   if (h.tri < 0) {
     sky_radiance(c, df, L);
+    if (c.shading == 1)
+      for (int ch = 0; ch < 3; ++ch) L[ch] = ref_unorm8(ref_srgb(L[ch]));
     if (vis_out) *vis_out = 2;
     if (edge_out) *edge_out = INFINITY;
     return;
   }
   const Tri& tr = sc.tris[h.tri];
   if (edge_out) *edge_out = edge_distance(tr, h.b1, h.b2);
+  if (c.shading == 1) {
+    shade_ref(sc, c, r, o, d, h, L, vis_out);
+    return;
+  }
   double n[3]; cross3(tr.e1, tr.e2, n);
   const double nl = std::sqrt(dot3(n, n));
   n[0] /= nl; n[1] /= nl; n[2] /= nl;
@@ -827,7 +875,7 @@ void orc_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
 void orc_bake(const void* scene, const float* probes, uint32_t np, const float* dirs, uint32_t ns, const double* basis,
               int K, const float* sun_dir, float sun_intensity, float tmin, float tmax, float bias, const float* sky,
               uint32_t sky_n, const int32_t* force_hit, const uint8_t* force_vis, int nthreads, double* out_sh,
-              int32_t* hit_ids, uint8_t* vis, double* edge, float* radiance) {
+              int32_t* hit_ids, uint8_t* vis, double* edge, float* radiance, int shading, const float* light) {
   const Scene& sc = *static_cast<const Scene*>(scene);
   BakeCfg c{};
   c.probes = probes; c.np = np; c.dirs = dirs; c.ns = ns; c.basis = basis; c.K = K;
@@ -836,6 +884,8 @@ void orc_bake(const void* scene, const float* probes, uint32_t np, const float* 
   c.sun_scale = double(sun_intensity) / 3.141592653589793;
   c.tmin = tmin; c.tmax = tmax; c.bias = bias; c.sky = sky; c.sky_n = sky_n;
   c.force_hit = force_hit; c.force_vis = force_vis;
+  c.shading = shading;
+  for (int a = 0; a < 3; ++a) c.light[a] = light ? light[a] : 0.0;
   parallel_for(np, nthreads, [&](uint32_t p) {
     std::vector<double> acc(size_t(K) * 3, 0.0);
     for (uint32_t s = 0; s < ns; ++s) {

@@ -26,8 +26,11 @@ def per_probe_rel(a, b):
     return np.where(den > 0, num / np.maximum(den, 1e-300), num)
 
 
-def classify(orc, probes, dirs32, sun, gpu_hit, gpu_vis, o_hit, o_vis, o_edge, tmin=1e-3, tmax=1e4, bias=5e-3):
-    """Returns counts of explained / unexplained decision mismatches."""
+def classify(orc, probes, dirs32, sun, gpu_hit, gpu_vis, o_hit, o_vis, o_edge, tmin=1e-3, tmax=1e4, bias=5e-3,
+             light=None):
+    """Returns counts of explained / unexplained decision mismatches.  With
+    `light` the shadow rays are the reference shading's (the winding normal,
+    toward the point light, ending at it); else the sun's."""
     res = {"rays": int(gpu_hit.size), "hit_mismatch": 0, "hit_explained": 0, "shadow_mismatch": 0,
            "shadow_explained": 0, "unexplained": []}
     sunv = np.asarray(sun, np.float64)
@@ -60,11 +63,23 @@ def classify(orc, probes, dirs32, sun, gpu_hit, gpu_vis, o_hit, o_vis, o_edge, t
         v = orc.pos[tri].astype(np.float64)
         n = np.cross(v[1] - v[0], v[2] - v[0])
         n /= np.linalg.norm(n)
-        if n @ d > 0:
-            n = -n
-        ndl = n @ sunv
-        m = orc.shadow_margin(P + bias * n, sunv, 0.0, tmax)
-        if abs(m) < SHADOW_TOL or abs(ndl) < 1e-6:
+        if light is None:
+            if n @ d > 0:
+                n = -n
+            ndl = n @ sunv
+            m = orc.shadow_margin(P + bias * n, sunv, 0.0, tmax)
+            end_flip = False
+        else:
+            S = np.asarray(light, np.float64) - P
+            ln = np.linalg.norm(S)
+            Ld = S / ln
+            ndl = n @ Ld
+            m = orc.shadow_margin(P + bias * n, Ld, 0.0, ln)
+            # a blocker at the light itself: the interval's end decides it
+            lo = orc.shadow_margin(P + bias * n, Ld, 0.0, ln * (1 - SHADOW_TOL))
+            hi = orc.shadow_margin(P + bias * n, Ld, 0.0, ln * (1 + SHADOW_TOL))
+            end_flip = (lo >= 0) != (hi >= 0)
+        if abs(m) < SHADOW_TOL or abs(ndl) < 1e-6 or end_flip:
             res["shadow_explained"] += 1
         else:
             res["unexplained"].append(("shadow", int(p), int(s), m))

@@ -57,6 +57,10 @@ EXPECT = {
     "shaders/main.rmiss:40": "sRGB(",
     "shaders/main.rchit:49-56": "vec3 sRGB",
     "shaders/sh_sum.comp:51": "1250.0f",
+    "shaders/env_map.rchit:51-102": "traceRayEXT",
+    "shaders/shadow.rmiss:6-9": "inShadow = false",
+    "src/baker/light_baker.cpp:110-121": "SHCoeffs = createBuffer",
+    "src/baker/light_baker.cpp:298-322": "memcpy(ptr, dataPtr",
 }
 
 CITE = re.compile(r"((?:src|shaders)/[A-Za-z_/]+\.(?:cpp|hpp|h|comp|rgen|rchit|rmiss)):(\d+)(?:-(\d+))?"

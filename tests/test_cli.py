@@ -113,6 +113,24 @@ def test_cli_bake_matches_library(ctx, tmp_path, dirs, lmax, prec):
 
 
 @pytest.mark.gpu
+def test_cli_reference_shading_and_running_sums(ctx, tmp_path):
+    """--shading ref --light --accumulate: the library's bake with the
+    reference's shading and its carry-over sums."""
+    scene_path = write_scene(tmp_path / "r.gltf", seed=2)
+    r = run_cli(scene_path, "--dirs", "equirect:64x32", "--shading", "ref", "--light", 0.5, 4, 0.5, "--accumulate",
+                "--precision", "fp32")
+    assert r.returncode == 0, r.stderr
+    step, K, data = vlb.gltf_read_light((tmp_path / "baked_r.gltf").read_text())
+    got = np.frombuffer(data, np.float32).reshape(-1, K, 3)
+    scene = ctx.scene_gltf(scene_path)
+    probes, _ = vlb.probe_grid_ref_order(scene.bounds(include_origin=True), (7, 7, 7))
+    p = vlb.bake_params(ctx.equirect(64, 32), 3, vlb.PREC_FP32, shading=vlb.SHADE_REF_PHONG,
+                        light_pos=(0.5, 4, 0.5), flags=vlb.BAKE_REF_ACCUMULATE)
+    np.testing.assert_array_equal(got, ctx.bake(scene, probes, p))
+    assert run_cli(scene_path, "--shading", "phong").returncode == 1
+
+
+@pytest.mark.gpu
 def test_cli_counts_and_out(ctx, tmp_path):
     scene_path = write_scene(tmp_path / "s.gltf", seed=5, nboxes=4)
     out = tmp_path / "sub" / "x.gltf"

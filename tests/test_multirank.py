@@ -29,7 +29,7 @@ def _rank(rank, world, port, q):
     times = [10.0, 25.0, 17.5, 3.0]
     mx = bench.max_over_ranks(times[rank], dist, "cpu")
     rate = bench.whole_job_rate(4096 * 20, world, mx)
-    ref = bench.run_reference(type("A", (), {"cpu_probes": 8, "warmup": 0, "steps": 1, "gpus": world})(), rank)
+    ref = bench.run_reference(type("A", (), {"ref_probes": 8, "warmup": 0, "steps": 1, "gpus": world})(), rank)
     dist.barrier()
     dist.destroy_process_group()
     q.put((rank, mx, rate, ref is None))

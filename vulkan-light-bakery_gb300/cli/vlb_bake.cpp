@@ -20,6 +20,12 @@
 //   --sun X Y Z          direction toward the sun (default 0 1 0)
 //   --intensity I        sun intensity (default 5)
 //   --precision fp32|fused|mixed|bf16   (default fused: FP32 arithmetic, one kernel)
+//   --shading sun|ref    sun: Lambert + the sun above (default); ref: the
+//                        reference baker's own shading (point light, Phong,
+//                        sRGB, 8-bit samples; shaders/env_map.rchit:51-102)
+//   --light X Y Z        the ref shading's point light (default 1 10 1)
+//   --accumulate         write the reference's running sums (probe i holds
+//                        probes 0..i: its coefficient buffer is never cleared)
 //   --out PATH           output file (default baked_<name> next to the input)
 //   --device N           CUDA device (default 0)
 #include <cstdio>
@@ -57,7 +63,9 @@ int main(int argc, char** argv) {
     uint32_t counts[3] = {7, 7, 7};
     uint32_t lmax = 3;
     int device = 0;
-    float sun[3] = {0.f, 1.f, 0.f}, intensity = 5.f;
+    float sun[3] = {0.f, 1.f, 0.f}, intensity = 5.f, light[3] = {1.f, 10.f, 1.f};
+    std::string shading = "sun";
+    bool accumulate = false;
     for (int i = 2; i < argc; ++i) {
       const std::string o = argv[i];
       auto need = [&](int n) {
@@ -69,6 +77,9 @@ int main(int argc, char** argv) {
       else if (o == "--sun") { need(3); for (float& c : sun) c = float(std::atof(argv[++i])); }
       else if (o == "--intensity") { need(1); intensity = float(std::atof(argv[++i])); }
       else if (o == "--precision") { need(1); prec = argv[++i]; }
+      else if (o == "--shading") { need(1); shading = argv[++i]; }
+      else if (o == "--light") { need(3); for (float& c : light) c = float(std::atof(argv[++i])); }
+      else if (o == "--accumulate") accumulate = true;
       else if (o == "--out") { need(1); out = argv[++i]; }
       else if (o == "--device") { need(1); device = std::atoi(argv[++i]); }
       else throw std::runtime_error("unknown option " + o);
@@ -80,6 +91,7 @@ int main(int argc, char** argv) {
       throw std::runtime_error("bad --dirs " + dirs);
     if (prec != "fp32" && prec != "fused" && prec != "mixed" && prec != "bf16")
       throw std::runtime_error("bad --precision " + prec);
+    if (shading != "sun" && shading != "ref") throw std::runtime_error("bad --shading " + shading);
     const std::string src = read_text(in);  // the document re-written after the bake
     if (src.compare(0, 4, "glTF") == 0)
       throw std::runtime_error("binary glTF input: the baked file is written from a JSON .gltf document");
@@ -117,6 +129,9 @@ int main(int argc, char** argv) {
                                     : VLB_PREC_FUSED;
     for (int a = 0; a < 3; ++a) p.sun_dir[a] = sun[a];
     p.sun_intensity = intensity;
+    p.shading = shading == "ref" ? VLB_SHADE_REF_PHONG : VLB_SHADE_LAMBERT_SUN;
+    for (int a = 0; a < 3; ++a) p.light_pos[a] = light[a];
+    if (accumulate) p.flags |= VLB_BAKE_REF_ACCUMULATE;
     p.dirs = ds;
     const uint32_t K = (lmax + 1) * (lmax + 1);
     std::vector<float> sh(np * K * 3);

@@ -286,3 +286,39 @@ void launch_sh_eval_dirs(const float* coeffs, uint32_t lmax, const float* dirs, 
 }
 
 }  // namespace vlbk
+
+namespace vlbk {
+
+// The reference's carry-over accumulator (vlb_bake VLB_BAKE_REF_ACCUMULATE):
+// out[p][v] <- sum of out[q][v] over q <= p, in FP64, rounded once.  One CTA
+// per value v walks the probes in chunks of 256: a block-wide inclusive scan
+// of the chunk plus the running carry of the chunks before it (a fixed order).
+__global__ void __launch_bounds__(256) k_probe_prefix(float* __restrict__ out, uint32_t nprobes, uint32_t V) {
+  __shared__ double wsum[8];
+  const uint32_t v = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double carry = 0.0;
+  for (uint32_t p0 = 0; p0 < nprobes; p0 += 256) {
+    const uint32_t p = p0 + tid;
+    double x = p < nprobes ? double(out[size_t(p) * V + v]) : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, x, o);
+      if (int(lane) >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    double before = carry;
+    for (uint32_t k = 0; k < warp; ++k) before += wsum[k];
+    double total = carry;
+    for (uint32_t k = 0; k < 8; ++k) total += wsum[k];
+    if (p < nprobes) out[size_t(p) * V + v] = float(before + x);
+    __syncthreads();
+    carry = total;
+  }
+}
+
+void launch_probe_prefix(float* out, uint32_t nprobes, uint32_t V, cudaStream_t s) {
+  if (nprobes && V) k_probe_prefix<<<V, 256, 0, s>>>(out, nprobes, V);
+}
+
+}  // namespace vlbk

@@ -117,7 +117,7 @@ struct TcShared {
 
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_project_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t rows,
-                 uint32_t S, uint32_t K, float* __restrict__ out, int* err) {
+                 uint32_t S, uint32_t K, float* __restrict__ out, int* err, uint32_t hold, uint32_t polls) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ TcShared sh;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -142,12 +142,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t tmem = sh.tmem_base;
 
   if (warp == 0) {
-    if (lane == 0) {
+    if (lane == 0 && !hold) {  // hold (a test hook): no copy is issued, the waits below give up
       uint32_t issued = 0;
       for (uint32_t tile = blockIdx.x; tile < ntiles && !sh.abort; tile += gridDim.x) {
         for (uint32_t kb = 0; kb < nkb; ++kb, ++issued) {
           const uint32_t st = issued % kStages, round = issued / kStages;
-          if (!mbar_wait_bounded(&sh.empty[st], (round & 1u) ^ 1u, err)) { sh.abort = 1; break; }
+          if (!mbar_wait_bounded(&sh.empty[st], (round & 1u) ^ 1u, err, polls)) { sh.abort = 1; break; }
           mbar_arrive_expect_tx(&sh.full[st], kStageBytes);
           uint8_t* sa = gbase + size_t(st) * kStageBytes;
           tma_load_2d(sa, &tmA, int(kb * kTileK), int(tile * kTileM), &sh.full[st]);
@@ -164,12 +164,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t used = 0, it = 0;
       for (uint32_t tile = blockIdx.x; tile < ntiles && !sh.abort; tile += gridDim.x, ++it) {
         const uint32_t acc = it & 1u;
-        if (!mbar_wait_bounded(&sh.acc_empty[acc], ((it >> 1) & 1u) ^ 1u, err)) { sh.abort = 1; break; }
+        if (!mbar_wait_bounded(&sh.acc_empty[acc], ((it >> 1) & 1u) ^ 1u, err, polls)) { sh.abort = 1; break; }
         tc_fence_after();
         const uint32_t d = tmem + acc * kTileN;
         for (uint32_t kb = 0; kb < nkb; ++kb, ++used) {
           const uint32_t st = used % kStages;
-          if (!mbar_wait_bounded(&sh.full[st], (used / kStages) & 1u, err)) { sh.abort = 1; break; }
+          if (!mbar_wait_bounded(&sh.full[st], (used / kStages) & 1u, err, polls)) { sh.abort = 1; break; }
           tc_fence_after();
           const uint32_t sa = base + st * kStageBytes, sb = sa + kStageA;
 #pragma unroll
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t it = 0;
     for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
       const uint32_t acc = it & 1u;
-      if (!mbar_wait_bounded(&sh.acc_full[acc], (it >> 1) & 1u, err)) { sh.abort = 1; break; }
+      if (!mbar_wait_bounded(&sh.acc_full[acc], (it >> 1) & 1u, err, polls)) { sh.abort = 1; break; }
       tc_fence_after();
       float v[32];
       tmem_ld32(tmem + (lane_base << 16) + acc * kTileN, v);
@@ -250,7 +250,8 @@ bool project_tc_supported(const void* radiance, uint32_t S) {
 }
 
 int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const uint16_t* basis_bt,
-                      uint32_t bt_pitch, uint32_t K, float* out, int* err, int num_sms, cudaStream_t s) {
+                      uint32_t bt_pitch, uint32_t K, float* out, int* err, int num_sms, cudaStream_t s,
+                      uint32_t hold, uint32_t wait_polls) {
   const uint32_t rows = nprobes * 3;
   if (rows == 0) return 0;
   CUtensorMap ta, tb;
@@ -260,7 +261,8 @@ int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, co
   smem_opt_in(k_project_tc, int(kSmemBytes), opted);
   const uint32_t ntiles = (rows + kTileM - 1) / kTileM;
   const uint32_t grid = std::min<uint32_t>(ntiles, uint32_t(num_sms));
-  k_project_tc<<<grid, kTcThreads, kSmemBytes, s>>>(ta, tb, rows, S, K, out, err);
+  k_project_tc<<<grid, kTcThreads, kSmemBytes, s>>>(ta, tb, rows, S, K, out, err, hold,
+                                                     wait_polls ? wait_polls : kWaitPolls);
   return 1;
 }
 

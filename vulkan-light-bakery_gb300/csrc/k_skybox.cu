@@ -177,12 +177,16 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
   }
   __syncthreads();
 
+  const uint32_t polls = a.wait_polls ? a.wait_polls : kWaitPolls;
   if (warp == kConsumerWarps) {  // producer warp
-    if (TMA && lane == 0) {
+    if (TMA && lane == 0 && !a.hold_producer) {  // hold (a test hook): nothing is issued, consumers give up
       It it{blockIdx.x, 0, 0};
       while (it.unit < units && !abort_flag) {
         const uint32_t st = it.seq % kSkyStages;
-        if (!mbar_wait_bounded(&empty[st], ((it.seq / kSkyStages) & 1u) ^ 1u, a.err)) { abort_flag = 1; break; }
+        if (!mbar_wait_bounded(&empty[st], ((it.seq / kSkyStages) & 1u) ^ 1u, a.err, polls)) {
+          abort_flag = 1;
+          break;
+        }
         uint32_t tb, nt, m0, gv;
         chunk_span(it, &tb, &nt, &m0, &gv);
         unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;
@@ -218,7 +222,7 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
     chunk_span(cons, &tb, &nt, &m0, &gv);
     const uint32_t st = cons.seq % kSkyStages;
     if constexpr (TMA) {
-      if (!mbar_wait_bounded(&full[st], (cons.seq / kSkyStages) & 1u, a.err)) abort_flag = 1;
+      if (!mbar_wait_bounded(&full[st], (cons.seq / kSkyStages) & 1u, a.err, polls)) abort_flag = 1;
     }
     if (abort_flag) break;
     const unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;

@@ -226,7 +226,7 @@ __device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, 
   }
 }
 
-template <bool COUNT, bool WIDE>
+template <bool COUNT, bool WIDE, bool REF>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
     if (L.leaf >= 0) lr_leaf<COUNT>(a, L, w);
     if (L.cur != kWalkEnd) continue;
     Shaded o;
-    if (!lr_finish<COUNT>(a, L, o, w)) continue;
+    if (!lr_finish<COUNT, TraceArgs, REF>(a, L, o, w)) continue;
     L.has = false;
     emit_tile(a, L, o);
   }
@@ -282,9 +282,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) 
   }
 }
 
-template <bool COUNT, bool WIDE>
+template <bool COUNT, bool WIDE, bool REF>
 static void launch_dyn(const TraceArgs& a, int num_sms, cudaStream_t s) {
-  auto kern = k_trace_dyn<COUNT, WIDE>;
+  auto kern = k_trace_dyn<COUNT, WIDE, REF>;
   static int per_sm = 0;
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0);
@@ -666,12 +666,15 @@ void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
     return;
   }
   if (trace_dyn_supported(a)) {
-    if (a.wnodes) {
-      if (a.counters) launch_dyn<true, true>(a, num_sms, s);
-      else launch_dyn<false, true>(a, num_sms, s);
+    if (a.shading == VLB_SHADE_REF_PHONG) {  // the wide tree is not built into these: the binary walk
+      if (a.counters) launch_dyn<true, false, true>(a, num_sms, s);
+      else launch_dyn<false, false, true>(a, num_sms, s);
+    } else if (a.wnodes) {
+      if (a.counters) launch_dyn<true, true, false>(a, num_sms, s);
+      else launch_dyn<false, true, false>(a, num_sms, s);
     } else {
-      if (a.counters) launch_dyn<true, false>(a, num_sms, s);
-      else launch_dyn<false, false>(a, num_sms, s);
+      if (a.counters) launch_dyn<true, false, false>(a, num_sms, s);
+      else launch_dyn<false, false, false>(a, num_sms, s);
     }
     return;
   }
@@ -707,6 +710,7 @@ __device__ __forceinline__ void batch_emit(const BakeJobDev& j, uint32_t p, uint
 // written after the primary walk; a relight starts from the kept hit with only
 // its shadow walk.  Every job walks per lane: results do not depend on the
 // traversal mode.
+template <bool REF>
 __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobDev* __restrict__ jobs, uint32_t njobs,
                                                                uint32_t total, uint32_t chunk, uint32_t* counter) {
   const uint32_t lane = threadIdx.x & 31;
@@ -745,7 +749,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
               L.tb = __int_as_float(h.y);
               L.id = h.x >= 0 ? __float_as_int(__ldg(j.tris + 3 * h.x).w) : -1;
               Shaded o;
-              if (lr_finish<false>(j, L, o, w)) {
+              if (lr_finish<false, BakeJobDev, REF>(j, L, o, w)) {
                 L.has = false;
                 batch_emit(j, L.p, L.s, o);
               }
@@ -771,24 +775,31 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
       if (L.cur != kWalkEnd) continue;
       if (!L.shadow && j.hits_out) j.hits_out[size_t(L.p) * j.S + L.s] = make_int2(L.slot, __float_as_int(L.tb));
       Shaded o;
-      if (!lr_finish<false>(j, L, o, w)) continue;
+      if (!lr_finish<false, BakeJobDev, REF>(j, L, o, w)) continue;
       L.has = false;
       batch_emit(j, L.p, L.s, o);
     }
   }
 }
 
-void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
-                        uint32_t* counter, int num_sms, cudaStream_t s) {
-  if (!total_rays || !njobs) return;
+template <bool REF>
+static void launch_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
+                         uint32_t* counter, int num_sms, cudaStream_t s) {
   static int per_sm = 0;
   if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch, kTraceThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch<REF>, kTraceThreads, 0);
     if (per_sm < 1) per_sm = 1;
   }
   const uint64_t ctas = std::min<uint64_t>((uint64_t(total_rays) / chunk + kTraceWarps - 1) / kTraceWarps + 1,
                                            uint64_t(num_sms) * per_sm);
-  k_trace_batch<<<uint32_t(ctas), kTraceThreads, 0, s>>>(jobs, njobs, total_rays, chunk, counter);
+  k_trace_batch<REF><<<uint32_t(ctas), kTraceThreads, 0, s>>>(jobs, njobs, total_rays, chunk, counter);
+}
+
+void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
+                        uint32_t* counter, bool ref_shading, int num_sms, cudaStream_t s) {
+  if (!total_rays || !njobs) return;
+  if (ref_shading) launch_batch<true>(jobs, njobs, total_rays, chunk, counter, num_sms, s);
+  else launch_batch<false>(jobs, njobs, total_rays, chunk, counter, num_sms, s);
 }
 
 __global__ void k_scatter_rows(const float* __restrict__ src, float* const* __restrict__ dst,

@@ -189,8 +189,9 @@ __device__ __forceinline__ void store_ray(FusedWarp& fw, const BakeJobDev& J, co
   }
 }
 
-// MINB: resident CTAs per SM the register allocation is sized for (7, 8 or 9).
-template <int K, bool MULTI, int MINB>
+// MINB: resident CTAs per SM the register allocation is sized for (7, 8 or 9);
+// REF: the reference's shading (vlb_shading VLB_SHADE_REF_PHONG).
+template <int K, bool MULTI, int MINB, bool REF>
 __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJobDev* __restrict__ jobs,
                                                                      const BakeJobDev one, uint32_t njobs,
                                                                      uint32_t total, uint32_t* counter,
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
             L.tb = __int_as_float(hk.y);
             L.id = hk.x >= 0 ? __float_as_int(__ldg(J.tris + 3 * hk.x).w) : -1;
             Shaded o;
-            if (lr_finish<false>(J, L, o, w)) {
+            if (lr_finish<false, BakeJobDev, REF>(J, L, o, w)) {
               L.has = false;
               done_now = true;
               store_ray(fw, J, L, o, lslot);
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
           if (!L.shadow && J.hits_out)
             J.hits_out[size_t(L.p) * J.S + L.s] = make_int2(L.slot, __float_as_int(L.tb));
           Shaded o;
-          if (lr_finish<false>(J, L, o, w)) {
+          if (lr_finish<false, BakeJobDev, REF>(J, L, o, w)) {
             L.has = false;
             done_now = true;
             store_ray(fw, J, L, o, lslot);
@@ -289,10 +290,10 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
   }
 }
 
-template <int K, bool MULTI, int MINB>
+template <int K, bool MULTI, int MINB, bool REF>
 static void launch_k(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njobs, uint32_t total,
                      uint32_t* counter, const FusedSched& sc, int num_sms, cudaStream_t s) {
-  auto kern = k_trace_fused<K, MULTI, MINB>;
+  auto kern = k_trace_fused<K, MULTI, MINB, REF>;
   static int per_sm = 0;
   if (!per_sm) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTraceThreads, 0);
@@ -325,9 +326,11 @@ static void launch_k(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njo
 template <int K, bool MULTI>
 static void launch_occ(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njobs, uint32_t total,
                        uint32_t* counter, const FusedSched& sc, int num_sms, cudaStream_t s) {
-  if (sc.ctas_per_sm == 7) launch_k<K, MULTI, 7>(jobs, one, njobs, total, counter, sc, num_sms, s);
-  else if (sc.ctas_per_sm == 9) launch_k<K, MULTI, 9>(jobs, one, njobs, total, counter, sc, num_sms, s);
-  else launch_k<K, MULTI, 8>(jobs, one, njobs, total, counter, sc, num_sms, s);
+  if (one.shading == VLB_SHADE_REF_PHONG)  // one register budget for the reference shading
+    launch_k<K, MULTI, 8, true>(jobs, one, njobs, total, counter, sc, num_sms, s);
+  else if (sc.ctas_per_sm == 7) launch_k<K, MULTI, 7, false>(jobs, one, njobs, total, counter, sc, num_sms, s);
+  else if (sc.ctas_per_sm == 9) launch_k<K, MULTI, 9, false>(jobs, one, njobs, total, counter, sc, num_sms, s);
+  else launch_k<K, MULTI, 8, false>(jobs, one, njobs, total, counter, sc, num_sms, s);
 }
 
 void launch_trace_fused_lane(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njobs, uint32_t total_items,

@@ -196,6 +196,8 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
       // the keeping bake's hits are written by its own trace launch: never in the same batch
       if (std::find(in_batch.begin(), in_batch.end(), r->relight_of) != in_batch.end()) break;
     }
+    // one batch bakes one shading (vlb_bake_batch's rule)
+    if (!take.empty() && r->params.shading != take.front()->params.shading) break;
     const uint32_t n = src ? src->n : r->n;
     const uint32_t S = src ? src->dirs->n : r->params.dirs->n;
     uint64_t b = transient_bytes(n, S, K, cfg.precision);

@@ -464,14 +464,75 @@ __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uin
   }
 }
 
-// After a walk.  A finished primary walk is shaded: a miss takes the sky, a
+// The reference baker's sample encoding: the sRGB curve of
+// shaders/env_map.rchit:27-34 (the same in main.rmiss:9-16), then the 8-bit
+// UNORM store of its R8G8B8A8 env map (round to nearest, clamped to [0, 1]).
+__device__ __forceinline__ float ref_srgb(float c) {
+  return c < 0.0031308f ? c * 12.92f : 1.055f * powf(c, 1.0f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ float ref_unorm8(float c) { return rintf(fminf(fmaxf(c, 0.f), 1.f) * 255.f) / 255.f; }
+
+// The reference's shading of a primary result (vlb_shading
+// VLB_SHADE_REF_PHONG, shaders/env_map.rchit:51-102): a miss is done; a hit
+// facing the point light starts its shadow walk toward it (returns false;
+// diffuse + specular wait in lit), any other hit is black.
+template <class A>
+__device__ __forceinline__ bool lr_finish_ref_primary(const A& a, LaneRay& L, Shaded& o) {
+  if (L.slot < 0) {
+    if (a.sky) {
+      const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
+      o.r = ref_unorm8(ref_srgb(__ldg(tx)));
+      o.g = ref_unorm8(ref_srgb(__ldg(tx + 1)));
+      o.b = ref_unorm8(ref_srgb(__ldg(tx + 2)));
+    }
+    return true;
+  }
+  const float4 e1 = __ldg(a.tris + 3 * L.slot + 1), e2 = __ldg(a.tris + 3 * L.slot + 2);
+  o.tri = L.id;
+  float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+  const float rn = rsqrtf(nx * nx + ny * ny + nz * nz);
+  nx *= rn; ny *= rn; nz *= rn;
+  const float px = fmaf(L.tb, L.d.x, L.ox), py = fmaf(L.tb, L.d.y, L.oy), pz = fmaf(L.tb, L.d.z, L.oz);
+  const float sx = a.light.x - px, sy = a.light.y - py, sz = a.light.z - pz;
+  const float len = sqrtf(sx * sx + sy * sy + sz * sz);
+  const float lx = sx / len, ly = sy / len, lz = sz / len;
+  const float sdn = fmaxf(lx * nx + ly * ny + lz * nz, 0.f);
+  if (!(sdn > 0.f)) return true;  // no shadow ray: the sample stays black
+  const float rdot = 2.f * (nx * lx + ny * ly + nz * lz);
+  const float rx = lx - rdot * nx, ry = ly - rdot * ny, rz = lz - rdot * nz;
+  float sp = fmaxf(rx * L.d.x + ry * L.d.y + rz * L.d.z, 0.f);
+  sp *= sp; sp *= sp; sp *= sp; sp *= sp;  // ^16
+  L.lit = 0.5f * sdn + 0.5f * sp;
+  make_ray(L.ray, px + a.bias * nx, py + a.bias * ny, pz + a.bias * nz, lx, ly, lz);
+  L.shadow = true;
+  L.cur = walk_root(a.ntris);
+  L.sp = 0;
+  L.slot = -1;
+  L.tb = len;
+  if (L.oprev >= 0 && uint32_t(L.oprev) < a.ntris) {
+    int id;
+    const float t = lr_try(a, L, L.oprev, &id);
+    if (t > 0.0f && t < L.tb) { L.slot = L.oprev; L.cur = kWalkEnd; }
+  }
+  return false;
+}
+
+// After a walk (REF: the reference's shading, vlb_shading
+// VLB_SHADE_REF_PHONG; the kernels are built for one shading or the other).
+// A finished primary walk is shaded: a miss takes the sky, a
 // lit-facing hit starts its shadow walk (returns false: the lane walks on,
 // the triangle id and sun term wait in id / lit), anything else is done.  A
 // finished shadow walk gives the Lambert term or 0.  Returns true with the
 // sample in `o` when the ray is complete.
-template <bool COUNT, class A>
+template <bool COUNT, class A, bool REF = false>
 __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Work& w) {
   o = Shaded{0.f, 0.f, 0.f, -1, 2};
+  if constexpr (REF) {
+    if (!L.shadow) {
+      L.hprev = L.slot;
+      return lr_finish_ref_primary(a, L, o);
+    }
+  }
   if (!L.shadow) {
     L.hprev = L.slot;
     if (L.slot < 0) {
@@ -512,7 +573,13 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
   o.vis = occ ? 0 : 1;
   if (!occ) {
     const float4 alb = __ldg(a.albedo + L.id);
-    o.r = alb.x * L.lit; o.g = alb.y * L.lit; o.b = alb.z * L.lit;
+    if constexpr (REF) {
+      o.r = ref_unorm8(ref_srgb(alb.x * L.lit));
+      o.g = ref_unorm8(ref_srgb(alb.y * L.lit));
+      o.b = ref_unorm8(ref_srgb(alb.z * L.lit));
+    } else {
+      o.r = alb.x * L.lit; o.g = alb.y * L.lit; o.b = alb.z * L.lit;
+    }
   }
   return true;
 }

@@ -492,6 +492,14 @@ vlb_status vlb_ctx_profile_reset(vlb_ctx* ctx) {
 
 uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+vlb_status vlb_ctx_test_hook(vlb_ctx* ctx, uint32_t hook, uint32_t wait_polls) {
+  if (!ctx) return VLB_ERR_INVALID;
+  if (hook > VLB_HOOK_HOLD_PRODUCER) return fail(ctx, VLB_ERR_INVALID, "test hook %u", hook);
+  ctx->hold_producer = hook == VLB_HOOK_HOLD_PRODUCER ? 1u : 0u;
+  ctx->wait_polls = hook ? wait_polls : 0u;
+  return VLB_OK;
+}
+
 // ---- probe grid (light_baker.cpp:80-101) ---------------------------------------
 vlb_status vlb_probe_grid_ref_order(const float bounds[6], const uint32_t counts[3], float* out_xyz,
                                     float grid_step[3]) {
@@ -813,6 +821,7 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
   vlbk::SkyboxArgs a{};
   a.texels = dtex; a.fmt = fmt; a.layout = layout; a.w = w; a.h = h; a.count = count; a.lmax = lmax;
   a.flags = flags; a.texels_per_map = T; a.err = ctx->d_err;
+  a.hold_producer = ctx->hold_producer; a.wait_polls = ctx->wait_polls;
   if (layout == VLB_SKY_CUBEMAP) {
     st = cube_sa_table(ctx, w, &a.solid_angle);
     // faces up to 512: per-texel weighted basis cached on the device (6n^2 x 48-64 B)
@@ -894,6 +903,8 @@ void vlb_bake_params_default(vlb_bake_params* p) {
   p->sun_intensity = 5.f;
   p->tmin = 0.001f; p->tmax = 10000.f;
   p->shadow_bias = 0.005f;
+  p->shading = VLB_SHADE_LAMBERT_SUN;
+  p->light_pos[0] = 1.f; p->light_pos[1] = 10.f; p->light_pos[2] = 1.f;  // shaders/env_map.rchit:25
 }
 
 // The BF16 basis of a direction set for hi/lo split tiles ([32][2S]): built
@@ -938,9 +949,10 @@ static vlb_status project_bf16(vlb_ctx* ctx, const uint16_t* rad, uint32_t nprob
   if (vlbk::project_tc_supported(rad, split ? 2 * S : S) && (!split || dirs->d_bt2)) {
     KScope k(ctx, split ? "project_tc_split" : "project_tc");
     const int r = split ? vlbk::launch_project_tc(rad, nprobes, 2 * S, dirs->d_bt2, dirs->bt2_pitch, K, out,
-                                                  ctx->d_err, ctx->num_sms, ctx->stream)
+                                                  ctx->d_err, ctx->num_sms, ctx->stream, ctx->hold_producer,
+                                                  ctx->wait_polls)
                         : vlbk::launch_project_tc(rad, nprobes, S, dirs->d_bt, dirs->bt_pitch, K, out, ctx->d_err,
-                                                  ctx->num_sms, ctx->stream);
+                                                  ctx->num_sms, ctx->stream, ctx->hold_producer, ctx->wait_polls);
     if (r < 0) return fail(ctx, VLB_ERR_CUDA, "tensor map encoding failed for the BF16 projection");
     return VLB_OK;
   }
@@ -978,7 +990,8 @@ static vlb_status project_f32(vlb_ctx* ctx, const float* rad, uint32_t nprobes, 
 // 32k probes (1.04x on 32k probes in 200 triangles to 8.6x on 64 probes in
 // 200k triangles; 262,144 grid probes x 1024 directions in 49k triangles:
 // 179 ms against 242 ms).
-static uint32_t lane_mode(const vlb_scene*, uint32_t, uint32_t flags) {
+static uint32_t lane_mode(const vlb_scene*, uint32_t, uint32_t flags, uint32_t shading) {
+  if (shading == VLB_SHADE_REF_PHONG) return 1;  // the reference's shading is built into the lane walks
   return (flags & VLB_BAKE_TRAVERSAL_PACKET) && !(flags & VLB_BAKE_TRAVERSAL_LANE) ? 0 : 1;
 }
 
@@ -996,7 +1009,8 @@ static bool grid_mode(const vlb_scene* scene, uint32_t nprobes, uint32_t S, cons
   const uint64_t G = grid_cells_per_side(T);
   const uint64_t bytes = uint64_t(S + 1) * (64 + (G * G + 1) * 4 + uint64_t(vlbk::kGridCap) * 2 + uint64_t(T) * 24);
   if (bytes > (2ull << 30)) return false;
-  return (p->flags & VLB_BAKE_TRAVERSAL_GRID) && !(p->flags & VLB_BAKE_FORCE_FUSED_KERNEL);
+  return (p->flags & VLB_BAKE_TRAVERSAL_GRID) && !(p->flags & VLB_BAKE_FORCE_FUSED_KERNEL) &&
+         p->shading == VLB_SHADE_LAMBERT_SUN;  // the grids hold the sun's parallel shadow rays
 }
 
 // Checks the parameters of one bake; *sun_len gets |sun_dir| (FP64).
@@ -1011,6 +1025,12 @@ static vlb_status check_params(vlb_ctx* ctx, const vlb_scene* scene, const vlb_b
                               double(p->sun_dir[2]) * p->sun_dir[2]);
   if (!(sl > 0.0) || !std::isfinite(sl)) return fail(ctx, VLB_ERR_INVALID, "sun direction must be non-zero");
   if (!(p->tmax > p->tmin) || p->tmin < 0.f) return fail(ctx, VLB_ERR_INVALID, "bad ray interval");
+  if (p->shading > VLB_SHADE_REF_PHONG) return fail(ctx, VLB_ERR_INVALID, "shading %u", p->shading);
+  if (p->shading == VLB_SHADE_REF_PHONG &&
+      !(std::isfinite(p->light_pos[0]) && std::isfinite(p->light_pos[1]) && std::isfinite(p->light_pos[2])))
+    return fail(ctx, VLB_ERR_INVALID, "light position must be finite");
+  if (p->shading == VLB_SHADE_REF_PHONG && (p->flags & VLB_BAKE_FORCE_FUSED_KERNEL))
+    return fail(ctx, VLB_ERR_UNSUPPORTED, "the packet fused kernel has the sun's shading only");
   *sun_len = sl;
   return VLB_OK;
 }
@@ -1050,7 +1070,9 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a.tmin = p->tmin; a.tmax = p->tmax; a.bias = p->shadow_bias;
   a.sky = p->sky ? p->sky->d_texels : nullptr; a.sky_n = p->sky ? p->sky->n : 0;
   a.basis16 = p->dirs->d_basis16; a.K = k_of(p->lmax); a.err = ctx->d_err;
-  a.lane = lane_mode(scene, nprobes, p->flags);
+  a.lane = lane_mode(scene, nprobes, p->flags, p->shading);
+  a.shading = p->shading;
+  a.light = make_float3(p->light_pos[0], p->light_pos[1], p->light_pos[2]);
   if (grid_mode(scene, nprobes, a.S, p)) {
     const uint32_t G = grid_cells_per_side(scene->ntris), T = scene->ntris;
     const size_t n = size_t(a.S) + 1;
@@ -1094,6 +1116,7 @@ static void job_from_trace(const vlbk::TraceArgs& a, vlbk::BakeJobDev* j) {
   j->tmin = a.tmin; j->tmax = a.tmax; j->bias = a.bias;
   j->sun = a.sun; j->sun_inv = a.sun_inv; j->sun_scale = a.sun_scale;
   j->sky = a.sky; j->sky_n = a.sky_n; j->err = a.err;
+  j->shading = a.shading; j->light = a.light;
   j->probes = a.probes; j->order = const_cast<uint32_t*>(a.order); j->nprobes = a.nprobes;
   j->dirs = a.dirs; j->dinv = a.dinv; j->dir_order = a.dir_order; j->S = a.S;
   j->basis16 = a.basis16;
@@ -1148,6 +1171,10 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     KScope k(ctx, "trace_fused_lane");
     vlbk::launch_trace_fused_lane(nullptr, j, 1, uint32_t(items), K, a.work_counter, fused_sched(ctx->batch_sched),
                                   ctx->num_sms, ctx->stream);
+    if (p->flags & VLB_BAKE_REF_ACCUMULATE) {
+      KScope k(ctx, "probe_prefix");
+      vlbk::launch_probe_prefix(static_cast<float*>(ob.dev), nprobes, V, ctx->stream);
+    }
     if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) ||
         (st = copy_out(ctx, orad)))
       return st;
@@ -1192,6 +1219,10 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     } else if ((st = project_f32(ctx, a.radiance, nprobes, p->dirs, K, static_cast<float*>(ob.dev)))) {
       return st;
     }
+  }
+  if (p->flags & VLB_BAKE_REF_ACCUMULATE) {
+    KScope k(ctx, "probe_prefix");
+    vlbk::launch_probe_prefix(static_cast<float*>(ob.dev), nprobes, V, ctx->stream);
   }
   if ((st = copy_out(ctx, ob)) || (st = copy_out(ctx, oh)) || (st = copy_out(ctx, os)) || (st = copy_out(ctx, orad)))
     return st;
@@ -1311,8 +1342,8 @@ static vlb_status batch_plan(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t nj
     BatchJob b{};
     vlb_status st = check_params(ctx, j.scene, p, &b.sun_len);
     if (st) return fail(ctx, st, "job %u: %s", i, ctx->err.c_str());
-    if (p->lmax != params->lmax || p->precision != params->precision)
-      return fail(ctx, VLB_ERR_INVALID, "job %u: lmax and precision must equal the batch's", i);
+    if (p->lmax != params->lmax || p->precision != params->precision || p->shading != params->shading)
+      return fail(ctx, VLB_ERR_INVALID, "job %u: lmax, precision and shading must equal the batch's", i);
     if (j.nprobes == 0) continue;
     if (!j.probe_xyz || !j.out) return fail(ctx, VLB_ERR_INVALID, "job %u: null probes or output", i);
     b.idx = i; b.p = p; b.nprobes = j.nprobes; b.S = p->dirs->n;
@@ -1366,7 +1397,8 @@ static vlb_status batch_enqueue(vlb_ctx* ctx, const BatchPlan& pl, const BatchBu
                                   ctx->num_sms, ctx->stream);
   } else {
     KScope k(ctx, "trace_batch");
-    vlbk::launch_trace_batch(table, ntable, total_rays, chunk, bb.counter, ctx->num_sms, ctx->stream);
+    vlbk::launch_trace_batch(table, ntable, total_rays, chunk, bb.counter,
+                             ctx->batch_table[0].shading == VLB_SHADE_REF_PHONG, ctx->num_sms, ctx->stream);
   }
   for (const auto& g : pl.groups) {
     if (pl.fused) break;  // the fused walk wrote the projected rows
@@ -1472,6 +1504,8 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
         make_float3(vlbk::host_safe_inv(d.sun.x), vlbk::host_safe_inv(d.sun.y), vlbk::host_safe_inv(d.sun.z));
     d.sun_scale = float(double(p->sun_intensity) / kPi);
     d.sky = p->sky ? p->sky->d_texels : nullptr; d.sky_n = p->sky ? p->sky->n : 0;
+    d.shading = p->shading;
+    d.light = make_float3(p->light_pos[0], p->light_pos[1], p->light_pos[2]);
     d.err = ctx->d_err;
     if (is_device_ptr(j.probe_xyz)) {
       d.probes = j.probe_xyz;

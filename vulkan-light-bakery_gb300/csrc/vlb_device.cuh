@@ -82,7 +82,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait: gives up after max_tries polls (each try_wait may suspend the
 // thread for a hardware-defined interval) and bumps the timeout counter.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, uint32_t max_tries = 1u << 22) {
+constexpr uint32_t kWaitPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err,
+                                                  uint32_t max_tries = kWaitPolls) {
   for (uint32_t i = 0; i < max_tries; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   if (err) atomicAdd(err + 1, 1);

@@ -47,6 +47,8 @@ struct SkyboxArgs {
   const float4* row_tab;     // panorama: h entries (sin theta, cos theta, weight, 0)
   float* partial;            // count*slabs_per_map*K*3
   int* err;
+  uint32_t hold_producer;    // test hook: the producer warp issues nothing
+  uint32_t wait_polls;       // bounded-wait polls (0: kWaitPolls)
 };
 // The skybox kernel writes one partial per (map, slab, consumer warp):
 // partial[map][slab][warp][v], kSkyPartialsPerSlab warps.
@@ -80,8 +82,12 @@ void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32
 // Needs S % 8 == 0 and a 16-byte aligned tile; returns -1 if the tensor maps
 // cannot be built.
 bool project_tc_supported(const void* radiance, uint32_t S);
+// hold / wait_polls: vlb_ctx_test_hook (0, 0 in normal use).
 int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const uint16_t* basis_bt,
-                      uint32_t bt_pitch, uint32_t K, float* out, int* err, int num_sms, cudaStream_t s);
+                      uint32_t bt_pitch, uint32_t K, float* out, int* err, int num_sms, cudaStream_t s,
+                      uint32_t hold = 0, uint32_t wait_polls = 0);
+// out[p][v] <- sum over q <= p of out[q][v] (FP64 running sum, one rounding).
+void launch_probe_prefix(float* out, uint32_t nprobes, uint32_t V, cudaStream_t s);
 void launch_sh_eval_envmap(const float* coeffs, uint32_t K, uint32_t w, uint32_t h, float scale, const float2* col_tab,
                            const float4* row_tab, float* out, cudaStream_t s);
 
@@ -143,6 +149,8 @@ struct TraceArgs {
   float tmin, tmax, bias;
   const float* sky;       // device cubemap or null
   uint32_t sky_n;
+  uint32_t shading;       // vlb_shading
+  float3 light;           // VLB_SHADE_REF_PHONG point light
   // outputs
   float* radiance;        // [nprobes][3][S] fp32 or null
   uint16_t* radiance_bf16;  // [nprobes][3][S] bf16, or [nprobes][3][2S] hi/lo split, or null
@@ -207,6 +215,8 @@ struct BakeJobDev {
   float sun_scale;
   const float* sky;
   uint32_t sky_n;
+  uint32_t shading;       // vlb_shading
+  float3 light;           // VLB_SHADE_REF_PHONG point light
   int* err;
   // probes and directions
   const float* probes;    // device nprobes*3
@@ -267,7 +277,8 @@ struct FusedSched {
 // from *counter (zero before the launch), trace them per lane and project
 // each chunk's radiance in the warp (FP32 sums in a fixed order, chunk sums
 // added in FP64 in chunk order by the chunk that finishes last).  njobs == 1
-// passes the job by value (jobs may be null).
+// passes the job by value (jobs may be null).  The jobs share one shading,
+// read from `one` (for a table, the host copy of its first job).
 void launch_trace_fused_lane(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njobs, uint32_t total_items,
                              uint32_t K, uint32_t* counter, const FusedSched& sc, int num_sms, cudaStream_t s);
 // One CTA per job: spatial order of each job's probes into job.order
@@ -276,8 +287,9 @@ void launch_trace_fused_lane(const BakeJobDev* jobs, const BakeJobDev& one, uint
 void launch_probe_order_batch(const BakeJobDev* jobs, uint32_t njobs, cudaStream_t s);
 // Persistent trace over all jobs' rays (tile output), warps taking chunks of
 // `chunk` rays (a multiple of 32); counter zeroed before.
+// ref_shading: every job's shading is VLB_SHADE_REF_PHONG (else every job's is Lambert + sun).
 void launch_trace_batch(const BakeJobDev* jobs, uint32_t njobs, uint32_t total_rays, uint32_t chunk,
-                        uint32_t* counter, int num_sms, cudaStream_t s);
+                        uint32_t* counter, bool ref_shading, int num_sms, cudaStream_t s);
 // Copies job j's rows of a projected group output to its own output:
 // dst[j] <- src + src_row0[j]*K*3 floats, nprobes[j]*K*3 floats.
 void launch_scatter_rows(const float* src, float* const* dst, const uint32_t* src_probe0, const uint32_t* nprobes,
@@ -357,6 +369,9 @@ struct vlb_ctx {
   std::vector<uint8_t> batch_meta;             // job table + scatter arrays, uploaded each call
   bool batch_tuned = false;
   vlb_batch_schedule batch_sched{0, 1, 1, 0, 0, 0};
+  // vlb_ctx_test_hook: producers of the TMA pipelines issue nothing; waits
+  // give up after wait_polls polls (0: the default bound)
+  uint32_t hold_producer = 0, wait_polls = 0;
 };
 
 struct vlb_scene {

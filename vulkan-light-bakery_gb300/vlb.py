@@ -26,6 +26,9 @@ SKY_REF_BGRA_SWAP = 1
 PREC_FP32, PREC_FUSED, PREC_MIXED, PREC_BF16 = 0, 1, 2, 3
 BAKE_FORCE_FUSED_KERNEL = 1
 BAKE_TRAVERSAL_PACKET, BAKE_TRAVERSAL_LANE, BAKE_TRAVERSAL_GRID = 2, 4, 8
+BAKE_REF_ACCUMULATE = 16
+HOOK_HOLD_PRODUCER = 1
+SHADE_LAMBERT_SUN, SHADE_REF_PHONG = 0, 1
 SCENE_TRAVERSAL_LBVH, SCENE_TRAVERSAL_WIDE = 1, 2
 DTYPE_F32, DTYPE_BF16, DTYPE_BF16_SPLIT = 0, 1, 2
 
@@ -46,7 +49,7 @@ class BakeParams(C.Structure):
         ("lmax", C.c_uint32), ("precision", C.c_uint32), ("flags", C.c_uint32),
         ("sun_dir", C.c_float * 3), ("sun_intensity", C.c_float),
         ("tmin", C.c_float), ("tmax", C.c_float), ("shadow_bias", C.c_float),
-        ("dirs", C.c_void_p), ("sky", C.c_void_p),
+        ("dirs", C.c_void_p), ("sky", C.c_void_p), ("shading", C.c_uint32), ("light_pos", C.c_float * 3),
     ]
 
 
@@ -102,6 +105,7 @@ def _load() -> C.CDLL:
         "vlb_ctx_profile_read": (I32, [P, P, U32, C.POINTER(U32)]),
         "vlb_ctx_profile_reset": (I32, [P]),
         "vlb_ctx_launch_count": (U64, [P]),
+        "vlb_ctx_test_hook": (I32, [P, U32, U32]),
         "vlb_probe_grid_ref_order": (I32, [P, P, P, P]),
         "vlb_scene_create": (I32, [P, P, U32, U32, P, U32, P, C.POINTER(P)]),
         "vlb_scene_create_ex": (I32, [P, P, U32, U32, P, U32, P, U32, C.POINTER(P)]),
@@ -263,6 +267,11 @@ class Context:
     @property
     def launch_count(self) -> int:
         return int(lib.vlb_ctx_launch_count(self.h))
+
+    def test_hook(self, hook: int, wait_polls: int = 0) -> None:
+        """vlb_ctx_test_hook: HOOK_HOLD_PRODUCER makes the TMA pipelines' waits
+        give up (VLB_ERR_TIMEOUT) without a copy in flight; 0 clears it."""
+        self.check(lib.vlb_ctx_test_hook(self.h, hook, wait_polls))
 
     # objects
     def scene(self, positions, indices, albedo=None, stride_bytes: int = 12, flags: int = 0) -> "Scene":
@@ -676,11 +685,17 @@ class Sky:
 
 
 def bake_params(dirs: DirSet, lmax: int = 2, precision: int = PREC_FP32, sun=(0.0, 1.0, 0.0),
-                sun_intensity: float = 5.0, sky: Sky | None = None) -> BakeParams:
+                sun_intensity: float = 5.0, sky: Sky | None = None, shading: int = SHADE_LAMBERT_SUN,
+                light_pos=None, flags: int = 0) -> BakeParams:
     p = BakeParams()
     lib.vlb_bake_params_default(C.byref(p))
     p.lmax = lmax
     p.precision = precision
+    p.shading = shading
+    p.flags = flags
+    if light_pos is not None:
+        for i in range(3):
+            p.light_pos[i] = float(light_pos[i])
     for i in range(3):
         p.sun_dir[i] = float(sun[i])
     p.sun_intensity = sun_intensity
