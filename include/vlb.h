@@ -50,6 +50,13 @@ typedef struct vlb_sky vlb_sky;
  * Replaces Application::Application (src/application.cpp:540-556): device,
  * queues and command pools become one CUDA device + one stream. */
 uint32_t vlb_version(void);
+/* Build options of this library (no reference counterpart):
+ * VLB_BUILD_BOUNDS_CHECK when compiled with -DVLB_BOUNDS_CHECK, the variant
+ * whose kernels check every data-dependent index (tree nodes, triangle
+ * slots, probe and direction permutations, sky texels, ring slots) and count
+ * a violation (the call then returns VLB_ERR_INTERNAL) instead of using it. */
+#define VLB_BUILD_BOUNDS_CHECK 1u
+uint32_t vlb_build_flags(void);
 const char* vlb_status_string(vlb_status s);
 vlb_status vlb_ctx_create(int device, vlb_ctx** out);
 /* Destroy every scene, direction set, sky and service made on a context

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs a) {
     const uint32_t chunk = item / npg, pg = item - chunk * npg;
     const uint32_t slot = pg * 32 + lane;
     const bool valid = slot < a.nprobes;
-    const uint32_t p = valid ? a.order[slot] : 0;
+    const uint32_t p = valid ? VLB_CLAMP(a.order[slot], a.nprobes, a.err) : 0;
     const float ox = valid ? a.probes[3 * size_t(p)] : 0.f, oy = valid ? a.probes[3 * size_t(p) + 1] : 0.f,
                 oz = valid ? a.probes[3 * size_t(p) + 2] : 0.f;
     const uint32_t s0 = min(a.S, chunk * a.dirs_per_warp), s1 = min(a.S, s0 + a.dirs_per_warp);
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const TraceArgs a) {
       for (int v = 0; v < V; ++v) acc[warp][v][lane] = 0.f;
     }
     for (uint32_t t = s0; t < s1; ++t) {
-      const uint32_t s = __ldg(a.dir_order + t);  // direction index (caller order)
+      const uint32_t s = VLB_CLAMP(__ldg(a.dir_order + t), a.S, a.err);  // direction index (caller order)
       const float4 dv = __ldg(a.dirs + s);
       const Shaded o = a.lane ? trace_sample<COUNT, true>(a, valid, ox, oy, oz, dv, w)
                               : trace_sample<COUNT, false>(a, valid, ox, oy, oz, dv, w);
@@ -208,6 +208,7 @@ static void launch(const TraceArgs& a, int num_sms, cudaStream_t s) {
 
 // A finished ray's tile entries (and debug arrays).
 __device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, const Shaded& o) {
+  if (!VLB_INB(L.p, a.nprobes, a.err) || !VLB_INB(L.s, a.S, a.err)) return;
   const size_t ri = size_t(L.p) * a.S + L.s, row = size_t(L.p) * 3;
   if (a.hit_tri) a.hit_tri[ri] = o.tri;
   if (a.shadow) a.shadow[ri] = o.vis;
@@ -540,10 +541,10 @@ __device__ __forceinline__ bool grid_setup(const TraceArgs& a, uint32_t gi, cons
 // nearest hit beyond tmin with the tie rule); g.e = g.e1 when the walk is over.
 template <bool COUNT>
 __device__ __forceinline__ void grid_step(const TraceArgs& a, LaneRay& L, GridWalk& g, Work& w) {
-  const uint32_t t = g.nt, T = a.ntris;
+  const uint32_t t = VLB_CLAMP(g.nt, a.ntris, a.err), T = a.ntris;
   const float2 dd = __ldg(a.grid_dep + size_t(g.gi) * T + t);
   const float4 b = __ldg(a.grid_box + size_t(g.gi) * T + t);
-  if (g.e + 1 < g.e1) g.nt = __ldg(a.grid_ent + size_t(g.gi) * kGridCap + g.e + 1);
+  if (g.e + 1 < g.e1) g.nt = __ldg(a.grid_ent + size_t(g.gi) * kGridCap + VLB_CLAMP(g.e + 1, kGridCap, a.err));
   ++g.e;
   if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
   const float tlo = L.shadow ? 0.0f : a.tmin, m = a.grid_margin;
@@ -687,6 +688,7 @@ void launch_trace_tile(const TraceArgs& a, int num_sms, cudaStream_t s) {
 // finds its job by binary search over the item ranges and traces that job's
 // scene.  Radiance goes to the job's rows of its direction set's tile.
 __device__ __forceinline__ void batch_emit(const BakeJobDev& j, uint32_t p, uint32_t s, const Shaded& o) {
+  if (!VLB_INB(p, j.nprobes, j.err) || !VLB_INB(s, j.S, j.err)) return;
   const size_t row = size_t(p) * 3;
   if (j.radiance) {
     j.radiance[row * j.S + s] = o.r;
@@ -747,7 +749,7 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
               const int2 h = __ldg(j.hits_in + size_t(p) * j.S + L.s);
               L.slot = h.x;
               L.tb = __int_as_float(h.y);
-              L.id = h.x >= 0 ? __float_as_int(__ldg(j.tris + 3 * h.x).w) : -1;
+              L.id = h.x >= 0 ? __float_as_int(__ldg(j.tris + 3 * VLB_CLAMP(h.x, j.ntris, j.err)).w) : -1;
               Shaded o;
               if (lr_finish<false, BakeJobDev, REF>(j, L, o, w)) {
                 L.has = false;

@@ -89,10 +89,10 @@ __device__ __forceinline__ void retire_head(FusedWarp& fw, const BakeJobDev* __r
     float s = 0.f;
 #pragma unroll 4
     for (uint32_t i = 0; i < q.cnt; ++i)
-      s = fmaf(__ldg(J.basis16 + size_t(__ldg(dord + i)) * 16 + k), fw.rad[e][ch][i], s);
+      s = fmaf(__ldg(J.basis16 + size_t(VLB_CLAMP(__ldg(dord + i), J.S, J.err)) * 16 + k), fw.rad[e][ch][i], s);
     fw.acc[v] = ((q.flags & kSubFirst) ? 0.0 : fw.acc[v]) + double(s);
   }
-  if (q.flags & kSubLast) {
+  if ((q.flags & kSubLast) && VLB_INB(q.p, J.nprobes, J.err) && VLB_INB(q.c, J.chunks, J.err)) {
     float* dst = J.chunks == 1 ? J.out + size_t(q.p) * V : J.partial + (size_t(q.p) * J.chunks + q.c) * V;
     for (int v = int(lane); v < V; v += 32) dst[v] = float(fw.acc[v]);
     if (J.chunks > 1) {
@@ -147,7 +147,7 @@ __device__ __forceinline__ void fill_ring(FusedWarp& fw, const BakeJobDev* __res
       const uint32_t loc = it - J.item_begin;
       const uint32_t slot = loc / J.chunks;
       const uint32_t c = loc - slot * J.chunks;
-      const uint32_t p = J.order[slot];
+      const uint32_t p = VLB_CLAMP(J.order[VLB_CLAMP(slot, J.nprobes, J.err)], J.nprobes, J.err);
       __syncwarp();
       if (lane == 0) {
         fw.ij = j; fw.ip = p; fw.ic = c;
@@ -176,6 +176,7 @@ __device__ __forceinline__ void fill_ring(FusedWarp& fw, const BakeJobDev* __res
 __device__ __forceinline__ void store_ray(FusedWarp& fw, const BakeJobDev& J, const LaneRay& L, const Shaded& o,
                                           uint32_t lslot) {
   const uint32_t le = lslot >> 8, lpos = lslot & 255;
+  if (!VLB_INB(le, kSubBufs, J.err) || !VLB_INB(lpos, kSubRays, J.err)) return;
   fw.rad[le][0][lpos] = o.r;
   fw.rad[le][1][lpos] = o.g;
   fw.rad[le][2][lpos] = o.b;
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
             const int2 hk = __ldg(J.hits_in + size_t(L.p) * J.S + s);
             L.slot = hk.x;
             L.tb = __int_as_float(hk.y);
-            L.id = hk.x >= 0 ? __float_as_int(__ldg(J.tris + 3 * hk.x).w) : -1;
+            L.id = hk.x >= 0 ? __float_as_int(__ldg(J.tris + 3 * VLB_CLAMP(hk.x, J.ntris, J.err)).w) : -1;
             Shaded o;
             if (lr_finish<false, BakeJobDev, REF>(J, L, o, w)) {
               L.has = false;

@@ -140,6 +140,7 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
   for (;;) {
     const bool test = active && in;
     if (cur >= 0) {
+      if (!VLB_INB(cur, ntris - 1, err)) break;
       if constexpr (COUNT) { w.wnodes += lane == 0; w.lnodes += test; }
       const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
                    n3 = __ldg(nodes + 4 * cur + 3);
@@ -168,7 +169,7 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
       if (b1) { cur = c1; in = h1; continue; }
     } else {
       if constexpr (COUNT) w.wtris += lane == 0;
-      const int slot = ~cur;
+      const int slot = VLB_CLAMP(~cur, ntris, err);
       const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
       if (test) {
         const float t = tri_hit(r, v0, e1, e2);
@@ -203,6 +204,7 @@ __device__ __forceinline__ void lane_traverse(const RayCtx& r, bool& active, con
   int cur = ntris > 1 ? 0 : ~0;
   for (;;) {
     if (cur >= 0) {
+      if (!VLB_INB(cur, ntris - 1, err)) break;
       if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
       const float4 n0 = __ldg(nodes + 4 * cur), n1 = __ldg(nodes + 4 * cur + 1), n2 = __ldg(nodes + 4 * cur + 2),
                    n3 = __ldg(nodes + 4 * cur + 3);
@@ -222,7 +224,7 @@ __device__ __forceinline__ void lane_traverse(const RayCtx& r, bool& active, con
       if (h1) { cur = c1; continue; }
     } else {
       if constexpr (COUNT) ++w.wtris;
-      const int slot = ~cur;
+      const int slot = VLB_CLAMP(~cur, ntris, err);
       const float4 v0 = __ldg(tris + 3 * slot), e1 = __ldg(tris + 3 * slot + 1), e2 = __ldg(tris + 3 * slot + 2);
       const float t = tri_hit(r, v0, e1, e2);
       if (t > tmin) {
@@ -330,10 +332,12 @@ __device__ __forceinline__ Shaded shade_hit(const A& a, bool valid, const RayCtx
   if (valid) {
     if (slot < 0) {
       if (a.sky) {
-        const float* tx = a.sky + 3 * size_t(cube_texel(d.x, d.y, d.z, a.sky_n));
+        const float* tx = a.sky + 3 * size_t(VLB_CLAMP(cube_texel(d.x, d.y, d.z, a.sky_n), 6u * a.sky_n * a.sky_n,
+                                                       a.err));
         o.r = __ldg(tx); o.g = __ldg(tx + 1); o.b = __ldg(tx + 2);
       }
     } else {
+      slot = VLB_CLAMP(slot, a.ntris, a.err);
       const float4 e1 = __ldg(a.tris + 3 * slot + 1), e2 = __ldg(a.tris + 3 * slot + 2);
       o.tri = id;
       float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
@@ -360,7 +364,7 @@ __device__ __forceinline__ Shaded shade_hit(const A& a, bool valid, const RayCtx
     o.vis = occ ? 0 : 1;
     if (!occ) {
       const float k = a.sun_scale * ndl;
-      const float4 alb = __ldg(a.albedo + o.tri);
+      const float4 alb = __ldg(a.albedo + VLB_CLAMP(o.tri, a.ntris, a.err));
       o.r = alb.x * k; o.g = alb.y * k; o.b = alb.z * k;
     }
   }
@@ -433,6 +437,7 @@ struct LaneRay {
 // the current scene (a lane of a batch may change scenes between rays).
 template <class A>
 __device__ __forceinline__ float lr_try(const A& a, const LaneRay& L, int ts, int* id) {
+  ts = VLB_CLAMP(ts, a.ntris, a.err);
   const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);
   *id = __float_as_int(v0.w);
   return tri_hit(L.ray, v0, e1, e2);
@@ -441,6 +446,8 @@ __device__ __forceinline__ float lr_try(const A& a, const LaneRay& L, int ts, in
 // A: TraceArgs or BakeJobDev (scene, shading, probes and dirs fields).
 template <class A>
 __device__ __forceinline__ void lr_start(const A& a, LaneRay& L, uint32_t p, uint32_t s) {
+  p = VLB_CLAMP(p, a.nprobes, a.err);
+  s = VLB_CLAMP(s, a.S, a.err);
   L.p = p;
   L.s = s;
   L.d = __ldg(a.dirs + s);
@@ -480,13 +487,15 @@ template <class A>
 __device__ __forceinline__ bool lr_finish_ref_primary(const A& a, LaneRay& L, Shaded& o) {
   if (L.slot < 0) {
     if (a.sky) {
-      const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
+      const float* tx =
+          a.sky + 3 * size_t(VLB_CLAMP(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n), 6u * a.sky_n * a.sky_n, a.err));
       o.r = ref_unorm8(ref_srgb(__ldg(tx)));
       o.g = ref_unorm8(ref_srgb(__ldg(tx + 1)));
       o.b = ref_unorm8(ref_srgb(__ldg(tx + 2)));
     }
     return true;
   }
+  L.slot = VLB_CLAMP(L.slot, a.ntris, a.err);
   const float4 e1 = __ldg(a.tris + 3 * L.slot + 1), e2 = __ldg(a.tris + 3 * L.slot + 2);
   o.tri = L.id;
   float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
@@ -537,11 +546,13 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
     L.hprev = L.slot;
     if (L.slot < 0) {
       if (a.sky) {
-        const float* tx = a.sky + 3 * size_t(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n));
+        const float* tx =
+            a.sky + 3 * size_t(VLB_CLAMP(cube_texel(L.d.x, L.d.y, L.d.z, a.sky_n), 6u * a.sky_n * a.sky_n, a.err));
         o.r = __ldg(tx); o.g = __ldg(tx + 1); o.b = __ldg(tx + 2);
       }
       return true;
     }
+    L.slot = VLB_CLAMP(L.slot, a.ntris, a.err);
     const float4 e1 = __ldg(a.tris + 3 * L.slot + 1), e2 = __ldg(a.tris + 3 * L.slot + 2);
     o.tri = L.id;
     float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
@@ -572,7 +583,7 @@ __device__ __forceinline__ bool lr_finish(const A& a, LaneRay& L, Shaded& o, Wor
   if (occ) L.oprev = L.slot;
   o.vis = occ ? 0 : 1;
   if (!occ) {
-    const float4 alb = __ldg(a.albedo + L.id);
+    const float4 alb = __ldg(a.albedo + VLB_CLAMP(L.id, a.ntris, a.err));
     if constexpr (REF) {
       o.r = ref_unorm8(ref_srgb(alb.x * L.lit));
       o.g = ref_unorm8(ref_srgb(alb.y * L.lit));
@@ -615,6 +626,7 @@ __device__ __forceinline__ float q8(uint32_t word, int c) {
 // when its box is hit, to keep the walk's registers few.
 template <bool COUNT, class A>
 __device__ __forceinline__ void lr_node_wide(const A& a, LaneRay& L, int* stack, Work& w) {
+  if (!VLB_INB(L.cur, a.nwide, a.err)) { L.cur = kWalkEnd; L.sp = 0; return; }
   if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
   const float tlo = L.shadow ? 0.0f : a.tmin;
   const float4* nd = a.wnodes + 6 * size_t(L.cur);
@@ -675,6 +687,7 @@ __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work
     lr_node_wide<COUNT>(a, L, stack, w);
     return;
   }
+  if (!VLB_INB(L.cur, a.ntris - 1, a.err)) { L.cur = kWalkEnd; L.sp = 0; return; }
   if constexpr (COUNT) { ++w.wnodes; ++w.lnodes; }
   const float tlo = L.shadow ? 0.0f : a.tmin;
   const float4 n0 = __ldg(a.nodes + 4 * L.cur), n1 = __ldg(a.nodes + 4 * L.cur + 1),
@@ -702,7 +715,7 @@ __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work
 template <bool COUNT, class A>
 __device__ __forceinline__ void lr_leaf(const A& a, LaneRay& L, Work& w) {
   if constexpr (COUNT) ++w.wtris;
-  const int ts = L.leaf;
+  const int ts = VLB_CLAMP(L.leaf, a.ntris, a.err);
   L.leaf = -1;
   const float tlo = L.shadow ? 0.0f : a.tmin;
   const float4 v0 = __ldg(a.tris + 3 * ts), e1 = __ldg(a.tris + 3 * ts + 1), e2 = __ldg(a.tris + 3 * ts + 2);

@@ -125,6 +125,8 @@ vlb_status check_device_errors(vlb_ctx* ctx, const int* h) {
   if (h[vlbk::kErrTimeout]) return fail(ctx, VLB_ERR_TIMEOUT, "a bounded device wait gave up (%d)", h[vlbk::kErrTimeout]);
   if (h[vlbk::kErrStackOverflow])
     return fail(ctx, VLB_ERR_INTERNAL, "BVH traversal stack overflow on %d rays", h[vlbk::kErrStackOverflow]);
+  if (h[vlbk::kErrBounds])
+    return fail(ctx, VLB_ERR_INTERNAL, "device bounds check failed on %d accesses", h[vlbk::kErrBounds]);
   return fail(ctx, VLB_ERR_INTERNAL, "device-side check failed (%d)", h[vlbk::kErrBadInput]);
 }
 
@@ -388,6 +390,14 @@ void cube_face_dir(int face, double u, double v, double* d) {
 extern "C" {
 
 uint32_t vlb_version(void) { return VLB_VERSION; }
+
+uint32_t vlb_build_flags(void) {
+#ifdef VLB_BOUNDS_CHECK
+  return VLB_BUILD_BOUNDS_CHECK;
+#else
+  return 0;
+#endif
+}
 
 const char* vlb_status_string(vlb_status s) {
   switch (s) {
@@ -1060,6 +1070,7 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   a = vlbk::TraceArgs{};
   a.nodes = scene->nodes; a.tris = scene->tris; a.albedo = scene->albedo; a.ntris = scene->ntris;
   a.wnodes = scene->wnodes;
+  a.nwide = scene->nwide;
   a.probes = static_cast<const float*>(dprobes); a.nprobes = nprobes;
   a.order = static_cast<const uint32_t*>(order);
   a.dirs = p->dirs->d_dirs; a.dir_order = p->dirs->d_order; a.S = p->dirs->n;
@@ -1113,6 +1124,7 @@ static vlbk::FusedSched fused_sched(const vlb_batch_schedule& sc) {
 // fused lane walk (the fused-projection fields are set by the caller).
 static void job_from_trace(const vlbk::TraceArgs& a, vlbk::BakeJobDev* j) {
   j->nodes = a.nodes; j->wnodes = a.wnodes; j->tris = a.tris; j->albedo = a.albedo; j->ntris = a.ntris;
+  j->nwide = a.nwide;
   j->tmin = a.tmin; j->tmax = a.tmax; j->bias = a.bias;
   j->sun = a.sun; j->sun_inv = a.sun_inv; j->sun_scale = a.sun_scale;
   j->sky = a.sky; j->sky_n = a.sky_n; j->err = a.err;
@@ -1497,6 +1509,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
     vlbk::BakeJobDev& d = table[t];
     d.nodes = j.scene->nodes; d.tris = j.scene->tris; d.albedo = j.scene->albedo; d.ntris = j.scene->ntris;
     d.wnodes = j.scene->wnodes;
+    d.nwide = j.scene->nwide;
     d.tmin = p->tmin; d.tmax = p->tmax; d.bias = p->shadow_bias;
     d.sun = make_float3(float(p->sun_dir[0] / b.sun_len), float(p->sun_dir[1] / b.sun_len),
                         float(p->sun_dir[2] / b.sun_len));

@@ -20,8 +20,27 @@ enum ErrSlot : int {
   kErrStackOverflow = 0,  // BVH traversal stack overflow
   kErrTimeout = 1,        // bounded mbarrier / flag wait gave up
   kErrBadInput = 2,       // device-side argument check
+  kErrBounds = 3,         // bounds-check build: an index outside its array
   kErrSlots = 8
 };
+
+// Bounds-check build (compiled with -DVLB_BOUNDS_CHECK): VLB_INB(i, n, err) is
+// false for an index outside [0, n) and counts it in err[kErrBounds]; the
+// caller then skips the access or ends the walk.  VLB_CLAMP(i, n, err) maps
+// such an index to 0 (for reads whose value only feeds arithmetic).  In the
+// normal build they are `true` and `i`: no code.
+#if defined(VLB_BOUNDS_CHECK) && defined(__CUDACC__)
+__device__ __forceinline__ bool inb_checked(long long i, long long n, int* err) {
+  if (i >= 0 && i < n) return true;
+  if (err) atomicAdd(err + kErrBounds, 1);
+  return false;
+}
+#define VLB_INB(i, n, err) (::vlbk::inb_checked((long long)(i), (long long)(n), (err)))
+#define VLB_CLAMP(i, n, err) (VLB_INB(i, n, err) ? (i) : 0)
+#else
+#define VLB_INB(i, n, err) true
+#define VLB_CLAMP(i, n, err) (i)
+#endif
 
 // Sizes of the bake's trace kernels: the warp stack of the packet walk and
 // the per-lane stacks of the lane walks (a wide node pushes up to 7 children).
@@ -136,6 +155,7 @@ struct TraceArgs {
   const float4* tris;
   const float4* albedo;
   uint32_t ntris;
+  uint32_t nwide;         // wide nodes
   const float* probes;    // device nprobes*3
   const uint32_t* order;  // device permutation: packet slot -> probe index
   uint32_t nprobes;
@@ -209,6 +229,7 @@ struct BakeJobDev {
   const float4* tris;
   const float4* albedo;
   uint32_t ntris;
+  uint32_t nwide;         // wide nodes
   float tmin, tmax, bias;
   float3 sun;
   float3 sun_inv;

@@ -106,6 +106,7 @@ def _load() -> C.CDLL:
         "vlb_ctx_profile_reset": (I32, [P]),
         "vlb_ctx_launch_count": (U64, [P]),
         "vlb_ctx_test_hook": (I32, [P, U32, U32]),
+        "vlb_build_flags": (U32, []),
         "vlb_probe_grid_ref_order": (I32, [P, P, P, P]),
         "vlb_scene_create": (I32, [P, P, U32, U32, P, U32, P, C.POINTER(P)]),
         "vlb_scene_create_ex": (I32, [P, P, U32, U32, P, U32, P, U32, C.POINTER(P)]),

@@ -52,23 +52,32 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
-def build_library(verbose: bool = False, extra_nvcc: list[str] | None = None) -> Path:
-    BUILD.mkdir(exist_ok=True)
+BOUNDS_BUILD = PKG / "_build_bounds"
+
+
+def build_library(verbose: bool = False, extra_nvcc: list[str] | None = None, bounds_check: bool = False) -> Path:
+    """bounds_check: the bounds-check variant (-DVLB_BOUNDS_CHECK: every
+    data-dependent device index is checked and counted instead of used) in
+    _build_bounds/libvlb.so; load it with VLB_LIB."""
+    build = BOUNDS_BUILD if bounds_check else BUILD
+    lib_path = build / "libvlb.so"
+    defs = ["-DVLB_BOUNDS_CHECK"] if bounds_check else []
+    build.mkdir(exist_ok=True)
     nvcc = _nvcc()
     inc = _cuda_home() / "include"
     # every object also depends on this file (its compiler flags)
     headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "vlb.h", Path(__file__)]
     jobs = []
     for cu in sorted(CSRC.glob("*.cu")):
-        obj = BUILD / (cu.stem + ".o")
+        obj = build / (cu.stem + ".o")
         # -fmad=false: device arithmetic exactly as written (explicit fmaf stays fused), so a ray's
         # FP32 decisions do not depend on how a build schedules or allocates registers
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
-               "-ffp-contract=off", *(extra_nvcc or []), "-c", str(cu), "-o", str(obj)]
+               "-ffp-contract=off", *defs, *(extra_nvcc or []), "-c", str(cu), "-o", str(obj)]
         jobs.append((obj, [cu, *headers], cmd))
     for cpp in sorted(CSRC.glob("*.cpp")):
-        obj = BUILD / (cpp.stem + ".o")
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{inc}", "-c", str(cpp),
+        obj = build / (cpp.stem + ".o")
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", *defs, f"-I{inc}", "-c", str(cpp),
                "-o", str(obj)]
         jobs.append((obj, [cpp, *headers], cmd))
     todo = [(o, c) for o, d, c in jobs if _stale(o, d)]
@@ -76,13 +85,13 @@ def build_library(verbose: bool = False, extra_nvcc: list[str] | None = None) ->
         for _ in ex.map(lambda oc: _run(oc[1]), todo):
             pass
     objs = [str(o) for o, _, _ in jobs]
-    if todo or not LIB.exists():
-        tmp = BUILD / "libvlb.so.tmp"
+    if todo or not lib_path.exists():
+        tmp = build / "libvlb.so.tmp"
         _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_path)
     if verbose:
-        print(f"built {LIB} ({len(todo)} objects rebuilt)")
-    return LIB
+        print(f"built {lib_path} ({len(todo)} objects rebuilt)")
+    return lib_path
 
 
 def build_oracle(verbose: bool = False) -> Path:
