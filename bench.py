@@ -553,7 +553,7 @@ def c1_measure(ctx, torch, stream, steps, hbm_peak):
 
 # DRAM bytes per launch of the skybox kernel on this section's 1024-map batch,
 # from the ncu capture summarised in profiles/skybox_c0.md.
-SKYBOX_NCU = {"skybox_sh_tma": 1225426045}
+SKYBOX_NCU = {"skybox_cube_group": 1247949000}
 
 
 def skybox_measure(ctx, torch, stream, steps, hbm_peak):
@@ -585,7 +585,7 @@ def skybox_measure(ctx, torch, stream, steps, hbm_peak):
     ctx.set_profiling(False)
     prof = ctx.profile()
     ms_1 = run(one, 1, out1, steps)
-    kname = [k for k in prof if k.startswith("skybox_sh")][0]
+    kname = [k for k in prof if k.startswith("skybox")][0]
     kl, kms = prof[kname]
     bytes_per_launch = count * 6 * n * n * 12
     k_avg = kms / max(kl, 1)

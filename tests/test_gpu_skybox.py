@@ -39,14 +39,22 @@ def test_bgra_swap_flag(ctx, golden):
     assert np.allclose(got[:, 0], plain[:, 2]) and np.allclose(got[:, 2], plain[:, 0])
 
 
-def test_batched_equals_single_bit_exact(ctx):
-    maps = np.stack([vlb.synth_cubemap(s, 64) for s in range(5)])
-    batch = ctx.skybox_sh(maps, vlb.SKY_CUBEMAP, 64, 64, 2, count=5)
-    for i in range(5):
-        one = ctx.skybox_sh(maps[i], vlb.SKY_CUBEMAP, 64, 64, 2)
-        ref = O.skybox_sh(maps[i], 0, 0, 64, 64, 2)
-        assert rel(batch[i], ref) < TOL
-        assert rel(one, ref) < TOL
+@pytest.mark.parametrize("lmax", [2, 3])
+@pytest.mark.parametrize("n,count", [(64, 5), (40, 21)])
+def test_batched_equals_single_bit_exact(ctx, lmax, n, count):
+    """A map's result is the same bits alone, in a batch, and at any place in
+    it (21 maps: a group of 16 and a partial one; face 40: a partial last
+    chunk of 256 texels)."""
+    maps = np.stack([vlb.synth_cubemap(s, n) for s in range(count)])
+    batch = ctx.skybox_sh(maps, vlb.SKY_CUBEMAP, n, n, lmax, count=count)
+    shifted = ctx.skybox_sh(maps[1:], vlb.SKY_CUBEMAP, n, n, lmax, count=count - 1)
+    for i in range(count):
+        one = ctx.skybox_sh(maps[i], vlb.SKY_CUBEMAP, n, n, lmax)
+        assert np.array_equal(batch[i], one)
+        if i:
+            assert np.array_equal(shifted[i - 1], one)
+        if i < 3:
+            assert rel(one, O.skybox_sh(maps[i], 0, 0, n, n, lmax)) < TOL
 
 
 def test_repeatable(ctx):

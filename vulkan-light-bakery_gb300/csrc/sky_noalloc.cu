@@ -152,9 +152,9 @@ extern "C" vlb_status vlb_skybox_sh_noalloc(const void* texels, vlb_texel_format
   }
   if (launch_failed()) return VLB_ERR_CUDA;
   const bool tma = (reinterpret_cast<uintptr_t>(texels) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
-  vlbk::launch_skybox_sh(a, tma, num_sms, s);
+  const int per_map = vlbk::launch_skybox_sh(a, tma, num_sms, s);
   if (launch_failed()) return VLB_ERR_CUDA;
-  vlbk::launch_sh_finalize(partial, 1, spm * vlbk::kSkyPartialsPerSlab, V, out, s);
+  vlbk::launch_sh_finalize(partial, 1, uint32_t(per_map), V, out, s);
   if (launch_failed()) return VLB_ERR_CUDA;
   // the error counters come back on the caller's stream (no legacy-stream copy)
   int herr[vlbk::kErrSlots];

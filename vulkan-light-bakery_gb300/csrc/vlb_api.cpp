@@ -447,6 +447,7 @@ void vlb_ctx_destroy(vlb_ctx* ctx) {
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   for (auto& kv : ctx->cube_sa) cudaFree(kv.second);
   for (auto& kv : ctx->cube_bt) cudaFree(kv.second);
+  for (auto& kv : ctx->cube_pt) cudaFree(kv.second);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -795,6 +796,21 @@ static vlb_status cube_basis_table(vlb_ctx* ctx, uint32_t n, uint32_t lmax, cons
   return VLB_OK;
 }
 
+static vlb_status cube_pair_table(vlb_ctx* ctx, uint32_t n, uint32_t lmax, const float2** out) {
+  const uint64_t key = (uint64_t(n) << 8) | lmax;
+  auto it = ctx->cube_pt.find(key);
+  if (it != ctx->cube_pt.end()) { *out = it->second; return VLB_OK; }
+  float2* p = nullptr;
+  VLB_CUDA(ctx, cudaMalloc(&p, vlbk::cube_pair_table_bytes(n, lmax)));
+  {
+    KScope k(ctx, "cube_pair_table");
+    vlbk::launch_cube_pair_table(p, n, lmax, ctx->stream);
+  }
+  ctx->cube_pt[key] = p;
+  *out = p;
+  return VLB_OK;
+}
+
 static vlb_status cube_sa_table(vlb_ctx* ctx, uint32_t n, const float** out) {
   auto it = ctx->cube_sa.find(n);
   if (it != ctx->cube_sa.end()) { *out = it->second; return VLB_OK; }
@@ -834,8 +850,9 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
   a.hold_producer = ctx->hold_producer; a.wait_polls = ctx->wait_polls;
   if (layout == VLB_SKY_CUBEMAP) {
     st = cube_sa_table(ctx, w, &a.solid_angle);
-    // faces up to 512: per-texel weighted basis cached on the device (6n^2 x 48-64 B)
-    if (!st && w <= 512) st = cube_basis_table(ctx, w, lmax, &a.basis_table);
+    // faces up to 1024: the texel-pair basis table (6n^2 x 36-64 B), the
+    // group kernel (8 maps per basis row)
+    if (!st && w <= 1024) st = cube_pair_table(ctx, w, lmax, &a.pair_table);
     if (st) return st;
   } else {
     std::vector<float> col, row;
@@ -857,13 +874,14 @@ vlb_status vlb_skybox_sh_batched(vlb_ctx* ctx, const void* texels, vlb_texel_for
   const bool tma = (reinterpret_cast<uintptr_t>(dtex) % 16 == 0) && ((uint64_t(T) * TB) % 16 == 0);
   OutBuf ob;
   if ((st = stage_out(ctx, out, size_t(count) * V * 4, "sky_out", &ob))) return st;
+  int per_map;
   {
-    KScope k(ctx, tma ? "skybox_sh_tma" : "skybox_sh");
-    vlbk::launch_skybox_sh(a, tma, ctx->num_sms, ctx->stream);
+    KScope k(ctx, tma ? (a.pair_table ? "skybox_cube_group" : "skybox_sh_tma") : "skybox_sh");
+    per_map = vlbk::launch_skybox_sh(a, tma, ctx->num_sms, ctx->stream);
   }
   {
     KScope k(ctx, "sh_finalize");
-    vlbk::launch_sh_finalize(a.partial, count, spm * vlbk::kSkyPartialsPerSlab, V, static_cast<float*>(ob.dev), ctx->stream);
+    vlbk::launch_sh_finalize(a.partial, count, uint32_t(per_map), V, static_cast<float*>(ob.dev), ctx->stream);
   }
   if ((st = copy_out(ctx, ob))) return st;
   return finish(ctx, ob.host);

@@ -62,6 +62,7 @@ struct SkyboxArgs {
   uint32_t group;         // maps per work unit (1, 2 or 4)
   const float* solid_angle;  // cubemap: w*w table (same for every face)
   const float4* basis_table; // cubemap, optional: per texel w * Y_k, (lmax+1)^2 padded to a multiple of 4
+  const float2* pair_table;  // cubemap, optional: launch_cube_pair_table's layout (selects the group kernel)
   const float2* col_tab;     // panorama: w entries (cos phi, sin phi)
   const float4* row_tab;     // panorama: h entries (sin theta, cos theta, weight, 0)
   float* partial;            // count*slabs_per_map*K*3
@@ -77,11 +78,15 @@ void launch_cube_solid_angle(float* out, uint32_t n, cudaStream_t s);
 // solid angle, normalised direction, basis) and stored in FP32: 3 float4 per
 // texel for lmax 2, 4 for lmax 3.
 void launch_cube_basis_table(float4* out, uint32_t n, uint32_t lmax, cudaStream_t s);
+// Weighted basis of texel pairs per 256-texel chunk, [chunk][k][128] float2
+// (FP64, rounded once), for the group kernel of cubemap batches.
+size_t cube_pair_table_bytes(uint32_t n, uint32_t lmax);
+void launch_cube_pair_table(float2* out, uint32_t n, uint32_t lmax, cudaStream_t s);
 // Fills slab_texels / slabs_per_map / group from texels_per_map, count and
 // lmax.  The slab is 8192 texels whatever the batch (so a map's sums have one
 // order); max_slabs > 0 caps the slabs per map by widening the slab.
 void skybox_plan(SkyboxArgs& a, uint32_t max_slabs);
-// Returns the number of CTAs launched.
+// Returns the partials per map it wrote (the slab count for launch_sh_finalize).
 int launch_skybox_sh(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s);
 // out[m][v] = sum_j partial[m][j][v] in FP64, j in fixed order.
 void launch_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, uint32_t nvals, float* out,
@@ -381,6 +386,7 @@ struct vlb_ctx {
   std::map<std::string, Buf> scratch;
   std::map<uint32_t, float*> cube_sa;  // solid-angle tables by face size
   std::map<uint64_t, float4*> cube_bt;  // weighted-basis tables by (face size << 8 | lmax)
+  std::map<uint64_t, float2*> cube_pt;  // texel-pair basis tables by (face size << 8 | lmax)
   // batched bakes: the shape key of the last batch, its captured graph (made
   // on the second call with that key) and the tuned schedule
   std::vector<uint64_t> batch_key;
