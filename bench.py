@@ -929,15 +929,16 @@ def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
                        "Poisson arrivals, 64 GiB budget, L2 SH",
            "scene_build_s": build_s}
 
-    def run(prec, rate, n, seed):
-        svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=prec)
+    def run(prec, rate, n, seed, slice_probes=0):
+        svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=prec, slice_probes=slice_probes)
         reqs = service_requests(n, rate, seed, bounds)
         lat, wall, base = service_run(ctx, svc, scenes, dsets, sky, reqs, LMAX, prec)
         st = svc.stats()
         svc.close()
         lat = np.array(lat)
         return {"rate_offered": rate, "requests": n, "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "probes_per_s": st["probes"] / wall,
+                "p90_ms": float(np.percentile(lat, 90)), "p99_ms": float(np.percentile(lat, 99)),
+                "max_ms": float(lat.max()), "probes_per_s": st["probes"] / wall,
                 "grays_per_s": st["rays"] / wall / 1e9, "batches": st["batches"], "relights": st["relights"],
                 "relights_rebaked": st["relights_rebaked"], "evictions": st["evictions"],
                 "bytes_peak": st["bytes_peak"], "wall_s": wall}
@@ -952,8 +953,23 @@ def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
     def nfor(rate):
         return int(min(nreq, max(20, rate * 5.0)))
 
+    out["slice_probes"] = 2048
     out["fused"] = [run(vlb.PREC_FUSED, f * capacity, nfor(f * capacity), SEED + 11 + k)
                     for k, f in enumerate((0.3, 0.6, 0.9))]
+    # the same 0.3 x stream without slicing (whole requests per batch)
+    out["fused_unsliced"] = [run(vlb.PREC_FUSED, 0.3 * capacity, nfor(0.3 * capacity), SEED + 11, 0xFFFFFFFF)]
+    # the floor under p99: the largest request the stream can hold (16,384
+    # probes x 1,024 rays in the densest scene) alone in an idle service
+    big = service_requests(1, 1.0, SEED + 5, bounds)[0]
+    lo, hi = bounds[-1]
+    probes = (lo + np.random.default_rng(SEED + 5).random((16384, 3)) * (hi - lo)).astype(np.float32)
+    svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=vlb.PREC_FUSED)
+    alone = []
+    for r in range(4):
+        p = vlb.bake_params(dsets[1024], LMAX, vlb.PREC_FUSED, vlb.synth_sun(big["sun_seed"] + r), sky=sky)
+        alone.append(svc.wait(svc.submit(scenes[-1], probes, p))[1])
+    svc.close()
+    out["largest_request_alone_ms"] = float(np.median(alone[1:]))
     out["mixed_bf16_hilo"] = [run(vlb.PREC_MIXED, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
     out["fp32"] = [run(vlb.PREC_FP32, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
     return out

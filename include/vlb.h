@@ -395,6 +395,8 @@ typedef struct vlb_service_config {
   uint32_t precision;        /* vlb_precision of every request */
   uint32_t max_batch_probes; /* probes per batch (0: 1,048,576) */
   uint32_t max_inflight;     /* batches queued on the GPU at once (0: 2) */
+  uint32_t slice_probes;     /* probes of one request per batch (0: 2048): a larger request is baked
+                                in slices that share batches with the requests behind it */
 } vlb_service_config;
 typedef struct vlb_request {
   const vlb_scene* scene;         /* ignored by a relight (the original's) */
@@ -434,7 +436,9 @@ const char* vlb_service_last_error(void);
  * into batches, each at most max_batch_probes probes (a larger request goes
  * alone) and at most budget_bytes (a request over the budget is refused,
  * batch size 0).  out_batch[i] = index of request i's batch (or UINT32_MAX
- * if refused); returns the number of batches in *nbatches. */
+ * if refused); returns the number of batches in *nbatches.  The service
+ * applies it to slices: a request over slice_probes enters as consecutive
+ * slices, one per batch. */
 vlb_status vlb_service_plan(const uint64_t* probes, const uint64_t* bytes, uint32_t n, uint64_t max_batch_probes,
                             uint64_t budget_bytes, uint32_t* out_batch, uint32_t* nbatches);
 

@@ -58,6 +58,37 @@ def test_service_matches_bake(ctx, world, prec):
     svc.close()
 
 
+@pytest.mark.parametrize("prec", [vlb.PREC_FUSED, vlb.PREC_MIXED])
+def test_service_slices_large_requests(ctx, world, prec):
+    """slice_probes = 97: requests of up to 1500 probes bake in slices that
+    share batches with the requests behind them; every result, and every
+    relight of a sliced kept bake, equals vlb_bake bit for bit."""
+    w = world
+    svc = vlb.Service(ctx, lmax=2, precision=prec, max_batch_probes=400, slice_probes=97)
+    reqs = []
+    for i in range(12):
+        sc, b = w["scenes"][i % 3]
+        n = int(w["rng"].integers(1, 1500))
+        S = 64 if i % 2 else 256
+        p = _params(w, S, vlb.synth_sun(200 + i), prec)
+        pr = w["probes"](b, n)
+        t = svc.submit(sc, pr, p, keep_hits=i % 3 == 0)
+        reqs.append((t, sc, pr, p))
+        if i % 3 == 0:  # queued right behind its (sliced) bake
+            q = _params(w, S, vlb.synth_sun(300 + i), prec, intensity=2.5)
+            reqs.append((svc.submit(None, None, q, relight_of=t), sc, pr, q))
+    for t, sc, pr, p in reqs:
+        got, lat = svc.wait(t)
+        assert lat > 0
+        assert np.array_equal(got, ctx.bake(sc, pr, p))
+    st = svc.stats()
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    assert st["relights"] == 4 and st["relights_rebaked"] == 0
+    total = sum(len(pr) for _, _, pr, _ in reqs)
+    assert st["batches"] >= -(-total // 400) and st["probes"] == total
+    svc.close()
+
+
 def test_service_threads_and_relights(ctx, world):
     w = world
     svc = vlb.Service(ctx, lmax=2, precision=vlb.PREC_MIXED, max_batch_probes=4000)

@@ -5,7 +5,7 @@
 // the serving loop around the batched bake:
 //
 //   submit (any thread)  -> queue (FIFO, mutex)
-//   worker thread        -> cuts the queue head into a batch (probe cap,
+//   worker thread        -> cuts the queue into a batch (probe cap,
 //                           device-memory budget), launches it with the
 //                           vlb_bake_batch machinery on a private stream
 //                           without waiting, records an event, and retires
@@ -13,6 +13,14 @@
 //                           request's rows out of pinned staging);
 //                           up to max_inflight batches are queued on the GPU,
 //                           so the next batch is assembled while one runs.
+//
+// Slicing: a batch takes at most slice_probes probes of any one request.  A
+// larger request stays at its place in the queue and gives one slice (a range
+// of its probes) to each batch until all its probes are launched, so the
+// requests behind it ride in the same batches instead of waiting for all of
+// it: a small request waits for at most max_inflight batches of bounded
+// size.  Each probe's result does not depend on the batch or the slice (the
+// bake is per probe), so a sliced request returns the bits of vlb_bake.
 //   wait (any thread)    -> condition variable on the ticket.
 //
 // Kept hits: a bake submitted with keep_hits stores (triangle slot, distance)
@@ -48,6 +56,7 @@ using Clock = std::chrono::steady_clock;
 constexpr uint64_t kDefaultBudget = 64ull << 30;
 constexpr uint32_t kDefaultMaxProbes = 1u << 20;
 constexpr uint32_t kDefaultInflight = 2;
+constexpr uint32_t kDefaultSlice = 2048;
 
 uint32_t svc_k(uint32_t lmax) { return (lmax + 1) * (lmax + 1); }
 
@@ -86,7 +95,10 @@ struct Request {
   uint64_t ticket = 0;
   const vlb_scene* scene = nullptr;
   std::vector<float> probes;  // host copy (bakes)
-  uint32_t n = 0;
+  uint32_t n = 0;             // probes (a relight: the kept bake's)
+  uint32_t next_off = 0;      // probes launched so far (slices)
+  uint32_t pending = 0;       // slices launched and not yet retired
+  bool failed = false;
   vlb_bake_params params{};
   uint64_t relight_of = 0;
   bool keep = false;
@@ -112,9 +124,16 @@ struct HitSet {
   bool dropped = false;    // released by the user: freed by the worker
 };
 
+// One request's probes [off, off + cnt) in a batch, its rows at `out` floats
+// into the staging buffer.
+struct Slice {
+  Request* r;
+  uint32_t off, cnt;
+  size_t out;
+};
+
 struct Batch {
-  std::vector<Request*> reqs;
-  std::vector<size_t> offs;  // float offset of each request's rows in the staging buffer
+  std::vector<Slice> slices;
   cudaEvent_t done = nullptr;
   float* h_out = nullptr;    // pinned staging
   size_t h_cap = 0;
@@ -153,7 +172,9 @@ struct vlb_service {
   bool launch_next(std::unique_lock<std::mutex>& lk);
   void retire(Batch& b, std::unique_lock<std::mutex>& lk);
   void free_set(HitSet& s);
-  void fail_batch(std::vector<Request*>& rs, vlb_status st, const std::string& msg);
+  void fail_slices(std::vector<Slice>& sl, vlb_status st, const std::string& msg);
+  void fail_request(Request* r, vlb_status st, const std::string& msg);
+  void finalize(Request* r);
   void note_bytes() {
     stats.bytes_in_use = set_bytes + flight_bytes;
     stats.bytes_peak = std::max(stats.bytes_peak, stats.bytes_in_use);
@@ -170,41 +191,75 @@ void vlb_service::free_set(HitSet& s) {
   set_bytes -= s.bytes;
 }
 
-void vlb_service::fail_batch(std::vector<Request*>& rs, vlb_status st, const std::string& msg) {
-  for (Request* r : rs) {
+// A request is complete when all its probes are launched (or it failed) and
+// no slice of it is running.
+void vlb_service::finalize(Request* r) {
+  if (r->pending || (!r->failed && r->next_off < r->n)) return;
+  if (r->failed) {
+    auto q = std::find(queue.begin(), queue.end(), r->ticket);
+    if (q != queue.end()) queue.erase(q);
     r->state = Request::kFailed;
-    r->status = st;
-    r->err = msg;
+    r->result.clear();
     ++stats.failed;
+  } else {
+    r->state = Request::kDone;
+    r->latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
+    ++stats.completed;
   }
   cv_done.notify_all();
 }
 
-// Forms and launches the next batch from the queue head.  Called with the
-// lock held; returns false when nothing could be launched now.
+void vlb_service::fail_request(Request* r, vlb_status st, const std::string& msg) {
+  if (!r->failed) {
+    r->failed = true;
+    r->status = st;
+    r->err = msg;
+  }
+  finalize(r);
+}
+
+// Slices that were not launched (or whose batch failed): their requests fail.
+void vlb_service::fail_slices(std::vector<Slice>& sl, vlb_status st, const std::string& msg) {
+  for (Slice& x : sl) fail_request(x.r, st, msg);
+}
+
+// Forms and launches the next batch from the queue, in order, one slice per
+// request.  Called with the lock held; returns false when nothing could be
+// launched now.
 bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
   const uint64_t budget = cfg.hbm_budget_bytes;
-  std::vector<Request*> take;
-  uint64_t probes = 0, bytes = 0;
-  std::vector<uint64_t> in_batch;  // tickets of the bakes in this batch
-  while (!queue.empty()) {
-    Request* r = reqs[queue.front()].get();
+  std::vector<Slice> take;
+  uint64_t probes = 0, bytes = 0, keep_bytes = 0;
+  auto room = [&]() { return budget > set_bytes + flight_bytes ? budget - set_bytes - flight_bytes : 0; };
+  for (size_t qi = 0; qi < queue.size();) {
+    Request* r = reqs[queue[qi]].get();
+    if (r->failed) {  // a slice of it failed: its other probes are not launched
+      queue.erase(queue.begin() + long(qi));
+      finalize(r);
+      continue;
+    }
     HitSet* src = nullptr;
     if (r->relight_of) {
       auto it = sets.find(r->relight_of);
       src = it == sets.end() ? nullptr : it->second.get();
-      // the keeping bake's hits are written by its own trace launch: never in the same batch
-      if (std::find(in_batch.begin(), in_batch.end(), r->relight_of) != in_batch.end()) break;
+      // the kept bake's hits are written by its own launches: every probe of it
+      // launched before, none in this batch
+      auto kr = reqs.find(r->relight_of);
+      const bool launched = kr == reqs.end() || kr->second->failed || kr->second->next_off >= kr->second->n;
+      bool here = false;
+      for (const Slice& x : take) here |= x.r->ticket == r->relight_of;
+      if (!launched || here) { ++qi; continue; }
     }
     // one batch bakes one shading (vlb_bake_batch's rule)
-    if (!take.empty() && r->params.shading != take.front()->params.shading) break;
-    const uint32_t n = src ? src->n : r->n;
+    if (!take.empty() && r->params.shading != take.front().r->params.shading) break;
+    const uint32_t cnt = std::min(r->n - r->next_off, cfg.slice_probes);
     const uint32_t S = src ? src->dirs->n : r->params.dirs->n;
-    uint64_t b = transient_bytes(n, S, K, cfg.precision);
-    if (r->keep && !r->relight_of) b += hitset_bytes(n, S);
+    uint64_t b = transient_bytes(cnt, S, K, cfg.precision);
+    // a kept set is allocated whole with a bake's first slice
+    const uint64_t kb = r->keep && !r->relight_of && r->next_off == 0 ? hitset_bytes(r->n, S) : 0;
+    b += kb;
     // room: budget minus what is held; evict unused kept sets (LRU) if the head does not fit
-    auto room = [&]() { return budget > set_bytes + flight_bytes ? budget - set_bytes - flight_bytes : 0; };
-    if (!joins(take.empty(), probes, bytes, n, b, cfg.max_batch_probes, room())) {
+    if (!joins(take.empty(), probes, bytes, cnt, b, cfg.max_batch_probes, room())) {
       if (!take.empty()) break;
       while (b > room()) {
         HitSet* lru = nullptr;
@@ -219,18 +274,19 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
       note_bytes();
       if (b > room()) {
         if (!inflight.empty()) return false;  // wait for the batches in flight to free their room
-        std::vector<Request*> one{r};
-        queue.pop_front();
-        fail_batch(one, VLB_ERR_OOM, "request exceeds the free device-memory budget");
+        queue.erase(queue.begin() + long(qi));
+        fail_request(r, VLB_ERR_OOM, "request exceeds the free device-memory budget");
         continue;
       }
     }
-    queue.pop_front();
-    take.push_back(r);
-    in_batch.push_back(r->ticket);
-    probes += n;
+    take.push_back({r, r->next_off, cnt, 0});
+    r->next_off += cnt;
+    probes += cnt;
     bytes += b;
+    keep_bytes += kb;
     if (src) src->last_use = ++use_clock;
+    if (r->next_off >= r->n) queue.erase(queue.begin() + long(qi));
+    else ++qi;
   }
   if (take.empty()) return false;
 
@@ -241,60 +297,68 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
   std::vector<vlbh::JobExt> ext(nj);
   std::vector<vlb_bake_params> jp(nj);
   Batch bt;
-  bt.reqs = take;
-  bt.offs.resize(nj);
   size_t rows = 0;
   for (size_t i = 0; i < nj; ++i) {
-    Request* r = take[i];
+    Slice& x = take[i];
+    Request* r = x.r;
+    if (x.off == 0) r->result.assign(size_t(r->n) * 3 * K, 0.f);
     jp[i] = r->params;
     jp[i].lmax = cfg.lmax;
     jp[i].precision = cfg.precision;
     vlb_bake_job& j = jobs[i];
     j.params = &jp[i];
+    j.nprobes = x.cnt;
     if (r->relight_of) {
-      ++stats.relights;
       HitSet* s = sets[r->relight_of].get();
+      const size_t S = s->dirs->n;
       jp[i].dirs = s->dirs;
       jp[i].tmin = s->tmin;
       jp[i].tmax = s->tmax;
       j.scene = s->scene;
-      j.nprobes = s->n;
+      if (x.off == 0) ++stats.relights;
       if (s->resident && !s->dropped) {
-        j.probe_xyz = s->d_probes;
-        ext[i].hits_in = s->d_hits;
+        j.probe_xyz = s->d_probes + size_t(x.off) * 3;
+        ext[i].hits_in = s->d_hits + size_t(x.off) * S;
       } else {
-        ++stats.relights_rebaked;
-        j.probe_xyz = s->h_probes.data();
+        if (x.off == 0) ++stats.relights_rebaked;
+        j.probe_xyz = s->h_probes.data() + size_t(x.off) * 3;
       }
     } else {
       j.scene = r->scene;
-      j.nprobes = r->n;
-      j.probe_xyz = r->probes.data();
+      j.probe_xyz = r->probes.data() + size_t(x.off) * 3;
       if (r->keep) {
         HitSet* s = sets[r->ticket].get();
-        const size_t rays = size_t(r->n) * r->params.dirs->n;
-        if (cudaMallocAsync(reinterpret_cast<void**>(&s->d_hits), rays * 8, ctx->stream) != cudaSuccess ||
-            cudaMallocAsync(reinterpret_cast<void**>(&s->d_probes), size_t(r->n) * 12, ctx->stream) != cudaSuccess ||
-            cudaMemcpyAsync(s->d_probes, r->probes.data(), size_t(r->n) * 12, cudaMemcpyHostToDevice, ctx->stream) !=
-                cudaSuccess) {
-          cudaGetLastError();
-          if (s->d_hits) cudaFreeAsync(s->d_hits, ctx->stream);
-          if (s->d_probes) cudaFreeAsync(s->d_probes, ctx->stream);
-          s->d_hits = nullptr;
-          s->d_probes = nullptr;
-        } else {
-          s->resident = true;  // a set released before its bake launched is freed right after
-          s->bytes = hitset_bytes(r->n, r->params.dirs->n);
-          set_bytes += s->bytes;
-          s->last_use = ++use_clock;
-          ext[i].hits_out = s->d_hits;
-          j.probe_xyz = s->d_probes;
+        const size_t S = r->params.dirs->n;
+        if (x.off == 0) {
+          const size_t rays = size_t(r->n) * S;
+          if (cudaMallocAsync(reinterpret_cast<void**>(&s->d_hits), rays * 8, ctx->stream) != cudaSuccess ||
+              cudaMallocAsync(reinterpret_cast<void**>(&s->d_probes), size_t(r->n) * 12, ctx->stream) !=
+                  cudaSuccess ||
+              cudaMemcpyAsync(s->d_probes, r->probes.data(), size_t(r->n) * 12, cudaMemcpyHostToDevice,
+                              ctx->stream) != cudaSuccess) {
+            cudaGetLastError();
+            if (s->d_hits) cudaFreeAsync(s->d_hits, ctx->stream);
+            if (s->d_probes) cudaFreeAsync(s->d_probes, ctx->stream);
+            s->d_hits = nullptr;
+            s->d_probes = nullptr;
+          } else {
+            s->resident = true;  // a set released before its bake launched is freed right after
+            s->bytes = hitset_bytes(r->n, S);
+            set_bytes += s->bytes;
+            s->last_use = ++use_clock;
+          }
+        }
+        // later slices write into the set while it stays resident (an evicted
+        // set is baked in full by its relights)
+        if (s->resident) {
+          ext[i].hits_out = s->d_hits + size_t(x.off) * S;
+          j.probe_xyz = s->d_probes + size_t(x.off) * 3;
         }
       }
     }
-    bt.offs[i] = rows * 3 * K;
-    rows += j.nprobes;
-    bt.rays += uint64_t(j.nprobes) * jp[i].dirs->n;
+    x.out = rows * 3 * K;
+    rows += x.cnt;
+    bt.rays += uint64_t(x.cnt) * jp[i].dirs->n;
   }
   // pinned staging for the outputs and the error counters
   const size_t need = std::max<size_t>(rows * 3 * K, 1);
@@ -308,7 +372,7 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
   if (!bt.h_out) {
     if (cudaMallocHost(reinterpret_cast<void**>(&bt.h_out), need * 4) != cudaSuccess) {
       cudaGetLastError();
-      fail_batch(take, VLB_ERR_OOM, "pinned staging allocation failed");
+      fail_slices(take, VLB_ERR_OOM, "pinned staging allocation failed");
       return true;
     }
     bt.h_cap = need;
@@ -317,10 +381,10 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
   else if (cudaMallocHost(reinterpret_cast<void**>(&bt.h_err), vlbk::kErrSlots * sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     pinned_pool.push_back({bt.h_out, bt.h_cap});
-    fail_batch(take, VLB_ERR_OOM, "pinned staging allocation failed");
+    fail_slices(take, VLB_ERR_OOM, "pinned staging allocation failed");
     return true;
   }
-  for (size_t i = 0; i < nj; ++i) jobs[i].out = bt.h_out + bt.offs[i];
+  for (size_t i = 0; i < nj; ++i) jobs[i].out = bt.h_out + take[i].out;
   if (!event_pool.empty()) { bt.done = event_pool.back(); event_pool.pop_back(); }
   else cudaEventCreateWithFlags(&bt.done, cudaEventDisableTiming);
 
@@ -344,13 +408,15 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
     pinned_pool.push_back({bt.h_out, bt.h_cap});
     err_pool.push_back(bt.h_err);
     event_pool.push_back(bt.done);
-    fail_batch(take, st, ctx->err);
+    fail_slices(take, st, ctx->err);
     return true;
   }
-  for (Request* r : take) r->state = Request::kRunning;
-  bt.bytes = bytes;
-  for (size_t i = 0; i < nj; ++i)
-    if (take[i]->keep && !take[i]->relight_of) bt.bytes -= hitset_bytes(take[i]->n, take[i]->params.dirs->n);
+  for (Slice& x : take) {
+    x.r->state = Request::kRunning;
+    ++x.r->pending;
+  }
+  bt.slices = std::move(take);
+  bt.bytes = bytes - keep_bytes;
   flight_bytes += bt.bytes;
   ++stats.batches;
   note_bytes();
@@ -360,26 +426,28 @@ bool vlb_service::launch_next(std::unique_lock<std::mutex>& lk) {
 }
 
 void vlb_service::retire(Batch& b, std::unique_lock<std::mutex>&) {
-  const auto now = Clock::now();
   bool bad = false;
   for (int i = 0; i < vlbk::kErrSlots; ++i) bad |= b.h_err[i] != 0;
-  if (bad) {
-    char msg[160];
-    std::snprintf(msg, sizeof msg, "device check failed in the batch (stack overflow %d, timeout %d, input %d)",
-                  b.h_err[vlbk::kErrStackOverflow], b.h_err[vlbk::kErrTimeout], b.h_err[vlbk::kErrBadInput]);
-    fail_batch(b.reqs, VLB_ERR_INTERNAL, msg);
-  } else {
-    for (size_t i = 0; i < b.reqs.size(); ++i) {
-      Request* r = b.reqs[i];
-      const uint32_t n = r->relight_of ? sets[r->relight_of]->n : r->n;
-      r->result.assign(b.h_out + b.offs[i], b.h_out + b.offs[i] + size_t(n) * 3 * K);
-      r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
-      r->state = Request::kDone;
-      ++stats.completed;
-      stats.probes += n;
+  char msg[200] = "";
+  if (bad)
+    std::snprintf(msg, sizeof msg,
+                  "device check failed in the batch (stack overflow %d, timeout %d, input %d, bounds %d)",
+                  b.h_err[vlbk::kErrStackOverflow], b.h_err[vlbk::kErrTimeout], b.h_err[vlbk::kErrBadInput],
+                  b.h_err[vlbk::kErrBounds]);
+  for (Slice& x : b.slices) {
+    Request* r = x.r;
+    --r->pending;
+    if (bad) {
+      fail_request(r, VLB_ERR_INTERNAL, msg);
+      continue;
     }
-    stats.rays += b.rays;
+    if (!r->failed) {
+      std::memcpy(r->result.data() + size_t(x.off) * 3 * K, b.h_out + x.out, size_t(x.cnt) * 3 * K * 4);
+      stats.probes += x.cnt;
+    }
+    finalize(r);
   }
+  if (!bad) stats.rays += b.rays;
   flight_bytes -= b.bytes;
   note_bytes();
   pinned_pool.push_back({b.h_out, b.h_cap});
@@ -398,7 +466,8 @@ void vlb_service::run() {
       if (q == cudaErrorNotReady) break;
       if (q != cudaSuccess) {
         cudaGetLastError();
-        fail_batch(inflight.front().reqs, VLB_ERR_CUDA, cudaGetErrorString(q));
+        for (Slice& x : inflight.front().slices) --x.r->pending;
+        fail_slices(inflight.front().slices, VLB_ERR_CUDA, cudaGetErrorString(q));
         flight_bytes -= inflight.front().bytes;
         note_bytes();
       } else {
@@ -453,6 +522,7 @@ vlb_status vlb_service_create(vlb_ctx* ctx, const vlb_service_config* cfg, vlb_s
   if (!c.hbm_budget_bytes) c.hbm_budget_bytes = kDefaultBudget;
   if (!c.max_batch_probes) c.max_batch_probes = kDefaultMaxProbes;
   if (!c.max_inflight) c.max_inflight = kDefaultInflight;
+  if (!c.slice_probes) c.slice_probes = kDefaultSlice;
   vlb_ctx* priv = nullptr;
   vlb_status st = vlb_ctx_create(ctx->device, &priv);
   if (st) return sfail(st, "service: private context creation failed");
@@ -501,6 +571,7 @@ vlb_status vlb_service_submit(vlb_service* s, const vlb_request* q, uint64_t* ti
     if (it == s->sets.end()) return sfail(VLB_ERR_INVALID, "relight_of names no bake that keeps its hits");
     n = it->second->n;
     S = it->second->dirs->n;
+    r->n = n;
   } else {
     if (!q->scene || (q->nprobes && !q->probe_xyz))
       return sfail(VLB_ERR_INVALID, "request needs a scene and probes");

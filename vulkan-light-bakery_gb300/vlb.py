@@ -73,7 +73,7 @@ class BatchSchedule(C.Structure):
 
 class ServiceConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("lmax", C.c_uint32), ("precision", C.c_uint32),
-                ("max_batch_probes", C.c_uint32), ("max_inflight", C.c_uint32)]
+                ("max_batch_probes", C.c_uint32), ("max_inflight", C.c_uint32), ("slice_probes", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -414,8 +414,8 @@ class Service:
     """Resident bake service (vlb_service_*): submit from any thread, wait by ticket."""
 
     def __init__(self, ctx: Context, budget_bytes: int = 0, lmax: int = 2, precision: int = PREC_MIXED,
-                 max_batch_probes: int = 0, max_inflight: int = 0):
-        cfg = ServiceConfig(budget_bytes, lmax, precision, max_batch_probes, max_inflight)
+                 max_batch_probes: int = 0, max_inflight: int = 0, slice_probes: int = 0):
+        cfg = ServiceConfig(budget_bytes, lmax, precision, max_batch_probes, max_inflight, slice_probes)
         h = C.c_void_p()
         self.ctx = ctx
         self.lmax = lmax
