@@ -145,8 +145,14 @@ __device__ __forceinline__ void fill_ring(FusedWarp& fw, const BakeJobDev* __res
       const uint32_t j = MULTI ? find_job(jobs, njobs, it) : 0;
       const BakeJobDev& J = job_of<MULTI>(jobs, one, j);
       const uint32_t loc = it - J.item_begin;
-      const uint32_t slot = loc / J.chunks;
-      const uint32_t c = loc - slot * J.chunks;
+      uint32_t slot, c;
+      if (J.chunk_major) {
+        c = loc / J.nprobes;
+        slot = loc - c * J.nprobes;
+      } else {
+        slot = loc / J.chunks;
+        c = loc - slot * J.chunks;
+      }
       const uint32_t p = VLB_CLAMP(J.order[VLB_CLAMP(slot, J.nprobes, J.err)], J.nprobes, J.err);
       __syncwarp();
       if (lane == 0) {

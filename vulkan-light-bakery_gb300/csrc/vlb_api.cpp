@@ -1186,6 +1186,7 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     j.out = static_cast<float*>(ob.dev);
     j.chunk_rays = vlbk::fused_chunk_rays(S);
     j.chunks = (S + j.chunk_rays - 1) / j.chunk_rays;
+    j.chunk_major = vlbk::fused_chunk_major(S);
     j.hit_tri = a.hit_tri; j.shadow = a.shadow; j.dbg_radiance = a.dbg_radiance;
     if (j.chunks > 1) {
       void *part, *done;
@@ -1555,6 +1556,7 @@ vlb_status vlbh::batch_launch(vlb_ctx* ctx, const vlb_bake_job* jobs, const vlbh
       d.out = bb.out + b.row0 * V;
       d.chunk_rays = vlbk::fused_chunk_rays(b.S);
       d.chunks = (b.S + d.chunk_rays - 1) / d.chunk_rays;
+      d.chunk_major = vlbk::fused_chunk_major(b.S);
       if (d.chunks > 1) {
         d.partial = bb.partial + part_off;
         part_off += size_t(b.nprobes) * d.chunks * V;

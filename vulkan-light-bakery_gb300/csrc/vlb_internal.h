@@ -274,6 +274,11 @@ struct BakeJobDev {
   float* partial;         // [nprobes][chunks][K*3] FP32 chunk sums (chunks > 1)
   uint32_t* done;         // [nprobes] chunk tickets, zero before the launch
   uint32_t chunks, chunk_rays;
+  // item order: 0 probe-major (a probe's chunks in a row: the rays in flight
+  // share origins), 1 chunk-major (every probe's chunk c in a row: the basis
+  // rows of chunk c are read once from HBM while all probes use them; for
+  // direction sets whose basis does not stay in L2).  Results do not depend on it.
+  uint32_t chunk_major;
   uint32_t item_begin;    // first work item of this job in the launch's numbering
   // per-ray debug outputs of the fused walk (null: none), ray r = probe * S + s
   int32_t* hit_tri;
@@ -293,6 +298,9 @@ inline uint32_t fused_chunk_rays(uint32_t S) {
   const uint32_t d = (per + kFusedSubRays - 1) / kFusedSubRays * kFusedSubRays;
   return d < kFusedMaxChunkRays ? d : kFusedMaxChunkRays;
 }
+// Chunk-major item order when the direction set's basis (64 B a direction)
+// exceeds 16 MiB.
+inline uint32_t fused_chunk_major(uint32_t S) { return uint64_t(S) * 64 > (16ull << 20) ? 1u : 0u; }
 // Launch knobs of the fused walk (vlb_batch_schedule; results do not depend on them).
 struct FusedSched {
   uint32_t ctas_per_sm = 8;  // register budget: 7, 8 or 9 resident 4-warp CTAs per SM
