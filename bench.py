@@ -766,6 +766,13 @@ def batch_measure(ctx, torch, stream, steps, hbm_peak):
             sched, tune_ms = ctx.batch_autotune(jobs, plist[0], reps=1)
             r["schedule"] = {f: getattr(sched, f) for f, _ in vlb.BatchSchedule._fields_}
             r["schedule"].update({"autotune_s": time.perf_counter() - t0, "autotune_best_ms": tune_ms})
+            trials, cls = ctx.batch_tune_log()
+            default_ms = trials[0][1]
+            r["autotune"] = {
+                "size_class": cls, "default_ms": default_ms, "best_ms": tune_ms,
+                "gain_vs_default": default_ms / tune_ms - 1.0,
+                "winner": "default" if trials[0][1] <= tune_ms else "tuned",
+                "trials": [dict(sched, ms=ms) for sched, ms in trials]}
         run(jobs, plist[0], 3)  # direct, capture, replay
         ms, launches = run(jobs, plist[0], steps)
         ctx.profile_reset()

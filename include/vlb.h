@@ -359,20 +359,34 @@ typedef struct vlb_batch_schedule {
                              0 = 6 */
   uint32_t refill_idle;   /* fused walk: idle lanes that make a warp hand out new rays, 1..32; 0 = 16 */
 } vlb_batch_schedule;
-/* sched NULL: the schedule vlb_batch_autotune stored in the context, else
- * the library default {0, 1, 1, 0, 0, 0}.  A VLB_PREC_FUSED vlb_bake uses
- * the tuned fused-walk knobs too. */
+/* sched NULL: the schedule vlb_batch_autotune stored in the context for the
+ * batch's scene-size class (its largest scene: under 4,096, 65,536, 1,048,576
+ * triangles, or more), else the library default {0, 1, 1, 0, 0, 0}.  A
+ * VLB_PREC_FUSED vlb_bake uses the fused-walk knobs tuned for its scene's
+ * class too. */
 vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                           const vlb_batch_schedule* sched);
 /* Times the batch under candidate schedules (reps runs each, outputs written
- * every run), stores the fastest in the context for later vlb_bake_batch calls
- * with sched NULL and returns it with its mean milliseconds per batch.  Tile
- * walks: rays per lane per chunk 1, 2, 4, 8, 16 x job order.  Fused walks
- * (VLB_PREC_FUSED): one knob at a time from the default -- CTAs per SM 7, 8,
- * 9; node steps 4, 6, 8, 12; refill threshold 8, 16, 24; job order -- each
- * kept at its fastest value before the next is swept. */
+ * every run), stores the fastest in the context for the batch's scene-size
+ * class (later vlb_bake_batch calls with sched NULL and fused vlb_bake calls
+ * on scenes of that class) and returns it with its mean milliseconds per
+ * batch.  Tile walks: rays per lane per chunk 1, 2, 4, 8, 16 x job order.
+ * Fused walks (VLB_PREC_FUSED): one knob at a time from the default -- CTAs
+ * per SM (warps per SM) 7, 8, 9; node steps 2, 4, 6, 8, 12, 16; refill
+ * threshold 4, 8, 16, 24, 32; job order 0, 1 -- each kept at its fastest value
+ * before the next is swept. */
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                               uint32_t reps, vlb_batch_schedule* best, float* best_ms);
+/* The trials of the context's last vlb_batch_autotune in the order run: up
+ * to cap entries into out (may be NULL), their count in *n, the class the
+ * winner was stored for in *size_class (0-3, may be NULL).  The first trial is
+ * the default schedule. */
+typedef struct vlb_tune_trial {
+  vlb_batch_schedule schedule;
+  float ms;
+} vlb_tune_trial;
+vlb_status vlb_batch_tune_log(const vlb_ctx* ctx, vlb_tune_trial* out, uint32_t cap, uint32_t* n,
+                              uint32_t* size_class);
 
 /* ---- bake service ------------------------------------------------------------
  * No reference counterpart (the reference bakes once per process,

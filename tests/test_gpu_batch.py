@@ -101,10 +101,26 @@ def test_batch_autotune(ctx, batch_world):
     ref = _singles(ctx, w, plist)
     jobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], plist)]
     sched, ms = ctx.batch_autotune(jobs, plist[0], reps=1)
-    assert sched.dirs_per_item in (1, 2, 4, 8, 16) and sched.cost_order in (0, 1) and ms > 0
-    for _ in range(3):  # the tuned schedule, graph on
+    assert sched.dirs_per_item in (0, 1, 2, 4, 8, 16) and sched.cost_order in (0, 1) and ms > 0
+    trials, cls = ctx.batch_tune_log()
+    assert len(trials) == 12 and trials[0][0]["dirs_per_item"] == 0 and trials[0][0]["cost_order"] == 1
+    assert ms == min(t for _, t in trials)
+    ntris = max(j["scene"].ntris for j in w["jobs"])
+    assert cls == (0 if ntris < 4096 else 1 if ntris < 65536 else 2 if ntris < (1 << 20) else 3)
+    for _ in range(3):  # the tuned schedule of the class, graph on
         outs = ctx.bake_batch(jobs, plist[0])
         assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
+    # fused: one knob at a time from the default, which is the first trial
+    fl = [_job_params(w, j, 2, vlb.PREC_FUSED) for j in w["jobs"]]
+    fjobs = [(j["scene"], j["probes"], None, p) for j, p in zip(w["jobs"], fl)]
+    fsched, fms = ctx.batch_autotune(fjobs, fl[0], reps=1)
+    trials, _ = ctx.batch_tune_log()
+    first = trials[0][0]
+    assert (first["ctas_per_sm"], first["node_steps"], first["refill_idle"], first["cost_order"]) == (8, 6, 16, 1)
+    assert 10 <= len(trials) <= 13 and fms == min(t for _, t in trials)
+    fref = _singles(ctx, w, fl)
+    outs = ctx.bake_batch(fjobs, fl[0])
+    assert all(np.array_equal(a, b) for a, b in zip(outs, fref))
 
 
 def test_fused_batch_schedule_and_graph_invariance(ctx, batch_world):
@@ -134,8 +150,8 @@ def test_fused_batch_schedule_and_graph_invariance(ctx, batch_world):
         ctx.bake_batch(jobs, plist[0], vlb.BatchSchedule(0, 1, 0, 5, 6, 16))
     # the autotuner sweeps the fused knobs and keeps a schedule that bakes the same bits
     sched, ms = ctx.batch_autotune(jobs, plist[0], reps=1)
-    assert sched.ctas_per_sm in (7, 8, 9) and sched.node_steps in (4, 6, 8, 12) and ms > 0
-    assert sched.refill_idle in (8, 16, 24) and sched.graph == 1
+    assert sched.ctas_per_sm in (7, 8, 9) and sched.node_steps in (2, 4, 6, 8, 12, 16) and ms > 0
+    assert sched.refill_idle in (4, 8, 16, 24, 32) and sched.graph == 1
     outs = ctx.bake_batch(jobs, plist[0])
     assert all(np.array_equal(a, b) for a, b in zip(outs, ref))
     # a single fused bake with the tuned knobs bakes the same bits too

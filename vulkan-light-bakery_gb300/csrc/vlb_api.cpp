@@ -1129,6 +1129,21 @@ static vlb_status prepare_trace(vlb_ctx* ctx, const vlb_scene* scene, const floa
   return VLB_OK;
 }
 
+// Scene-size class of a triangle count: under 4K, 64K, 1M triangles, or more.
+static uint32_t size_class(uint32_t ntris) {
+  return ntris < 4096 ? 0u : ntris < 65536 ? 1u : ntris < (1u << 20) ? 2u : 3u;
+}
+static uint32_t batch_class(const vlb_bake_job* jobs, uint32_t njobs) {
+  uint32_t m = 0;
+  for (uint32_t i = 0; i < njobs; ++i)
+    if (jobs[i].scene) m = std::max(m, jobs[i].scene->ntris);
+  return size_class(m);
+}
+// The tuned schedule of a class, else the library default.
+static vlb_batch_schedule class_sched(const vlb_ctx* ctx, uint32_t cls) {
+  return ctx->tuned_set[cls] ? ctx->tuned[cls] : vlb_batch_schedule{0, 1, 1, 0, 0, 0};
+}
+
 // The fused walk's launch knobs of a schedule (0: the library default).
 static vlbk::FusedSched fused_sched(const vlb_batch_schedule& sc) {
   vlbk::FusedSched f;
@@ -1200,7 +1215,8 @@ vlb_status vlb_bake_ex(vlb_ctx* ctx, const vlb_scene* scene, const float* probe_
     const uint64_t items = uint64_t(nprobes) * j.chunks;
     if (items >= (1ull << 32) - (1ull << 20)) return fail(ctx, VLB_ERR_INVALID, "too many probes for one bake");
     KScope k(ctx, "trace_fused_lane");
-    vlbk::launch_trace_fused_lane(nullptr, j, 1, uint32_t(items), K, a.work_counter, fused_sched(ctx->batch_sched),
+    vlbk::launch_trace_fused_lane(nullptr, j, 1, uint32_t(items), K, a.work_counter,
+                                  fused_sched(class_sched(ctx, size_class(scene->ntris))),
                                   ctx->num_sms, ctx->stream);
     if (p->flags & VLB_BAKE_REF_ACCUMULATE) {
       KScope k(ctx, "probe_prefix");
@@ -1670,7 +1686,7 @@ vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs
                           const vlb_batch_schedule* sched) {
   if (!ctx) return VLB_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  vlb_batch_schedule sc = sched ? *sched : ctx->batch_sched;
+  vlb_batch_schedule sc = sched ? *sched : class_sched(ctx, batch_class(jobs, njobs));
   if (sc.dirs_per_item > 64) return fail(ctx, VLB_ERR_INVALID, "dirs_per_item %u > 64", sc.dirs_per_item);
   if (sc.ctas_per_sm && (sc.ctas_per_sm < 7 || sc.ctas_per_sm > 9))
     return fail(ctx, VLB_ERR_INVALID, "ctas_per_sm %u: 7, 8 or 9", sc.ctas_per_sm);
@@ -1707,43 +1723,59 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
   };
   vlb_batch_schedule win{0, 1, 1, 0, 0, 0};
   float win_ms = -1.f;
+  std::vector<vlb_tune_trial> log;
+  auto trial = [&](const vlb_batch_schedule& c) {
+    const float ms = time_one(c);
+    if (ms >= 0.f) log.push_back({c, ms});
+    if (ms >= 0.f && (win_ms < 0.f || ms < win_ms)) { win_ms = ms; win = c; }
+  };
   if (params->precision == VLB_PREC_FUSED) {
     // one knob at a time from the default, each kept at its fastest value
-    const vlb_batch_schedule start{0, 1, 0, 8, 6, 16};
-    win_ms = time_one(start);
-    win = start;
+    trial(vlb_batch_schedule{0, 1, 0, 8, 6, 16});
     auto sweep = [&](uint32_t vlb_batch_schedule::*knob, std::initializer_list<uint32_t> vals) {
+      const vlb_batch_schedule base = win;
       for (uint32_t v : vals) {
         if (st) return;
-        vlb_batch_schedule c = win;
+        if (base.*knob == v) continue;
+        vlb_batch_schedule c = base;
         c.*knob = v;
-        const float ms = time_one(c);
-        if (ms >= 0.f && ms < win_ms) { win_ms = ms; win = c; }
+        trial(c);
       }
     };
     sweep(&vlb_batch_schedule::ctas_per_sm, {7, 9});
-    sweep(&vlb_batch_schedule::node_steps, {4, 8, 12});
-    sweep(&vlb_batch_schedule::refill_idle, {8, 24});
+    sweep(&vlb_batch_schedule::node_steps, {2, 4, 8, 12, 16});
+    sweep(&vlb_batch_schedule::refill_idle, {4, 8, 24, 32});
     sweep(&vlb_batch_schedule::cost_order, {0});
   } else {
-    const uint32_t dpws[] = {1, 2, 4, 8, 16};
-    for (uint32_t order = 0; order < 2 && !st; ++order)
+    const uint32_t dpws[] = {0, 1, 2, 4, 8, 16};
+    for (uint32_t order : {1u, 0u})
       for (uint32_t dpw : dpws) {
-        const vlb_batch_schedule sc{dpw, order, 0, 0, 0, 0};
-        const float ms = time_one(sc);
         if (st) break;
-        if (win_ms < 0.f || ms < win_ms) { win_ms = ms; win = sc; }
+        trial(vlb_batch_schedule{dpw, order, 0, 0, 0, 0});
       }
   }
   win.graph = 1;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st) return st;
-  ctx->batch_sched = win;
-  ctx->batch_tuned = true;
+  const uint32_t cls = batch_class(jobs, njobs);
+  ctx->tuned[cls] = win;
+  ctx->tuned_set[cls] = true;
+  ctx->tune_log = std::move(log);
+  ctx->tune_class = cls;
   if (best) *best = win;
   if (best_ms) *best_ms = win_ms;
   return finish(ctx, true);
+}
+
+vlb_status vlb_batch_tune_log(const vlb_ctx* ctx, vlb_tune_trial* out, uint32_t cap, uint32_t* n,
+                              uint32_t* size_class_out) {
+  if (!ctx || !n) return VLB_ERR_INVALID;
+  const uint32_t m = uint32_t(ctx->tune_log.size());
+  for (uint32_t i = 0; out && i < m && i < cap; ++i) out[i] = ctx->tune_log[i];
+  *n = m;
+  if (size_class_out) *size_class_out = ctx->tune_class;
+  return VLB_OK;
 }
 
 // ---- evaluating a baked grid ------------------------------------------------------------------

@@ -402,8 +402,12 @@ struct vlb_ctx {
   uint32_t batch_graph_kernels = 0;
   std::vector<vlbk::BakeJobDev> batch_table;  // host copy of the job table
   std::vector<uint8_t> batch_meta;             // job table + scatter arrays, uploaded each call
-  bool batch_tuned = false;
-  vlb_batch_schedule batch_sched{0, 1, 1, 0, 0, 0};
+  // vlb_batch_autotune's winners by scene-size class, and its last trials
+  static constexpr int kSizeClasses = 4;
+  vlb_batch_schedule tuned[kSizeClasses] = {};
+  bool tuned_set[kSizeClasses] = {};
+  std::vector<vlb_tune_trial> tune_log;
+  uint32_t tune_class = 0;
   // vlb_ctx_test_hook: producers of the TMA pipelines issue nothing; waits
   // give up after wait_polls polls (0: the default bound)
   uint32_t hold_producer = 0, wait_polls = 0;

@@ -71,6 +71,10 @@ class BatchSchedule(C.Structure):
                 ("ctas_per_sm", C.c_uint32), ("node_steps", C.c_uint32), ("refill_idle", C.c_uint32)]
 
 
+class TuneTrial(C.Structure):
+    _fields_ = [("schedule", BatchSchedule), ("ms", C.c_float)]
+
+
 class ServiceConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("lmax", C.c_uint32), ("precision", C.c_uint32),
                 ("max_batch_probes", C.c_uint32), ("max_inflight", C.c_uint32), ("slice_probes", C.c_uint32)]
@@ -133,6 +137,7 @@ def _load() -> C.CDLL:
         "vlb_bake_trace_stats": (I32, [P, P, P, U32, P, P]),
         "vlb_bake_batch": (I32, [P, P, U32, P, P]),
         "vlb_batch_autotune": (I32, [P, P, U32, P, U32, P, P]),
+        "vlb_batch_tune_log": (I32, [P, P, U32, C.POINTER(U32), C.POINTER(U32)]),
         "vlb_service_create": (I32, [P, P, C.POINTER(P)]),
         "vlb_service_destroy": (None, [P]),
         "vlb_service_submit": (I32, [P, P, C.POINTER(U64)]),
@@ -360,6 +365,15 @@ class Context:
         self.check(lib.vlb_batch_autotune(self.h, arr, len(jobs), C.byref(params), reps, C.byref(best), C.byref(ms)))
         del keep
         return best, float(ms.value)
+
+    def batch_tune_log(self):
+        """(trials of the last batch_autotune as [(schedule dict, ms)], scene-size class)."""
+        n, cls = C.c_uint32(), C.c_uint32()
+        self.check(lib.vlb_batch_tune_log(self.h, None, 0, C.byref(n), C.byref(cls)))
+        buf = (TuneTrial * max(n.value, 1))()
+        self.check(lib.vlb_batch_tune_log(self.h, buf, n.value, C.byref(n), C.byref(cls)))
+        return [({f: getattr(buf[i].schedule, f) for f, _ in BatchSchedule._fields_}, float(buf[i].ms))
+                for i in range(n.value)], int(cls.value)
 
     def probe_eval(self, scene, coeffs, lmax: int, origin, step, counts, points, normals, shadow_bias: float = 0.005):
         """Evaluate a baked grid at shading points; returns (rgb [n,3], visibility mask [n])."""
