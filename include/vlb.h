@@ -357,7 +357,7 @@ typedef struct vlb_batch_schedule {
                              7, 8 or 9 (fewer: more registers a thread); 0 = 8 */
   uint32_t node_steps;    /* fused walk: inner-node steps of a lane turn before the leaf tests, 1..16;
                              0 = 6 */
-  uint32_t refill_idle;   /* fused walk: idle lanes that make a warp hand out new rays, 1..32; 0 = 16 */
+  uint32_t refill_idle;   /* fused walk: idle lanes that make a warp hand out new rays, 1..32; 0 = 32 */
 } vlb_batch_schedule;
 /* sched NULL: the schedule vlb_batch_autotune stored in the context for the
  * batch's scene-size class (its largest scene: under 4,096, 65,536, 1,048,576
@@ -373,7 +373,7 @@ vlb_status vlb_bake_batch(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs
  * batch.  Tile walks: rays per lane per chunk 1, 2, 4, 8, 16 x job order.
  * Fused walks (VLB_PREC_FUSED): one knob at a time from the default -- CTAs
  * per SM (warps per SM) 7, 8, 9; node steps 2, 4, 6, 8, 12, 16; refill
- * threshold 4, 8, 16, 24, 32; job order 0, 1 -- each kept at its fastest value
+ * threshold 8, 16, 24, 32; job order 0, 1 -- each kept at its fastest value
  * before the next is swept. */
 vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t njobs, const vlb_bake_params* params,
                               uint32_t reps, vlb_batch_schedule* best, float* best_ms);

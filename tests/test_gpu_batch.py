@@ -116,8 +116,8 @@ def test_batch_autotune(ctx, batch_world):
     fsched, fms = ctx.batch_autotune(fjobs, fl[0], reps=1)
     trials, _ = ctx.batch_tune_log()
     first = trials[0][0]
-    assert (first["ctas_per_sm"], first["node_steps"], first["refill_idle"], first["cost_order"]) == (8, 6, 16, 1)
-    assert 10 <= len(trials) <= 13 and fms == min(t for _, t in trials)
+    assert (first["ctas_per_sm"], first["node_steps"], first["refill_idle"], first["cost_order"]) == (8, 6, 32, 1)
+    assert 10 <= len(trials) <= 12 and fms == min(t for _, t in trials)
     fref = _singles(ctx, w, fl)
     outs = ctx.bake_batch(fjobs, fl[0])
     assert all(np.array_equal(a, b) for a, b in zip(outs, fref))

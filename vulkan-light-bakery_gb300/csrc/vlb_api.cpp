@@ -1731,7 +1731,7 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
   };
   if (params->precision == VLB_PREC_FUSED) {
     // one knob at a time from the default, each kept at its fastest value
-    trial(vlb_batch_schedule{0, 1, 0, 8, 6, 16});
+    trial(vlb_batch_schedule{0, 1, 0, 8, 6, 32});
     auto sweep = [&](uint32_t vlb_batch_schedule::*knob, std::initializer_list<uint32_t> vals) {
       const vlb_batch_schedule base = win;
       for (uint32_t v : vals) {
@@ -1744,7 +1744,7 @@ vlb_status vlb_batch_autotune(vlb_ctx* ctx, const vlb_bake_job* jobs, uint32_t n
     };
     sweep(&vlb_batch_schedule::ctas_per_sm, {7, 9});
     sweep(&vlb_batch_schedule::node_steps, {2, 4, 8, 12, 16});
-    sweep(&vlb_batch_schedule::refill_idle, {4, 8, 24, 32});
+    sweep(&vlb_batch_schedule::refill_idle, {8, 16, 24});
     sweep(&vlb_batch_schedule::cost_order, {0});
   } else {
     const uint32_t dpws[] = {0, 1, 2, 4, 8, 16};

@@ -305,7 +305,7 @@ inline uint32_t fused_chunk_major(uint32_t S) { return uint64_t(S) * 64 > (16ull
 struct FusedSched {
   uint32_t ctas_per_sm = 8;  // register budget: 7, 8 or 9 resident 4-warp CTAs per SM
   uint32_t node_steps = 6;   // inner-node steps per turn
-  uint32_t refill_idle = 16; // idle lanes that trigger a refill
+  uint32_t refill_idle = 32; // idle lanes that trigger a refill
 };
 // One persistent launch: warps pull work items (job, probe, direction chunk)
 // from *counter (zero before the launch), trace them per lane and project
