@@ -5,11 +5,12 @@ Workload (one "step"): bake the 64x64x64 probe grid (262,144 probes, the
 reference's breadth-first grid order over the scene bounds) of the 4096-box
 scene (49,162 triangles, open unit room, seeded sun + 128^2 cubemap sky) with
 1024 shared Fibonacci directions per probe, L2 SH -- 268,435,456 primary rays
-plus the sun shadow rays.  The chosen path (VLB_PREC_FUSED: trace, shading
-and projection in one kernel, FP32, no radiance tile) is timed with inputs
-resident in HBM; the plain FP32 path (radiance tile + CUDA-core projection,
-the drop-in), the mixed path (BF16 hi/lo tile + tcgen05 projection) and the
-one-BF16 form are timed beside it; `e2e` times the public C-ABI call with
+plus the sun shadow rays.  The chosen path is the library's default
+(VLB_PREC_FP32: the lane walk traces into an FP32 radiance tile, a CUDA-core
+kernel projects it), timed with inputs resident in HBM; the one-kernel path
+(VLB_PREC_FUSED: trace, shading and projection in one kernel, no tile), the
+mixed path (BF16 hi/lo tile + tcgen05 projection) and the one-BF16 form are
+timed beside it; `e2e` times the public C-ABI call with
 pinned host probe positions in and host SH out.  L2 is flushed (256 MiB
 write) before every timed step; each step is bracketed by CUDA events on the
 context's stream.  Accuracy is measured against the FP64 oracle on a spread
@@ -50,12 +51,18 @@ LMAX = 2
 SKY_N = 128
 WORKLOAD = ("probe bake 64^3 probes x 1024 Fibonacci dirs, 4096-box scene (49,162 tris), sun + 128^2 cubemap "
             "sky, L2 SH")
-METRIC_FULL = "probes/s, Grays/s, p99 bake latency: chosen vs plain FP32, <=1e-4 SH rel err"
-# The headline kernel's per-launch figures from one ncu capture of the same
-# workload (profiles/trace_fused_c2.md gives the command): DRAM bytes read +
-# written, warp instructions issued, ncu's L1 and issue utilisation.
-TRACE_NCU = {"capture": "profiles/trace_fused_c2.md", "dram_bytes": 490277888, "warp_instructions": 156708407819,
-             "l1tex_throughput_pct": 84.5, "issue_active_pct": 70.5}
+METRIC_FULL = "probes/s, Grays/s, p99 bake latency of the default path, <=1e-4 SH rel err"
+# The trace kernels' per-launch figures from ncu captures (the named profile
+# gives the command): DRAM bytes read + written and warp instructions issued
+# per launch of the headline workload, ncu's L1 and issue utilisation.
+TRACE_NCU = {
+    "trace_tile": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
+                   "dram_bytes": 3158200000, "warp_instructions": 141878000000,
+                   "l1tex_throughput_pct": 91.8, "issue_active_pct": 72.9},
+    "trace_fused_lane": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
+                         "dram_bytes": 266100000, "warp_instructions": 144591000000,
+                         "l1tex_throughput_pct": 82.8, "issue_active_pct": 70.0},
+}
 
 
 def parse():
@@ -70,6 +77,10 @@ def parse():
                     default=None,
                     help="time one section alone (for profiling captures); prints its JSON object")
     ap.add_argument("--no-sections", action="store_true", help="headline only (skip the C0/C1/C3/C4 sections)")
+    ap.add_argument("--bake-precision", choices=["fp32", "fused"], default="fp32",
+                    help="--only bake: the path to time")
+    ap.add_argument("--bake-grid", type=int, default=GRID[0],
+                    help="--only bake: probes per grid axis (a smaller grid for ncu captures)")
     return ap.parse_args()
 
 
@@ -272,7 +283,7 @@ def accuracy_vs_fp64(ctx, scene, probes, params, pos, idx, alb, sky, sun, nsampl
             "note": "max/mean: decisions replayed; direct: the oracle's own FP64 decisions"}
 
 
-def trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, peaks_measured, P, ntri, K, C):
+def trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, peaks_measured, P, ntri, K, C, tile):
     """Roofline of the trace kernel.  It is bound by instruction issue or by
     L1 throughput (the scene's nodes and triangles stay in L1/L2), not by HBM:
     `bound` names whichever of the two the committed ncu capture of this
@@ -286,12 +297,19 @@ def trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, peaks_measured, P
     l1_bytes = stats["bytes"]
     l1_peak = sms * 128 * mhz * 1e6 / 1e9
     issue_peak = sms * 4 * mhz * 1e6
-    wi = TRACE_NCU["warp_instructions"]
-    # DRAM-level algorithmic bytes of one fused launch: probes and their order
-    # in, SH out, the chunk partials written and read once, the scene's nodes,
-    # triangles and albedo, the direction, reciprocal, order and basis tables
-    dram_alg = (P * (12 + 4 + K * 12 + 4) + (P * C * K * 3 * 4 * 2 if C > 1 else 0) + max(ntri - 1, 0) * 64
-                + ntri * (48 + 16) + NDIRS * (16 + 16 + 4 + 64))
+    ncu = TRACE_NCU.get(kname, {"capture": None, "dram_bytes": None, "warp_instructions": None,
+                                "l1tex_throughput_pct": None, "issue_active_pct": None})
+    wi = ncu["warp_instructions"]
+    if tile:
+        # one tile launch: probes and their order in, the FP32 radiance tile
+        # out, the scene's nodes, triangles and albedo, the direction tables
+        dram_alg = (P * (12 + 4) + P * NDIRS * 12 + max(ntri - 1, 0) * 64 + ntri * (48 + 16)
+                    + NDIRS * (16 + 16 + 4))
+    else:
+        # one fused launch: probes and their order in, SH out, the chunk
+        # partials written and read once, the scene, the direction and basis tables
+        dram_alg = (P * (12 + 4 + K * 12 + 4) + (P * C * K * 3 * 4 * 2 if C > 1 else 0) + max(ntri - 1, 0) * 64
+                    + ntri * (48 + 16) + NDIRS * (16 + 16 + 4 + 64))
     l1 = {"achieved": l1_bytes / secs / 1e9 if secs else None, "peak": l1_peak, "unit": "GB/s",
           "peak_source": f"nominal L1: {sms} SMs x 128 B/clock x {mhz:.0f} MHz (no measured L1 peak)",
           "requested_bytes_per_launch": l1_bytes}
@@ -303,12 +321,12 @@ def trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, peaks_measured, P
            "algorithmic_bytes_per_launch": dram_alg,
            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks_measured else "fallback 6.8 TB/s"}
     hbm["frac"] = hbm["achieved"] / hbm_peak if hbm["achieved"] else None
-    l1p, isp = TRACE_NCU["l1tex_throughput_pct"], TRACE_NCU["issue_active_pct"]
+    l1p, isp = ncu["l1tex_throughput_pct"], ncu["issue_active_pct"]
     main = issue if (l1p is not None and isp is not None and isp >= l1p and wi) else l1
     bound = "issue" if main is issue else "l1"
     return {"kernel": kname, "bound": bound, "achieved": main["achieved"], "peak": main["peak"], "unit": main["unit"],
-            "frac": main["frac"], "traffic": TRACE_NCU["dram_bytes"], "avg_launch_ms": k_avg_ms,
-            "peak_source": main["peak_source"], "l1": l1, "issue": issue, "hbm": hbm, "ncu": TRACE_NCU,
+            "frac": main["frac"], "traffic": ncu["dram_bytes"], "avg_launch_ms": k_avg_ms,
+            "peak_source": main["peak_source"], "l1": l1, "issue": issue, "hbm": hbm, "ncu": ncu,
             "node_tests_per_ray": stats["node_tests_per_ray"], "node_fetches_per_ray": stats["node_fetches_per_ray"]}
 
 
@@ -341,6 +359,7 @@ def main():
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     if args.only:
+        BAKE_ONLY.update(precision=args.bake_precision, grid=args.bake_grid)
         fn = {"bake": bake_measure, "c1": c1_measure, "skybox": skybox_measure, "projection": projection_measure,
               "batch": batch_measure, "service": service_measure, "refbake": refbake_measure}[args.only]
         print(json.dumps(fn(ctx, torch, stream, args.steps, hbm_peak)), flush=True)
@@ -360,7 +379,7 @@ def main():
         "mixed": vlb.bake_params(dirs, LMAX, vlb.PREC_MIXED, sun, sky=skyh),
         "bf16": vlb.bake_params(dirs, LMAX, vlb.PREC_BF16, sun, sky=skyh),
     }
-    chosen = "fused"
+    chosen = "fp32"  # the library's default precision
 
     def barrier():
         if dist is not None:
@@ -389,7 +408,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     ms_chosen, launches = timed(chosen, args.steps)
-    ms_plain, _ = timed("fp32", args.steps)
+    ms_fused, _ = timed("fused", args.steps)
     clk = clocks.stop()
     res_chosen = d_out.cpu().numpy().copy()
     side = {n: timed(n, max(3, args.steps // 3))[0] for n in ("mixed", "bf16")}
@@ -397,6 +416,9 @@ def main():
     ctx.profile_reset()
     timed(chosen, min(args.steps, 5), profile=True)
     prof = ctx.profile()
+    ctx.profile_reset()
+    timed("fused", min(args.steps, 5), profile=True)
+    prof_fused = ctx.profile()
     # per-ray work counts for the L1 bytes (one instrumented bake, untimed)
     stats = ctx_trace_stats(ctx, scene, d_probes, params["fp32"])
 
@@ -404,9 +426,9 @@ def main():
         return max_over_ranks(sum(ms), dist, "cuda")
 
     tot_chosen = agg(ms_chosen)
-    tot_plain = agg(ms_plain)
+    tot_fused = agg(ms_fused)
     value = whole_job_rate(P * args.steps, world, tot_chosen)
-    plain = whole_job_rate(P * args.steps, world, tot_plain)
+    fused_value = whole_job_rate(P * args.steps, world, tot_fused)
 
     # e2e: public call with pinned host buffers (H2D probes, D2H SH) inside the timed region
     h_probes = torch.from_numpy(probes).pin_memory()
@@ -429,15 +451,20 @@ def main():
     # the timed bake's outputs equal the sample bake's (the sample checks the timed bake)
     sel = spread(P, 256)
     same = bool(np.array_equal(ctx.bake(scene, probes[sel], params[chosen]), res_chosen[sel]))
-    kname = max(prof, key=lambda k: prof[k][1])
-    klaunch, kms = prof.get(kname, (0, 0.0))
-    k_avg_ms = kms / max(klaunch, 1)
     ntri = int(idx.shape[0])
     per = -(-NDIRS // 16)        # the fused walk's chunk: at most 16 per probe,
     D = min(-(-per // 64) * 64, 4096)  # a multiple of 64 rays, at most 4096
     C = -(-NDIRS // D)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    roof = trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, bool(peaks), P, ntri, K, C)
+
+    def roof_of(pr, tile):
+        kname = max(pr, key=lambda k: pr[k][1])
+        klaunch, kms = pr.get(kname, (0, 0.0))
+        return trace_roofline(kname, kms / max(klaunch, 1), stats, clk, sms, hbm_peak, bool(peaks), P, ntri, K, C,
+                              tile)
+
+    roof = roof_of(prof, True)
+    roof_fused = roof_of(prof_fused, False)
     step_ms = sorted(ms_chosen)
     p50 = step_ms[len(step_ms) // 2]
     p99 = step_ms[min(len(step_ms) - 1, int(round(0.99 * (len(step_ms) - 1))))]
@@ -451,23 +478,25 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded SplitMix64 scene, sky and sun)",
         "config": config_dict(P, ntri),
-        "timing": {"path": "VLB_PREC_FUSED (" + "+".join(sorted(prof)) + ")",
+        "timing": {"path": "VLB_PREC_FP32, the library default (" + "+".join(sorted(prof)) + ")",
                    "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{world}"},
         "grays_per_s": value * NDIRS / 1e9,
         "grays_incl_shadow_per_s": value * (NDIRS + stats["shadow_rays"] / P) / 1e9,
         "latency_ms": {"p50": p50, "p99": p99},
-        "plain_fp32": {"value": plain, "unit": "probes/s", "ms": tot_plain / args.steps,
-                       "p99_ms": sorted(ms_plain)[-1], "rel_err_vs_fp64": acc["fp32"]},
-        "chosen_vs_plain": value / plain,
+        "fused_one_kernel": {"value": fused_value, "unit": "probes/s", "ms": tot_fused / args.steps,
+                             "p99_ms": sorted(ms_fused)[-1], "rel_err_vs_fp64": acc["fused"],
+                             "roofline": roof_fused,
+                             "kernels_ms": {k: {"launches": v[0], "avg_ms": v[1] / max(v[0], 1)}
+                                            for k, v in prof_fused.items()}},
         "precisions": {
-            "fused": {"ms": tot_chosen / args.steps, "rel_err_vs_fp64": acc["fused"],
-                      "timed_bake_matches_sample": same},
-            "fp32": {"ms": tot_plain / args.steps, "rel_err_vs_fp64": acc["fp32"]},
+            "fp32": {"ms": tot_chosen / args.steps, "rel_err_vs_fp64": acc["fp32"],
+                     "timed_bake_matches_sample": same},
+            "fused": {"ms": tot_fused / args.steps, "rel_err_vs_fp64": acc["fused"]},
             "mixed_bf16_hilo_tcgen05": {"ms": sum(side["mixed"]) / len(side["mixed"]),
                                         "rel_err_vs_fp64": acc["mixed"]},
             "bf16_tcgen05": {"ms": sum(side["bf16"]) / len(side["bf16"]), "rel_err_vs_fp64": acc["bf16"],
                              "note": "one BF16 per radiance sample: the stated-error form"}},
-        "sh_rel_err_vs_fp64": acc["fused"],
+        "sh_rel_err_vs_fp64": acc["fp32"],
         "e2e": {"value": e2e_value, "unit": "probes/s", "h2d_bytes_per_step": int(P * 12),
                 "d2h_bytes_per_step": int(P * K * 12)},
         "gpu_launches": int(launches),
@@ -492,15 +521,20 @@ def main():
     return 0
 
 
+BAKE_ONLY = {"precision": "fp32", "grid": GRID[0]}
+
+
 def bake_measure(ctx, torch, stream, steps, hbm_peak):
-    """The headline workload's chosen path alone (VLB_PREC_FUSED on the
-    4096-box scene, 262,144 probes x 1024 directions): `steps` bakes with
-    inputs resident in HBM, per-kernel library times (for profiling captures)."""
+    """The headline workload's bake alone (the 4096-box scene, n^3 probes x
+    1024 directions; --bake-precision, --bake-grid): `steps` bakes with inputs
+    resident in HBM, per-kernel library times (for profiling captures)."""
     import vlb
 
-    pos, idx, alb, sky, sun, probes = workload_inputs()
+    n = BAKE_ONLY["grid"]
+    pos, idx, alb, sky, sun, probes = grid_probes(vlb, NBOXES, (n, n, n))
     scene = ctx.scene(pos, idx, alb)
-    p = vlb.bake_params(ctx.fibonacci(NDIRS), LMAX, vlb.PREC_FUSED, sun, sky=ctx.sky(sky, SKY_N))
+    prec = vlb.PREC_FUSED if BAKE_ONLY["precision"] == "fused" else vlb.PREC_FP32
+    p = vlb.bake_params(ctx.fibonacci(NDIRS), LMAX, prec, sun, sky=ctx.sky(sky, SKY_N))
     d_probes = torch.from_numpy(probes).cuda()
     out = torch.empty((probes.shape[0], vlb.k_of(LMAX), 3), dtype=torch.float32, device="cuda")
     ctx.bake(scene, d_probes, p, out=out)
@@ -511,7 +545,9 @@ def bake_measure(ctx, torch, stream, steps, hbm_peak):
         ctx.bake(scene, d_probes, p, out=out)
     torch.cuda.synchronize()
     ctx.set_profiling(False)
-    return {"workload": WORKLOAD, "kernels_ms": {k: v[1] / max(v[0], 1) for k, v in ctx.profile().items()}}
+    return {"workload": f"probe bake {n}^3 probes x {NDIRS} Fibonacci dirs, {NBOXES}-box scene, "
+                        f"{BAKE_ONLY['precision']}",
+            "kernels_ms": {k: v[1] / max(v[0], 1) for k, v in ctx.profile().items()}}
 
 
 def c1_measure(ctx, torch, stream, steps, hbm_peak):

@@ -36,7 +36,7 @@
 namespace vlbk {
 
 constexpr int kSubRays = 32;
-constexpr int kSubBufs = 4;
+constexpr int kSubBufs = 2;
 constexpr uint32_t kSubFirst = 1, kSubLast = 2;
 
 // One sub-batch in flight.
@@ -48,10 +48,11 @@ struct SubBatch {
 // Per-warp shared state.  Everything but the lanes' own rays is warp-uniform
 // and lives here, not in registers (the trace walk needs them): written by
 // lane 0 only, read by every lane after a __syncwarp.
+template <int V>
 struct FusedWarp {
   float rad[kSubBufs][3][kSubRays];    // RGB of each ray, channel-major
   SubBatch q[kSubBufs];
-  double acc[48];                      // the current item's running FP64 sums, output v at acc[v]
+  double acc[V];                       // the current item's running FP64 sums, output v at acc[v]
   uint32_t head, n;                    // ring: oldest slot, sub-batches in flight
   uint32_t ij, ip, ic, itn, ite, it0;  // the item being cut: job, probe, chunk, next/end/first ray
   uint32_t have_item, exhausted;
@@ -77,7 +78,7 @@ __device__ __forceinline__ uint32_t find_job(const BakeJobDev* __restrict__ jobs
 // sums and, after the item's last sub-batch, writes the item (output or
 // partial, and the probe's FP64 chunk sum when its last chunk is done).
 template <int K, bool MULTI>
-__device__ __forceinline__ void retire_head(FusedWarp& fw, const BakeJobDev* __restrict__ jobs,
+__device__ __forceinline__ void retire_head(FusedWarp<3 * K>& fw, const BakeJobDev* __restrict__ jobs,
                                             const BakeJobDev& one, uint32_t lane) {
   constexpr int V = 3 * K;
   const uint32_t e = fw.head;
@@ -123,8 +124,8 @@ __device__ __forceinline__ void retire_head(FusedWarp& fw, const BakeJobDev* __r
 // Appends the next sub-batch (of the current item, or of a new item from the
 // counter) to the ring while there is room and the newest one has handed out
 // all its rays.
-template <bool MULTI>
-__device__ __forceinline__ void fill_ring(FusedWarp& fw, const BakeJobDev* __restrict__ jobs, const BakeJobDev& one,
+template <bool MULTI, class FW>
+__device__ __forceinline__ void fill_ring(FW& fw, const BakeJobDev* __restrict__ jobs, const BakeJobDev& one,
                                           uint32_t njobs, uint32_t total, uint32_t* counter, uint32_t lane) {
   while (fw.n < kSubBufs) {
     const uint32_t n = fw.n;
@@ -179,7 +180,8 @@ __device__ __forceinline__ void fill_ring(FusedWarp& fw, const BakeJobDev* __res
 }
 
 // A finished ray: its RGB into the ring, and the per-ray debug arrays.
-__device__ __forceinline__ void store_ray(FusedWarp& fw, const BakeJobDev& J, const LaneRay& L, const Shaded& o,
+template <class FW>
+__device__ __forceinline__ void store_ray(FW& fw, const BakeJobDev& J, const LaneRay& L, const Shaded& o,
                                           uint32_t lslot) {
   const uint32_t le = lslot >> 8, lpos = lslot & 255;
   if (!VLB_INB(le, kSubBufs, J.err) || !VLB_INB(lpos, kSubRays, J.err)) return;
@@ -203,9 +205,9 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
                                                                      const BakeJobDev one, uint32_t njobs,
                                                                      uint32_t total, uint32_t* counter,
                                                                      uint32_t node_steps, uint32_t refill_idle) {
-  __shared__ FusedWarp fw_all[kTraceWarps];
+  __shared__ FusedWarp<3 * K> fw_all[kTraceWarps];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  FusedWarp& fw = fw_all[warp];
+  FusedWarp<3 * K>& fw = fw_all[warp];
   if (lane == 0) {
     fw.head = fw.n = 0;
     fw.have_item = fw.exhausted = 0;
@@ -316,7 +318,7 @@ static void launch_k(const BakeJobDev* jobs, const BakeJobDev& one, uint32_t njo
     cudaGetDevice(&dev);
     const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
     if (bit && !(carved.load(std::memory_order_relaxed) & bit)) {
-      const size_t need = sizeof(FusedWarp) * kTraceWarps * size_t(per_sm);
+      const size_t need = sizeof(FusedWarp<3 * K>) * kTraceWarps * size_t(per_sm);
       const int pct = int(std::min<size_t>(100, (need * 100 + 228 * 1024 - 1) / (228 * 1024)));
       cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
       carved.fetch_or(bit, std::memory_order_relaxed);
