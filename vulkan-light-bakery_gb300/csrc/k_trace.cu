@@ -228,7 +228,9 @@ __device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, 
 }
 
 template <bool COUNT, bool WIDE, bool REF>
-__global__ void __launch_bounds__(kTraceThreads) k_trace_dyn(const TraceArgs a) {
+// Nine resident CTAs per SM (at most 56 registers): measured 1.7 % faster on
+// the config-2 bake than the unconstrained 60 registers (eight CTAs).
+__global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
   const uint32_t R = P * a.S;

@@ -630,6 +630,7 @@ vlb_status vlb_scene_create_ex(vlb_ctx* ctx, const float* positions, uint32_t st
     }
     if (st == VLB_OK) st = finish(ctx, true);
     if (st == VLB_OK && (flags & VLB_SCENE_TRAVERSAL_WIDE)) st = vlbh::build_wide(ctx, sc);
+    if (st == VLB_OK) st = vlbh::pair_siblings(ctx, sc);
   }
   cudaFree(dpos); cudaFree(didx); if (dalb) cudaFree(dalb); cudaFree(scr);
   if (st != VLB_OK) { vlb_scene_destroy(sc); return st; }

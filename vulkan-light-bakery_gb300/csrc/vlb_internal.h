@@ -369,6 +369,9 @@ vlb_status ctx_finish(vlb_ctx* ctx, bool sync);
 // Collapses the scene's binary traversal tree into the 8-wide quantised tree
 // (sc->wnodes, sc->nwide; wide_bvh.cpp).  Synchronous.
 vlb_status build_wide(vlb_ctx* ctx, vlb_scene* sc);
+// Re-lays the binary traversal tree with siblings in one 128-byte line
+// (2n - 2 node slots); same tree, same results.
+vlb_status pair_siblings(vlb_ctx* ctx, vlb_scene* sc);
 vlb_status ctx_fail(vlb_ctx* ctx, vlb_status s, const char* msg);
 }  // namespace vlbh
 

@@ -1,4 +1,5 @@
-// wide_bvh.cpp -- the 8-wide quantised traversal tree of a scene (host build).
+// wide_bvh.cpp -- host passes over a scene's traversal tree: the 8-wide
+// quantised tree (build_wide) and the sibling-pair node layout (pair_siblings).
 //
 // The binary traversal tree (PLOC clustering, or the LBVH) is collapsed into
 // nodes of up to 8 children: starting from a binary node's two children, the
@@ -163,5 +164,71 @@ vlb_status vlbh::build_wide(vlb_ctx* ctx, vlb_scene* sc) {
   sc->wnodes = dev;
   sc->nwide = uint32_t(wide.size() / 6);
   sc->bytes += wide.size() * sizeof(float4);
+  return VLB_OK;
+}
+
+// Sibling-pair layout of the binary traversal tree.  A walk that leaves node N
+// goes to one of N's two children, and the lanes of a warp that leave N
+// together go to either: storing both children in one 128-byte line (slots 2k
+// and 2k + 1 of the 64-byte nodes) lets those lanes' fetches share a line.
+// Slots are handed out depth first from the root (slot 0; slot 1 stays
+// empty), a pair per node with an internal child (a half-empty pair when only
+// one child is internal), so the array has at most 2n - 2 slots; it is
+// allocated with exactly 2n - 2 (unused slots zero) so every slot index a walk
+// can meet is inside it.  Only the storage changes: every walk visits the same
+// nodes in the same order and returns the same bits.
+vlb_status vlbh::pair_siblings(vlb_ctx* ctx, vlb_scene* sc) {
+  const uint32_t n = sc->ntris;
+  if (n < 3) return VLB_OK;  // one node: nothing to pair
+  const size_t nold = n - 1, nslots = 2 * size_t(n) - 2;
+  std::vector<float4> old(nold * 4);
+  if (cudaMemcpy(old.data(), sc->nodes, old.size() * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return ctx_fail(ctx, VLB_ERR_CUDA, "node layout: traversal tree download failed");
+  }
+  std::vector<float4> out(nslots * 4, make_float4(0.f, 0.f, 0.f, 0.f));
+  // (old index, new slot) of nodes whose children still need slots
+  std::vector<std::pair<int32_t, uint32_t>> stack{{0, 0}};
+  uint32_t next = 2;
+  while (!stack.empty()) {
+    const auto [oi, ns] = stack.back();
+    stack.pop_back();
+    float4 q[4];
+    for (int k = 0; k < 4; ++k) q[k] = old[4 * size_t(oi) + k];
+    int32_t c[2];
+    std::memcpy(&c[0], &q[3].x, 4);
+    std::memcpy(&c[1], &q[3].y, 4);
+    if (c[0] >= 0 || c[1] >= 0) {
+      if (next + 2 > nslots) return ctx_fail(ctx, VLB_ERR_INTERNAL, "node layout: slot count exceeded");
+      const uint32_t base = next;
+      next += 2;
+      uint32_t used = 0;
+      int32_t nc[2] = {c[0], c[1]};
+      for (int h = 0; h < 2; ++h)
+        if (c[h] >= 0) {
+          if (uint32_t(c[h]) >= nold) return ctx_fail(ctx, VLB_ERR_INTERNAL, "node layout: bad child");
+          nc[h] = int32_t(base + used++);
+        }
+      std::memcpy(&q[3].x, &nc[0], 4);
+      std::memcpy(&q[3].y, &nc[1], 4);
+      // push the second child first so the first is laid out (and walked) first
+      for (int h = 1; h >= 0; --h)
+        if (c[h] >= 0) stack.push_back({c[h], uint32_t(nc[h])});
+    }
+    for (int k = 0; k < 4; ++k) out[4 * size_t(ns) + k] = q[k];
+  }
+  float4* dev = nullptr;
+  if (cudaMalloc(&dev, out.size() * sizeof(float4)) != cudaSuccess) {
+    cudaGetLastError();
+    return ctx_fail(ctx, VLB_ERR_OOM, "node layout allocation failed");
+  }
+  if (cudaMemcpy(dev, out.data(), out.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(dev);
+    return ctx_fail(ctx, VLB_ERR_CUDA, "node layout upload failed");
+  }
+  cudaFree(sc->nodes);
+  sc->nodes = dev;
+  sc->bytes += nslots * 64 - nold * 64;
   return VLB_OK;
 }
