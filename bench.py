@@ -452,7 +452,7 @@ def main():
     sel = spread(P, 256)
     same = bool(np.array_equal(ctx.bake(scene, probes[sel], params[chosen]), res_chosen[sel]))
     ntri = int(idx.shape[0])
-    per = -(-NDIRS // 16)        # the fused walk's chunk: at most 16 per probe,
+    per = -(-NDIRS // 4)         # the fused walk's chunk: at most 4 per probe,
     D = min(-(-per // 64) * 64, 4096)  # a multiple of 64 rays, at most 4096
     C = -(-NDIRS // D)
     sms = torch.cuda.get_device_properties(local).multi_processor_count

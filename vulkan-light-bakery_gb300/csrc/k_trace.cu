@@ -239,20 +239,48 @@ __global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs 
   LaneRay L;
   make_ray(L.ray, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f);
   bool exhausted = false;
+  // A warp takes its rays in blocks of `block` consecutive rays (whole 32-ray
+  // groups of one probe's neighbouring directions) and hands a block's groups
+  // to its lanes one by one: its next rays then reuse the nodes its last ones
+  // fetched.  Blocks are sized by the rays per warp, so that every warp still
+  // takes about 64 blocks (the load stays balanced): up to 16 groups on the
+  // config-2 bake (9.5 % faster than one group), one group on small bakes.
+  // the warp's block (next ray, end) lives in shared memory: it is touched only
+  // when the warp takes rays, and the walk's registers stay free
+  __shared__ uint32_t s_block[kTraceWarps][2];
+  uint32_t* wblk = s_block[threadIdx.x >> 5];
+  if (lane == 0) { wblk[0] = 0; wblk[1] = 0; }
+  __syncwarp();
   for (;;) {
     const unsigned idle = __ballot_sync(kFull, !L.has);
-    if (!exhausted && (idle == kFull || __popc(idle) >= kRefillIdle)) {
-      const int leader = __ffs(idle) - 1;
-      uint32_t base = 0;
-      if (int(lane) == leader) base = atomicAdd(a.work_counter, uint32_t(__popc(idle)));
-      base = __shfl_sync(kFull, base, leader);
-      if (base >= R) exhausted = true;
-      if (!L.has) {
-        const uint32_t r = base + __popc(idle & lane_lt_mask());
-        if (r < R) {
-          const uint32_t sl = r / a.S, t = r - sl * a.S;
-          if (sl < a.nprobes) lr_start(a, L, a.order[sl], __ldg(a.dir_order + t));
+    if (!exhausted && idle == kFull) {  // a whole idle warp takes its next 32 rays together
+      const uint32_t groups_per_warp = (R / 32) / (gridDim.x * kTraceWarps);
+      const uint32_t block = 32u * min(16u, max(1u, groups_per_warp / 64));
+      uint32_t wb;
+      if (block == 32) {  // one group a block: straight from the counter
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(a.work_counter, 32u);
+        wb = __shfl_sync(kFull, base, 0);
+        if (wb >= R) exhausted = true;
+      } else {
+        wb = wblk[0];
+        if (wb >= wblk[1]) {
+          uint32_t base = 0;
+          if (lane == 0) base = atomicAdd(a.work_counter, block);
+          base = __shfl_sync(kFull, base, 0);
+          wb = base;
+          if (base >= R) exhausted = true;
+          __syncwarp();
+          if (lane == 0) wblk[1] = base + block;
         }
+        __syncwarp();
+        if (lane == 0) wblk[0] = wb + 32;
+        __syncwarp();
+      }
+      const uint32_t r = wb + lane;
+      if (r < R) {
+        const uint32_t sl = r / a.S, t = r - sl * a.S;
+        if (sl < a.nprobes) lr_start(a, L, a.order[sl], __ldg(a.dir_order + t));
       }
     }
     if (!__any_sync(kFull, L.has)) {
