@@ -87,8 +87,8 @@ uint64_t vlb_ctx_launch_count(const vlb_ctx* ctx);
  * an unbounded fence wait whose result is printed, src/application.cpp:
  * 265-273).  Makes the bounded device waits give up on purpose without
  * faulting the GPU: with VLB_HOOK_HOLD_PRODUCER the copy-issuing thread of
- * the TMA pipelines (the skybox projection's producer warp, the tcgen05
- * projection's TMA thread) issues nothing, so no copy is ever in flight;
+ * the TMA pipelines (the skybox projection's producer warp, the FP32 and the
+ * tcgen05 projections' TMA threads) issues nothing, so no copy is ever in flight;
  * each waiting thread gives up after `wait_polls` mbarrier polls (0: the
  * library's bound), the kernel stops (the tcgen05 kernel frees its tensor
  * memory) and the call returns VLB_ERR_TIMEOUT.  hook 0 clears it; the

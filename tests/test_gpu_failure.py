@@ -104,6 +104,23 @@ def test_tensor_core_projection_wait_runs_out(ctx):
         assert np.array_equal(ctx.project(bits, n, ds, 3, dtype=vlb.DTYPE_BF16), good)
 
 
+def test_fp32_projection_wait_runs_out(ctx):
+    """The TMA-staged FP32 projection (the default bake's): its consumer warps
+    give up when the producer is held."""
+    n, S = 300, 1024
+    ds = ctx.fibonacci(S)
+    rad = np.random.default_rng(11).random((n, 3, S)).astype(np.float32)
+    good = ctx.project(rad, n, ds, 2)
+    ctx.test_hook(vlb.HOOK_HOLD_PRODUCER, 1024)
+    try:
+        with pytest.raises(vlb.VlbError) as e:
+            ctx.project(rad, n, ds, 2)
+        assert e.value.status == vlb.ERR_TIMEOUT, e.value
+    finally:
+        ctx.test_hook(0)
+    assert np.array_equal(ctx.project(rad, n, ds, 2), good)
+
+
 def test_hook_is_validated(ctx):
     with pytest.raises(vlb.VlbError) as e:
         ctx.test_hook(7)

@@ -203,7 +203,14 @@ static void launch_project(const T* rad, uint32_t nprobes, uint32_t S, const flo
 }
 
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
-                        float* out, float* partial, cudaStream_t s) {
+                        float* out, float* partial, cudaStream_t s, int* err, int num_sms, uint32_t hold,
+                        uint32_t wait_polls) {
+  // unsplit tiles (enough rows for the whole GPU) go through the TMA-staged kernel
+  uint32_t per = 0;
+  const uint32_t rows = nprobes * 3;
+  if (err && num_sms && S && project_splits(rows, S, &per) == 1 &&
+      launch_project_f32_tma(radiance, nprobes, S, basis16, K, out, err, num_sms, s, hold, wait_polls))
+    return;
   launch_project<float>(radiance, nprobes, S, basis16, K, out, partial, 0, s);
 }
 

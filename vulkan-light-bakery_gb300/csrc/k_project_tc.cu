@@ -243,6 +243,136 @@ bool make_map(CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t outer, u
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// ---- FP32 tile projection through TMA (the default path's projection) -------------
+// The same per-row sums as k_project<float> (one thread a row, every sample in
+// order, FP32 fmaf: the same bits), with the tile staged by the TMA engine:
+// a producer warp streams [256 rows x 32 samples] boxes of the row-major tile
+// (128-byte rows, 128-byte swizzle) and the matching 32 x 16 basis rows (a 1-D
+// bulk copy) into a kF32Stages ring; four consumer warps, two rows a thread
+// (t and t + 128: each basis broadcast serves both), read their rows' 16-byte
+// chunks at the swizzled positions (chunk q of row r sits at q ^ (r & 7):
+// eight consecutive rows hit eight different bank groups, no conflicts).
+// Persistent CTAs take row tiles in turn.  A two-stage ring keeps three CTAs
+// (twelve consumer warps) on an SM: measured on the config-2 tile [786,432 x
+// 1024] at 92 % of the HBM copy rate (three stages, two CTAs: 74 %; one row a
+// thread: 49 %; the cp.async kernel k_project<float>: 62 %).
+constexpr int kF32Rows = 256, kF32Cols = 32;  // two rows a consumer thread: t and t + 128
+constexpr int kF32Stages = 2;
+constexpr int kF32Threads = 160;                                     // 4 consumer warps + 1 producer warp
+constexpr uint32_t kF32TileBytes = kF32Rows * kF32Cols * 4;         // 32 KiB
+constexpr uint32_t kF32BasBytes = kF32Cols * 16 * 4;                // 2 KiB
+constexpr uint32_t kF32StageBytes = kF32TileBytes + kF32BasBytes;   // 34 KiB, a multiple of 1024
+constexpr size_t kF32SmemBytes = size_t(kF32Stages) * kF32StageBytes + 1024;
+static_assert(kF32StageBytes % 1024 == 0, "stages stay 1024-byte aligned for the swizzle");
+
+template <int K>
+__global__ void __launch_bounds__(kF32Threads) k_project_f32_tma(const __grid_constant__ CUtensorMap tm,
+                                                                 const float* __restrict__ basis16, uint32_t rows,
+                                                                 uint32_t S, float* __restrict__ out, int* err,
+                                                                 uint32_t hold, uint32_t polls) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full[kF32Stages], empty[kF32Stages];
+  __shared__ volatile int abort_flag;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint8_t* base = smem_raw + (((smem_u32(smem_raw) + 1023u) & ~1023u) - smem_u32(smem_raw));
+  const uint32_t ntiles = (rows + kF32Rows - 1) / kF32Rows;
+  const uint32_t nst = (S + kF32Cols - 1) / kF32Cols;
+  if (tid == 0) {
+    for (int i = 0; i < kF32Stages; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], 4); }
+    abort_flag = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  if (warp == 4) {  // producer
+    if (lane == 0 && !hold) {  // hold (a test hook): no copy is issued, the consumers' waits give up
+      uint32_t seq = 0;
+      for (uint32_t tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x)
+        for (uint32_t c = 0; c < nst; ++c, ++seq) {
+          const uint32_t st = seq % kF32Stages;
+          if (!mbar_wait_bounded(&empty[st], ((seq / kF32Stages) & 1u) ^ 1u, err, polls)) { abort_flag = 1; break; }
+          const uint32_t nt = min(uint32_t(kF32Cols), S - c * kF32Cols);
+          uint8_t* sb = base + size_t(st) * kF32StageBytes;
+          mbar_arrive_expect_tx(&full[st], kF32TileBytes + nt * 64);
+          tma_load_2d(sb, &tm, int(c * kF32Cols), int(tile * kF32Rows), &full[st]);
+          bulk_g2s(sb + kF32TileBytes, basis16 + size_t(c) * kF32Cols * 16, nt * 64, &full[st]);
+        }
+      // copies still in flight land before the CTA may exit
+      const uint32_t first = seq > uint32_t(kF32Stages) ? seq - kF32Stages : 0;
+      for (uint32_t q = first; q < seq; ++q)
+        mbar_wait_bounded(&full[q % kF32Stages], (q / kF32Stages) & 1u, err, 1u << 16);
+    }
+    return;
+  }
+
+  constexpr int NQ = (K + 3) / 4;  // basis float4 per sample
+  uint32_t seq = 0;
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    float acc[2][K];  // rows t and t + 128 of the tile
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[h][k] = 0.f;
+    for (uint32_t c = 0; c < nst; ++c, ++seq) {
+      const uint32_t st = seq % kF32Stages;
+      if (!mbar_wait_bounded(&full[st], (seq / kF32Stages) & 1u, err, polls)) abort_flag = 1;
+      if (abort_flag) break;
+      const uint8_t* sb = base + size_t(st) * kF32StageBytes;
+      const float4* bas = reinterpret_cast<const float4*>(sb + kF32TileBytes);  // [32][16] floats
+      // the last stage of a row may be partial: its basis rows past nt were not copied
+      const uint32_t nt = min(uint32_t(kF32Cols), S - c * kF32Cols);
+#pragma unroll
+      for (int q = 0; q < kF32Cols / 4; ++q) {
+        // rows t and t + 128: the same swizzle phase (t & 7)
+        const uint32_t off = ((q ^ (tid & 7)) << 4);
+        const float4 v0 = *reinterpret_cast<const float4*>(sb + tid * 128 + off);
+        const float4 v1 = *reinterpret_cast<const float4*>(sb + (tid + 128) * 128 + off);
+        const float r4[2][4] = {{v0.x, v0.y, v0.z, v0.w}, {v1.x, v1.y, v1.z, v1.w}};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (uint32_t(4 * q + e) >= nt) break;
+          const float4* b4 = bas + (4 * q + e) * 4;
+#pragma unroll
+          for (int g = 0; g < NQ; ++g) {
+            const float4 b = b4[g];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              if (4 * g + 0 < K) acc[h][4 * g + 0] = fmaf(r4[h][e], b.x, acc[h][4 * g + 0]);
+              if (4 * g + 1 < K) acc[h][4 * g + 1] = fmaf(r4[h][e], b.y, acc[h][4 * g + 1]);
+              if (4 * g + 2 < K) acc[h][4 * g + 2] = fmaf(r4[h][e], b.z, acc[h][4 * g + 2]);
+              if (4 * g + 3 < K) acc[h][4 * g + 3] = fmaf(r4[h][e], b.w, acc[h][4 * g + 3]);
+            }
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
+    }
+    if (abort_flag) break;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint32_t row = tile * kF32Rows + tid + 128 * h;
+      if (row < rows) {
+        const uint32_t p = row / 3, ch = row - 3 * p;
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[(size_t(p) * K + k) * 3 + ch] = acc[h][k];
+      }
+    }
+  }
+}
+
+bool make_map_f32(CUtensorMap* m, const void* ptr, uint64_t S, uint64_t rows) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {S, rows};
+  const cuuint64_t strides[1] = {S * 4};
+  const cuuint32_t box[2] = {uint32_t(kF32Cols), uint32_t(kF32Rows)};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 bool project_tc_supported(const void* radiance, uint32_t S) {
@@ -263,6 +393,37 @@ int launch_project_tc(const uint16_t* radiance, uint32_t nprobes, uint32_t S, co
   const uint32_t grid = std::min<uint32_t>(ntiles, uint32_t(num_sms));
   k_project_tc<<<grid, kTcThreads, kSmemBytes, s>>>(ta, tb, rows, S, K, out, err, hold,
                                                      wait_polls ? wait_polls : kWaitPolls);
+  return 1;
+}
+
+}  // namespace vlbk
+
+namespace vlbk {
+
+int launch_project_f32_tma(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
+                           float* out, int* err, int num_sms, cudaStream_t s, uint32_t hold, uint32_t wait_polls) {
+  const uint32_t rows = nprobes * 3;
+  if (rows == 0 || S == 0 || S % 4 || (reinterpret_cast<uintptr_t>(radiance) % 16) ||
+      (reinterpret_cast<uintptr_t>(basis16) % 16))
+    return 0;
+  CUtensorMap tm;
+  if (!make_map_f32(&tm, radiance, S, rows)) return 0;
+  static std::atomic<uint64_t> opted9{0}, opted16{0};
+  const uint32_t ntiles = (rows + kF32Rows - 1) / kF32Rows;
+  const uint32_t polls = wait_polls ? wait_polls : kWaitPolls;
+  if (K == 9) {
+    smem_opt_in(k_project_f32_tma<9>, int(kF32SmemBytes), opted9);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project_f32_tma<9>, kF32Threads, kF32SmemBytes);
+    const uint32_t grid = std::min<uint32_t>(ntiles, uint32_t(num_sms) * uint32_t(std::max(per_sm, 1)));
+    k_project_f32_tma<9><<<grid, kF32Threads, kF32SmemBytes, s>>>(tm, basis16, rows, S, out, err, hold, polls);
+  } else {
+    smem_opt_in(k_project_f32_tma<16>, int(kF32SmemBytes), opted16);
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_project_f32_tma<16>, kF32Threads, kF32SmemBytes);
+    const uint32_t grid = std::min<uint32_t>(ntiles, uint32_t(num_sms) * uint32_t(std::max(per_sm, 1)));
+    k_project_f32_tma<16><<<grid, kF32Threads, kF32SmemBytes, s>>>(tm, basis16, rows, S, out, err, hold, polls);
+  }
   return 1;
 }
 

@@ -1007,7 +1007,8 @@ static vlb_status project_f32(vlb_ctx* ctx, const float* rad, uint32_t nprobes, 
     if (st) return st;
   }
   KScope k(ctx, "project_f32", pb ? 2 : 1);
-  vlbk::launch_project_f32(rad, nprobes, dirs->n, dirs->d_basis16, K, out, static_cast<float*>(part), ctx->stream);
+  vlbk::launch_project_f32(rad, nprobes, dirs->n, dirs->d_basis16, K, out, static_cast<float*>(part), ctx->stream,
+                           ctx->d_err, ctx->num_sms, ctx->hold_producer, ctx->wait_polls);
   return VLB_OK;
 }
 

@@ -97,7 +97,12 @@ void launch_sh_finalize(const float* partial, uint32_t nmaps, uint32_t slabs, ui
 // that is 0: the tile is projected unsplit).
 size_t project_partial_bytes(uint32_t nprobes, uint32_t S, uint32_t K);
 void launch_project_f32(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
-                        float* out, float* partial, cudaStream_t s);
+                        float* out, float* partial, cudaStream_t s, int* err = nullptr, int num_sms = 0,
+                        uint32_t hold = 0, uint32_t wait_polls = 0);
+// The TMA-staged form of the unsplit FP32 projection (same bits); returns 0
+// when the tile does not qualify (S % 4, alignment) and nothing was launched.
+int launch_project_f32_tma(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
+                           float* out, int* err, int num_sms, cudaStream_t s, uint32_t hold, uint32_t wait_polls);
 // split: the tile is [rows][2S] hi/lo BF16 pairs (the sample is hi + lo).
 void launch_project_bf16_simt(const uint16_t* radiance, uint32_t nprobes, uint32_t S, const float* basis16,
                               uint32_t K, float* out, float* partial, uint32_t split, cudaStream_t s);
