@@ -749,9 +749,10 @@ def refbake_measure(ctx, torch, stream, steps, hbm_peak, reps=3):
 
 def batch_measure(ctx, torch, stream, steps, hbm_peak):
     """Config 3: 256 uneven bake jobs in one batch, replayed as a CUDA graph,
-    L2 SH.  Chosen: VLB_PREC_FUSED (one persistent fused launch over every
-    job's work items, no tile); beside it the mixed path (BF16 hi/lo tile, one
-    tcgen05 projection per direction set) and the plain FP32 tile path.
+    L2 SH.  Chosen: the default FP32 tile path (one persistent lane-walk
+    launch over every job's rays, one projection per direction set); beside
+    it the one-kernel path (VLB_PREC_FUSED, no tile) and the mixed path (BF16
+    hi/lo tile, one tcgen05 projection per direction set).
     Inputs and outputs resident in HBM; `e2e` passes pinned host probes and
     outputs.  Accuracy: a sample of jobs against the FP64 oracle with the
     device's decisions replayed."""
@@ -846,9 +847,9 @@ def batch_measure(ctx, torch, stream, steps, hbm_peak):
         r["rel_err_vs_fp64"] = {"max": float(e.max()), "mean": float(e.mean()), "probes": int(e.size),
                                 "note": "6 jobs spread over the batch, decisions replayed"}
         res[name] = r
-    res["chosen_vs_plain"] = res["fused"]["probes_per_s"] / res["plain_fp32"]["probes_per_s"]
+    res["fused_vs_plain_fp32"] = res["fused"]["probes_per_s"] / res["plain_fp32"]["probes_per_s"]
     # the chosen jobs as 256 separate vlb_bake calls (device buffers, no sync between)
-    jobs, plist = jobs_for(vlb.PREC_FUSED)
+    jobs, plist = jobs_for(vlb.PREC_FP32)
 
     def singles():
         for sc, pr, o, p in jobs:
@@ -864,7 +865,7 @@ def batch_measure(ctx, torch, stream, steps, hbm_peak):
     torch.cuda.synchronize()
     single_ms = a.elapsed_time(b)
     res["separate_bakes"] = {"ms": single_ms, "probes_per_s": P / (single_ms / 1e3),
-                             "note": "the same 256 jobs as separate fused vlb_bake calls"}
+                             "note": "the same 256 jobs as separate vlb_bake calls (FP32 tile path)"}
     # e2e: pinned host probes in, host SH out, through the public call
     hjobs = [(sc, torch.from_numpy(v[3]).pin_memory(), torch.empty((v[3].shape[0], K, 3)).pin_memory(), p)
              for sc, v, p in zip(scenes, vols, plist)]
@@ -954,8 +955,9 @@ def service_run(ctx, svc, scenes, dsets, sky, reqs, lmax, prec):
 def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
     """Config 4: the bake service over 8 resident box scenes (64 ... 170,000
     boxes, 778 ... 2,040,010 triangles), Poisson arrivals swept over rates
-    relative to the measured capacity of the fused service, 20% relights,
-    64 GiB budget; the mixed and plain FP32 services at 0.6 x capacity."""
+    relative to the measured capacity of the default (FP32 tile) service, 20%
+    relights, 64 GiB budget; the one-kernel and mixed services at 0.6 x
+    capacity."""
     import vlb
 
     t0 = time.perf_counter()
@@ -987,8 +989,8 @@ def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
                 "relights_rebaked": st["relights_rebaked"], "evictions": st["evictions"],
                 "bytes_peak": st["bytes_peak"], "wall_s": wall}
 
-    # capacity of the chosen (fused) service: every request at t = 0 (closed burst)
-    cap = run(vlb.PREC_FUSED, 1e9, nreq // 2, SEED + 7)
+    # capacity of the default (FP32) service: every request at t = 0 (closed burst)
+    cap = run(vlb.PREC_FP32, 1e9, nreq // 2, SEED + 7)
     capacity = cap["requests"] / cap["wall_s"]
     out["capacity_req_per_s"] = capacity
     out["burst"] = cap
@@ -998,19 +1000,21 @@ def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
         return int(min(nreq, max(20, rate * 5.0)))
 
     out["slice_probes"] = 2048
-    out["fused"] = [run(vlb.PREC_FUSED, f * capacity, nfor(f * capacity), SEED + 11 + k)
-                    for k, f in enumerate((0.3, 0.6, 0.9))]
+    out["fp32"] = [run(vlb.PREC_FP32, f * capacity, nfor(f * capacity), SEED + 11 + k)
+                   for k, f in enumerate((0.3, 0.6, 0.9))]
     # the same 0.3 x stream without slicing (whole requests per batch)
-    out["fused_unsliced"] = [run(vlb.PREC_FUSED, 0.3 * capacity, nfor(0.3 * capacity), SEED + 11, 0xFFFFFFFF)]
+    out["fp32_unsliced"] = [run(vlb.PREC_FP32, 0.3 * capacity, nfor(0.3 * capacity), SEED + 11, 0xFFFFFFFF)]
+    out["fused"] = [run(vlb.PREC_FUSED, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
+    out["mixed_bf16_hilo"] = [run(vlb.PREC_MIXED, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
     # the floor under p99: the largest request the stream can hold (16,384
     # probes x 1,024 rays in the densest scene) alone in an idle service
     big = service_requests(1, 1.0, SEED + 5, bounds)[0]
     lo, hi = bounds[-1]
     probes = (lo + np.random.default_rng(SEED + 5).random((16384, 3)) * (hi - lo)).astype(np.float32)
-    svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=vlb.PREC_FUSED)
+    svc = vlb.Service(ctx, budget_bytes=64 << 30, lmax=LMAX, precision=vlb.PREC_FP32)
     alone = []
     for r in range(4):
-        p = vlb.bake_params(dsets[1024], LMAX, vlb.PREC_FUSED, vlb.synth_sun(big["sun_seed"] + r), sky=sky)
+        p = vlb.bake_params(dsets[1024], LMAX, vlb.PREC_FP32, vlb.synth_sun(big["sun_seed"] + r), sky=sky)
         alone.append(svc.wait(svc.submit(scenes[-1], probes, p))[1])
     svc.close()
     out["largest_request_alone_ms"] = float(np.median(alone[1:]))
