@@ -1018,8 +1018,6 @@ def service_measure(ctx, torch, stream, steps, hbm_peak, nreq=160):
         alone.append(svc.wait(svc.submit(scenes[-1], probes, p))[1])
     svc.close()
     out["largest_request_alone_ms"] = float(np.median(alone[1:]))
-    out["mixed_bf16_hilo"] = [run(vlb.PREC_MIXED, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
-    out["fp32"] = [run(vlb.PREC_FP32, 0.6 * capacity, nfor(0.6 * capacity), SEED + 12)]
     return out
 
 
