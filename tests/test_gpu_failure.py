@@ -105,9 +105,10 @@ def test_tensor_core_projection_wait_runs_out(ctx):
 
 
 def test_fp32_projection_wait_runs_out(ctx):
-    """The TMA-staged FP32 projection (the default bake's): its consumer warps
-    give up when the producer is held."""
-    n, S = 300, 1024
+    """The TMA-staged FP32 projection (the default bake's, for tiles of at
+    least one 256-row tile per SM): its consumer warps give up when the
+    producer is held."""
+    n, S = 16384, 1024
     ds = ctx.fibonacci(S)
     rad = np.random.default_rng(11).random((n, 3, S)).astype(np.float32)
     good = ctx.project(rad, n, ds, 2)

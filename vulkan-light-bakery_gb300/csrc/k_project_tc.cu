@@ -403,8 +403,10 @@ namespace vlbk {
 int launch_project_f32_tma(const float* radiance, uint32_t nprobes, uint32_t S, const float* basis16, uint32_t K,
                            float* out, int* err, int num_sms, cudaStream_t s, uint32_t hold, uint32_t wait_polls) {
   const uint32_t rows = nprobes * 3;
+  // small tiles (fewer 256-row tiles than SMs) stay with the cp.async kernel's
+  // 128-row CTAs, which spread them over more SMs
   if (rows == 0 || S == 0 || S % 4 || (reinterpret_cast<uintptr_t>(radiance) % 16) ||
-      (reinterpret_cast<uintptr_t>(basis16) % 16))
+      (reinterpret_cast<uintptr_t>(basis16) % 16) || (rows + kF32Rows - 1) / kF32Rows < uint32_t(num_sms))
     return 0;
   CUtensorMap tm;
   if (!make_map_f32(&tm, radiance, S, rows)) return 0;

@@ -254,8 +254,7 @@ __global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs 
   for (;;) {
     const unsigned idle = __ballot_sync(kFull, !L.has);
     if (!exhausted && idle == kFull) {  // a whole idle warp takes its next 32 rays together
-      const uint32_t groups_per_warp = (R / 32) / (gridDim.x * kTraceWarps);
-      const uint32_t block = 32u * min(16u, max(1u, groups_per_warp / 64));
+      const uint32_t block = a.ray_block;  // set by the launch: the kernel's registers stay free
       uint32_t wb;
       if (block == 32) {  // one group a block: straight from the counter
         uint32_t base = 0;
@@ -322,11 +321,16 @@ static void launch_dyn(const TraceArgs& a, int num_sms, cudaStream_t s) {
     if (per_sm < 1) per_sm = 1;
   }
   const uint64_t rays = uint64_t((a.nprobes + 31) / 32 * 32) * a.S;
-  const uint64_t ctas = std::min<uint64_t>((rays + kTraceThreads - 1) / kTraceThreads, uint64_t(num_sms) * per_sm);
-  kern<<<uint32_t(std::max<uint64_t>(ctas, 1)), kTraceThreads, 0, s>>>(a);
+  const uint64_t ctas = std::max<uint64_t>(
+      std::min<uint64_t>((rays + kTraceThreads - 1) / kTraceThreads, uint64_t(num_sms) * per_sm), 1);
+  // ray blocks: whole 32-ray groups, as many as keep ~64 blocks a warp, at most 16
+  TraceArgs b = a;
+  const uint64_t groups_per_warp = (rays / 32) / (ctas * kTraceWarps);
+  b.ray_block = 32u * uint32_t(std::min<uint64_t>(16, std::max<uint64_t>(1, groups_per_warp / 64)));
+  kern<<<uint32_t(ctas), kTraceThreads, 0, s>>>(b);
 }
 
-// The ray counter runs past R by at most 32 per resident warp: R < 2^31 keeps it in 32 bits.
+// The ray counter runs past R by at most one ray block (512) per resident warp: R < 2^31 keeps it in 32 bits.
 bool trace_dyn_supported(const TraceArgs& a) {
   return a.lane && a.ntris > 0 && a.ntris < 0x7fffffffu &&
          uint64_t((a.nprobes + 31) / 32 * 32) * a.S < (1ull << 31);

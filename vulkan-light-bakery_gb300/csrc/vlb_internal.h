@@ -200,6 +200,7 @@ struct TraceArgs {
   uint32_t dirs_per_warp;
   uint32_t chunks;        // direction chunks per packet
   uint32_t lane;          // 1: per-lane traversal, 0: packet traversal
+  uint32_t ray_block;     // tile lane walk: rays a warp takes from the counter at once (set by its launch)
   unsigned long long* counters;  // null, or [warp node fetches, warp triangle fetches, shadow rays, lane node tests]
   int* err;
   // grid mode (null grid_hdr: tree walks): grid g < S for direction g, grid S for the sun
