@@ -57,8 +57,8 @@ METRIC_FULL = "probes/s, Grays/s, p99 bake latency of the default path, <=1e-4 S
 # per launch of the headline workload, ncu's L1 and issue utilisation.
 TRACE_NCU = {
     "trace_tile": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
-                   "dram_bytes": 3172000000, "warp_instructions": 143587000000,
-                   "l1tex_throughput_pct": 85.9, "issue_active_pct": 79.3},
+                   "dram_bytes": 3503000000, "warp_instructions": 135526000000,
+                   "l1tex_throughput_pct": 76.5, "issue_active_pct": 78.1},
     "trace_fused_lane": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
                          "dram_bytes": 266100000, "warp_instructions": 144591000000,
                          "l1tex_throughput_pct": 82.8, "issue_active_pct": 70.0},

@@ -79,26 +79,6 @@ __device__ void cube_texel_basis64(uint32_t t, uint32_t n, double* b) {
   for (int k = 0; k < 16; ++k) b[k] = w * c[k];
 }
 
-// Weighted basis per cubemap texel, FP64 throughout, rounded once to FP32:
-// NQ float4 per texel (the form of k_skybox_sh's streamed table).
-__global__ void k_cube_basis_table(float4* out, uint32_t n, uint32_t lmax) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 6 * n * n) return;
-  double b[16];
-  cube_texel_basis64(t, n, b);
-  const uint32_t K = (lmax + 1) * (lmax + 1), NQ = (K + 3) / 4;
-  for (uint32_t q = 0; q < NQ; ++q) {
-    float f[4];
-    for (int e = 0; e < 4; ++e) f[e] = (4 * q + e < K) ? float(b[4 * q + e]) : 0.f;
-    out[size_t(t) * NQ + q] = make_float4(f[0], f[1], f[2], f[3]);
-  }
-}
-
-void launch_cube_basis_table(float4* out, uint32_t n, uint32_t lmax, cudaStream_t s) {
-  const uint32_t total = 6 * n * n;
-  k_cube_basis_table<<<(total + 255) / 256, 256, 0, s>>>(out, n, lmax);
-}
-
 void skybox_plan(SkyboxArgs& a, uint32_t max_slabs) {
   uint32_t slab = a.pair_table ? kGroupSlab : kSkySlab;
   if (max_slabs && (a.texels_per_map + slab - 1) / slab > max_slabs)
@@ -146,16 +126,14 @@ __device__ __forceinline__ void texel_rgb(const unsigned char* p, uint32_t i, bo
 // warp reduces its own sums with shuffles and writes one partial per (map,
 // slab, warp), so no CTA-wide barrier follows the set-up -- a consumer whose
 // bounded wait gives up simply stops, and nobody is left waiting for it.
-template <int LMAX, int LAYOUT, int FMT, int G, bool TMA, bool BT>
+template <int LMAX, int LAYOUT, int FMT, int G, bool TMA>
 __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
   constexpr int K = sh_k<LMAX>();
   constexpr int V = 3 * K;
   constexpr int GP = (G + 1) / 2;  // map pairs
   constexpr int TB = FMT == 0 ? 12 : 4;
   constexpr uint32_t kMapChunkBytes = kSkyChunk * TB;
-  constexpr int NQ = (K + 3) / 4;  // float4 per basis-table row
-  constexpr uint32_t kTabBytes = BT ? kSkyChunk * NQ * 16 : 0;
-  constexpr uint32_t kStageBytes = G * kMapChunkBytes + kTabBytes;  // G map chunks, then the table chunk
+  constexpr uint32_t kStageBytes = G * kMapChunkBytes;  // G map chunks
   constexpr uint32_t kConsumerWarps = kSkyConsumers / 32;
   extern __shared__ __align__(128) unsigned char stage_mem[];
   __shared__ __align__(8) uint64_t full[kSkyStages], empty[kSkyStages];
@@ -205,11 +183,9 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
         uint32_t tb, nt, m0, gv;
         chunk_span(it, &tb, &nt, &m0, &gv);
         unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;
-        mbar_arrive_expect_tx(&full[st], gv * nt * TB + (BT ? nt * NQ * 16 : 0));
+        mbar_arrive_expect_tx(&full[st], gv * nt * TB);
         for (uint32_t g = 0; g < gv; ++g)
           bulk_g2s(sbase + g * kMapChunkBytes, tex + (size_t(m0 + g) * T + tb) * TB, nt * TB, &full[st]);
-        if constexpr (BT)
-          bulk_g2s(sbase + G * kMapChunkBytes, a.basis_table + size_t(tb) * NQ, nt * NQ * 16, &full[st]);
         advance(it);
       }
       // every copy issued lands before the CTA may exit
@@ -241,18 +217,14 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
     }
     if (abort_flag) break;
     const unsigned char* sbase = stage_mem + size_t(st) * kStageBytes;
-    // per-chunk pointers: the group's texel chunks and the basis-table chunk
+    // per-chunk pointers: the group's texel chunks
     const unsigned char* mp[G];
 #pragma unroll
     for (int g = 0; g < G; ++g)
       mp[g] = TMA ? sbase + g * kMapChunkBytes : tex + (size_t(m0 + min(uint32_t(g), gv - 1)) * T + tb) * TB;
-    const float4* tab = BT ? (TMA ? reinterpret_cast<const float4*>(sbase + G * kMapChunkBytes)
-                                  : a.basis_table + size_t(tb) * NQ)
-                           : nullptr;
     // chunk origin: one division per chunk, the texels then step from it
     uint32_t face0 = 0, rem0 = 0, y0 = 0, x0 = 0;
-    if constexpr (BT) {
-    } else if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
+    if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
       face0 = udiv(tb, nn, inv_nn);
       rem0 = tb - face0 * nn;
     } else {
@@ -262,17 +234,7 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
 #pragma unroll 1
     for (uint32_t i = tid; i < nt; i += kSkyConsumers) {
       float Y[K];
-      if constexpr (BT) {
-        // cached weighted basis of this texel position (shared by every map)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          const float4 b = tab[size_t(i) * NQ + q];  // shared memory (TMA) or global: a generic load
-          const float bb[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (4 * q + e < K) Y[4 * q + e] = bb[e];
-        }
-      } else {
+      {
         float bx, by, bz, w;
         if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
           const uint32_t n = a.w;
@@ -352,8 +314,8 @@ __global__ void __launch_bounds__(kSkyThreads) k_skybox_sh(const SkyboxArgs a) {
 // MPW*w .. MPW*w + MPW - 1 of the group, and every warp reads the same
 // per-texel weighted basis, so one basis row serves 8 * MPW maps (the
 // basis stream is 9-16 floats a texel against 12 bytes a texel of every
-// map).  The basis comes from a table in FP64 rounded once (the form of
-// k_cube_basis_table), laid out per 256-texel chunk for texel pairs: lane l
+// map).  The basis comes from a table in FP64 rounded once
+// (cube_texel_basis64), laid out per 256-texel chunk for texel pairs: lane l
 // of a warp takes texels 64b + l and 64b + 32 + l (b = 0..3) -- stride-3
 // words across the lanes, so the texel reads are free of bank conflicts --
 // and entry [chunk][k][32b + l] holds the pair's two weighted basis values
@@ -543,14 +505,13 @@ static void launch_group(const SkyboxArgs& a, int num_sms, cudaStream_t s) {
   k<<<int(units < cap ? units : cap), kSkyThreads, smem, s>>>(a);
 }
 
-template <int LMAX, int LAYOUT, int FMT, int G, bool BT>
+template <int LMAX, int LAYOUT, int FMT, int G>
 static void launch4(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
   const int TB = FMT == 0 ? 12 : 4;
-  const size_t tab = BT ? size_t(kSkyChunk) * ((sh_k<LMAX>() + 3) / 4) * 16 : 0;
-  const size_t smem = tma ? size_t(kSkyStages) * (G * kSkyChunk * TB + tab) : 0;
+  const size_t smem = tma ? size_t(kSkyStages) * (G * kSkyChunk * TB) : 0;
   const uint32_t groups = (a.count + G - 1) / G;
   const uint64_t units = uint64_t(groups) * a.slabs_per_map;
-  auto k = tma ? k_skybox_sh<LMAX, LAYOUT, FMT, G, true, BT> : k_skybox_sh<LMAX, LAYOUT, FMT, G, false, BT>;
+  auto k = tma ? k_skybox_sh<LMAX, LAYOUT, FMT, G, true> : k_skybox_sh<LMAX, LAYOUT, FMT, G, false>;
   if (smem) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kSkyThreads, smem);
@@ -560,19 +521,11 @@ static void launch4(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) 
   k<<<grid, kSkyThreads, smem, s>>>(a);
 }
 
-template <int LMAX, int LAYOUT, int FMT, int G>
-static void launch4b(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
-  if constexpr (LAYOUT == VLB_SKY_CUBEMAP) {
-    if (a.basis_table) { launch4<LMAX, LAYOUT, FMT, G, true>(a, tma, num_sms, s); return; }
-  }
-  launch4<LMAX, LAYOUT, FMT, G, false>(a, tma, num_sms, s);
-}
-
 template <int LMAX, int LAYOUT, int FMT>
 static void launch3(const SkyboxArgs& a, bool tma, int num_sms, cudaStream_t s) {
-  if (a.group == 1) launch4b<LMAX, LAYOUT, FMT, 1>(a, tma, num_sms, s);
-  else if (LMAX == 2 && a.group == 4) launch4b<LMAX, LAYOUT, FMT, 4>(a, tma, num_sms, s);
-  else launch4b<LMAX, LAYOUT, FMT, 2>(a, tma, num_sms, s);
+  if (a.group == 1) launch4<LMAX, LAYOUT, FMT, 1>(a, tma, num_sms, s);
+  else if (LMAX == 2 && a.group == 4) launch4<LMAX, LAYOUT, FMT, 4>(a, tma, num_sms, s);
+  else launch4<LMAX, LAYOUT, FMT, 2>(a, tma, num_sms, s);
 }
 
 template <int LMAX, int LAYOUT>

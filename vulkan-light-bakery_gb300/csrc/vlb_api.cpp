@@ -446,7 +446,6 @@ void vlb_ctx_destroy(vlb_ctx* ctx) {
   if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
   for (auto& kv : ctx->scratch) cudaFree(kv.second.p);
   for (auto& kv : ctx->cube_sa) cudaFree(kv.second);
-  for (auto& kv : ctx->cube_bt) cudaFree(kv.second);
   for (auto& kv : ctx->cube_pt) cudaFree(kv.second);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -781,22 +780,6 @@ vlb_status vlb_dirset_export(const vlb_dirset* d, float* trace_dirs, float* basi
 }
 
 // ---- skybox SH ---------------------------------------------------------------------------
-static vlb_status cube_basis_table(vlb_ctx* ctx, uint32_t n, uint32_t lmax, const float4** out) {
-  const uint64_t key = (uint64_t(n) << 8) | lmax;
-  auto it = ctx->cube_bt.find(key);
-  if (it != ctx->cube_bt.end()) { *out = it->second; return VLB_OK; }
-  const size_t nq = (k_of(lmax) + 3) / 4;
-  float4* p = nullptr;
-  VLB_CUDA(ctx, cudaMalloc(&p, size_t(6) * n * n * nq * sizeof(float4)));
-  {
-    KScope k(ctx, "cube_basis_table");
-    vlbk::launch_cube_basis_table(p, n, lmax, ctx->stream);
-  }
-  ctx->cube_bt[key] = p;
-  *out = p;
-  return VLB_OK;
-}
-
 static vlb_status cube_pair_table(vlb_ctx* ctx, uint32_t n, uint32_t lmax, const float2** out) {
   const uint64_t key = (uint64_t(n) << 8) | lmax;
   auto it = ctx->cube_pt.find(key);

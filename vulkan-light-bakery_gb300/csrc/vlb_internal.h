@@ -61,7 +61,6 @@ struct SkyboxArgs {
   uint32_t slabs_per_map;
   uint32_t group;         // maps per work unit (1, 2 or 4)
   const float* solid_angle;  // cubemap: w*w table (same for every face)
-  const float4* basis_table; // cubemap, optional: per texel w * Y_k, (lmax+1)^2 padded to a multiple of 4
   const float2* pair_table;  // cubemap, optional: launch_cube_pair_table's layout (selects the group kernel)
   const float2* col_tab;     // panorama: w entries (cos phi, sin phi)
   const float4* row_tab;     // panorama: h entries (sin theta, cos theta, weight, 0)
@@ -74,10 +73,6 @@ struct SkyboxArgs {
 // partial[map][slab][warp][v], kSkyPartialsPerSlab warps.
 constexpr int kSkyPartialsPerSlab = 8;
 void launch_cube_solid_angle(float* out, uint32_t n, cudaStream_t s);
-// Per-texel weighted basis of a 6 x n x n cubemap, computed in FP64 (exact
-// solid angle, normalised direction, basis) and stored in FP32: 3 float4 per
-// texel for lmax 2, 4 for lmax 3.
-void launch_cube_basis_table(float4* out, uint32_t n, uint32_t lmax, cudaStream_t s);
 // Weighted basis of texel pairs per 256-texel chunk, [chunk][k][128] float2
 // (FP64, rounded once), for the group kernel of cubemap batches.
 size_t cube_pair_table_bytes(uint32_t n, uint32_t lmax);
@@ -404,7 +399,6 @@ struct vlb_ctx {
   struct Buf { void* p = nullptr; size_t bytes = 0; };
   std::map<std::string, Buf> scratch;
   std::map<uint32_t, float*> cube_sa;  // solid-angle tables by face size
-  std::map<uint64_t, float4*> cube_bt;  // weighted-basis tables by (face size << 8 | lmax)
   std::map<uint64_t, float2*> cube_pt;  // texel-pair basis tables by (face size << 8 | lmax)
   // batched bakes: the shape key of the last batch, its captured graph (made
   // on the second call with that key) and the tuned schedule
