@@ -228,7 +228,8 @@ void vlb_sky_destroy(vlb_sky* sky);
  * (light_baker.cpp:294-322), each probe's own sum (the reference never clears
  * its accumulator between probes; that carry-over is not reproduced). */
 typedef enum vlb_precision {
-  VLB_PREC_FP32 = 0,  /* plain path: FP32 radiance tile, FP32 CUDA-core projection (the drop-in) */
+  VLB_PREC_FP32 = 0,  /* the default: FP32 radiance tile, FP32 projection (staged by TMA for large
+                         tiles); the fastest path measured on the box scenes, within 1e-4 of FP64 */
   VLB_PREC_FUSED = 1, /* FP32, one kernel: each warp projects the rays it traced (FP32 sums in a
                          fixed order, FP64 chunk sums); no radiance tile */
   VLB_PREC_MIXED = 2, /* radiance stored as BF16 hi/lo pairs (4 bytes a sample), projected on the
