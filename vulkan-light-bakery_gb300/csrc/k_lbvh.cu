@@ -533,10 +533,7 @@ __global__ void k_pack_nodes(const int32_t* __restrict__ child, const float* __r
     b0[a] = widen_lo(p0[a], scale); b0[3 + a] = widen_hi(p0[3 + a], scale);
     b1[a] = widen_lo(p1[a], scale); b1[3 + a] = widen_hi(p1[3 + a], scale);
   }
-  nodes[4 * size_t(i) + 0] = make_float4(b0[0], b0[1], b0[2], b0[3]);
-  nodes[4 * size_t(i) + 1] = make_float4(b0[4], b0[5], b1[0], b1[1]);
-  nodes[4 * size_t(i) + 2] = make_float4(b1[2], b1[3], b1[4], b1[5]);
-  nodes[4 * size_t(i) + 3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
+  pack_node(nodes + 4 * size_t(i), b0, b1, c0, c1);
 }
 
 __global__ void k_pack_tris(const uint32_t* __restrict__ order, const float* __restrict__ pos, uint32_t stride,

@@ -187,10 +187,7 @@ __global__ void k_ploc_pack(const int32_t* __restrict__ child, const float* __re
     b0[a] = wlo(p0[a], scale); b0[3 + a] = whi(p0[3 + a], scale);
     b1[a] = wlo(p1[a], scale); b1[3 + a] = whi(p1[3 + a], scale);
   }
-  nodes[4 * size_t(id) + 0] = make_float4(b0[0], b0[1], b0[2], b0[3]);
-  nodes[4 * size_t(id) + 1] = make_float4(b0[4], b0[5], b1[0], b1[1]);
-  nodes[4 * size_t(id) + 2] = make_float4(b1[2], b1[3], b1[4], b1[5]);
-  nodes[4 * size_t(id) + 3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
+  pack_node(nodes + 4 * size_t(id), b0, b1, c0, c1);
 }
 
 namespace {

@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
         lr_park(L, stack);
         const bool at_node = L.has && L.cur >= 0;
         if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
-        if (at_node) lr_node<false>(J, L, stack, w);
+        if (at_node) lr_node<false, BakeJobDev, false, !MULTI>(J, L, stack, w);
       }
       lr_park(L, stack);
       if (L.has) {

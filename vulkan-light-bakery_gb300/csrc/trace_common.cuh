@@ -17,10 +17,12 @@ namespace vlbk {
 constexpr int kTraceThreads = kTraceWarps * 32;
 constexpr unsigned kFull = 0xffffffffu;
 
+// The box-test terms as pairs for packed FMAs: a plane p of axis a is crossed
+// at t = p * inv_a - o_a * inv_a, i.e. fma(p, inv_a, -(o_a * inv_a)).
 struct RayCtx {
   float ox, oy, oz, dx, dy, dz;
-  float ix, iy, iz;     // 1 / d (zero components nudged to 1e-30)
-  float oix, oiy, oiz;  // o * inv
+  float2 ixy, izz;  // (1/dx, 1/dy), (1/dz, 1/dz) (zero components nudged to 1e-30)
+  float2 nxy, nzz;  // -(o * inv) for the same components
 };
 
 struct Work {
@@ -42,20 +44,32 @@ __device__ __forceinline__ float safe_inv(float d) {
   return 1.0f / (fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
 }
 
-__device__ __forceinline__ void make_ray(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz) {
-  r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
-  r.ix = safe_inv(dx); r.iy = safe_inv(dy); r.iz = safe_inv(dz);
-  r.oix = ox * r.ix; r.oiy = oy * r.iy; r.oiz = oz * r.iz;
-}
-
-// make_ray with the reciprocals of d precomputed (host_safe_inv: the same bits).
 __device__ __forceinline__ void make_ray_inv(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz,
                                              float ix, float iy, float iz) {
   r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz;
-  r.ix = ix; r.iy = iy; r.iz = iz;
-  r.oix = ox * ix; r.oiy = oy * iy; r.oiz = oz * iz;
+  const float nz = -(oz * iz);
+  r.ixy = make_float2(ix, iy);
+  r.izz = make_float2(iz, iz);
+  r.nxy = make_float2(-(ox * ix), -(oy * iy));
+  r.nzz = make_float2(nz, nz);
 }
 
+__device__ __forceinline__ void make_ray(RayCtx& r, float ox, float oy, float oz, float dx, float dy, float dz) {
+  make_ray_inv(r, ox, oy, oz, dx, dy, dz, safe_inv(dx), safe_inv(dy), safe_inv(dz));
+}
+
+// (a.x * b.x + c.x, a.y * b.y + c.y), each one fma.rn.f32 (one packed instruction).
+__device__ __forceinline__ float2 fma_pair(float ax, float ay, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 a, b, c, d;\n\t"
+      "mov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tmov.b64 c, {%6, %7};\n\t"
+      "fma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(ax), "f"(ay), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// make_ray with the reciprocals of d precomputed (host_safe_inv: the same bits).
 // Slab test for a ray in octant OCT (bit a set: 1/d_a < 0).  The octant is
 // the same for every lane of a packet (one direction per packet), so the
 // entry and exit planes of each axis are chosen at compile time and no
@@ -63,9 +77,10 @@ __device__ __forceinline__ void make_ray_inv(RayCtx& r, float ox, float oy, floa
 template <int OCT>
 __device__ __forceinline__ bool slab(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
                                      float tmin, float tmax, float* tnear) {
-  const float tnx = fmaf((OCT & 1) ? hx : lx, r.ix, -r.oix), tfx = fmaf((OCT & 1) ? lx : hx, r.ix, -r.oix);
-  const float tny = fmaf((OCT & 2) ? hy : ly, r.iy, -r.oiy), tfy = fmaf((OCT & 2) ? ly : hy, r.iy, -r.oiy);
-  const float tnz = fmaf((OCT & 4) ? hz : lz, r.iz, -r.oiz), tfz = fmaf((OCT & 4) ? lz : hz, r.iz, -r.oiz);
+  const float ix = r.ixy.x, iy = r.ixy.y, iz = r.izz.x, nx = r.nxy.x, ny = r.nxy.y, nz = r.nzz.x;
+  const float tnx = fmaf((OCT & 1) ? hx : lx, ix, nx), tfx = fmaf((OCT & 1) ? lx : hx, ix, nx);
+  const float tny = fmaf((OCT & 2) ? hy : ly, iy, ny), tfy = fmaf((OCT & 2) ? ly : hy, iy, ny);
+  const float tnz = fmaf((OCT & 4) ? hz : lz, iz, nz), tfz = fmaf((OCT & 4) ? lz : hz, iz, nz);
   const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
   const float tf = fmin3(tfx, tfy, fminf(tfz, tmax));
   *tnear = tn;
@@ -159,8 +174,8 @@ __device__ __forceinline__ void packet_traverse(const RayCtx& r, bool& active, c
       float tn0 = 0.f, tn1 = 0.f;
       if (test) {
         const float lim = prune_limit(tbest);
-        h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
-        h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
+        h0 = slab<OCT>(r, n0.x, n0.y, n2.x, n0.z, n0.w, n2.y, tmin, lim, &tn0);
+        h1 = slab<OCT>(r, n1.x, n1.y, n2.z, n1.z, n1.w, n2.w, tmin, lim, &tn1);
       }
       const unsigned b0 = __ballot_sync(kFull, h0), b1 = __ballot_sync(kFull, h1);
       const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
@@ -221,8 +236,8 @@ __device__ __forceinline__ void lane_traverse(const RayCtx& r, bool& active, con
       ldg_node(nodes + 4 * cur, n0, n1, n2, n3);
       float tn0, tn1;
       const float lim = prune_limit(tbest);
-      const bool h0 = slab<OCT>(r, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tmin, lim, &tn0);
-      const bool h1 = slab<OCT>(r, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tmin, lim, &tn1);
+      const bool h0 = slab<OCT>(r, n0.x, n0.y, n2.x, n0.z, n0.w, n2.y, tmin, lim, &tn0);
+      const bool h1 = slab<OCT>(r, n1.x, n1.y, n2.z, n1.z, n1.w, n2.w, tmin, lim, &tn1);
       const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
       if (h0 && h1) {
         const bool first0 = tn0 <= tn1;
@@ -402,13 +417,28 @@ __device__ __forceinline__ Shaded trace_sample(const A& a, bool valid, float ox,
 // directions within a warp).
 __device__ __forceinline__ bool slab_rt(const RayCtx& r, float lx, float ly, float lz, float hx, float hy, float hz,
                                         float tmin, float tmax, float* tnear) {
-  const float ax = fmaf(lx, r.ix, -r.oix), bx = fmaf(hx, r.ix, -r.oix);
-  const float ay = fmaf(ly, r.iy, -r.oiy), by = fmaf(hy, r.iy, -r.oiy);
-  const float az = fmaf(lz, r.iz, -r.oiz), bz = fmaf(hz, r.iz, -r.oiz);
+  const float ix = r.ixy.x, iy = r.ixy.y, iz = r.izz.x, nx = r.nxy.x, ny = r.nxy.y, nz = r.nzz.x;
+  const float ax = fmaf(lx, ix, nx), bx = fmaf(hx, ix, nx);
+  const float ay = fmaf(ly, iy, ny), by = fmaf(hy, iy, ny);
+  const float az = fmaf(lz, iz, nz), bz = fmaf(hz, iz, nz);
   const float tn = fmax3(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
   const float tf = fmin3(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
   *tnear = tn;
   return tn <= tf;
+}
+
+// Both children of a binary node (vlbk::pack_node's layout) against a ray whose
+// octant differs per lane: the same terms and min/max as slab_rt, the six
+// pairs of plane crossings from six packed FMAs instead of twelve.
+__device__ __forceinline__ void slab_pair_rt(const RayCtx& r, const float4 q0, const float4 q1, const float4 q2,
+                                             float tmin, float tmax, bool& h0, bool& h1, float& tn0, float& tn1) {
+  const float2 l0 = fma_pair(q0.x, q0.y, r.ixy, r.nxy), u0 = fma_pair(q0.z, q0.w, r.ixy, r.nxy);
+  const float2 l1 = fma_pair(q1.x, q1.y, r.ixy, r.nxy), u1 = fma_pair(q1.z, q1.w, r.ixy, r.nxy);
+  const float2 z0 = fma_pair(q2.x, q2.y, r.izz, r.nzz), z1 = fma_pair(q2.z, q2.w, r.izz, r.nzz);
+  tn0 = fmax3(fminf(l0.x, u0.x), fminf(l0.y, u0.y), fmaxf(fminf(z0.x, z0.y), tmin));
+  tn1 = fmax3(fminf(l1.x, u1.x), fminf(l1.y, u1.y), fmaxf(fminf(z1.x, z1.y), tmin));
+  h0 = tn0 <= fmin3(fmaxf(l0.x, u0.x), fmaxf(l0.y, u0.y), fminf(fmaxf(z0.x, z0.y), tmax));
+  h1 = tn1 <= fmin3(fmaxf(l1.x, u1.x), fmaxf(l1.y, u1.y), fminf(fmaxf(z1.x, z1.y), tmax));
 }
 
 __device__ __forceinline__ uint32_t lane_lt_mask() {
@@ -692,7 +722,10 @@ __device__ __forceinline__ void lr_node_wide(const A& a, LaneRay& L, int* stack,
 // One inner node: nearer hit child next, the farther one on the stack.  WIDE:
 // the node is a node of the 8-wide tree (kernels built for it walk it when
 // the scene has one; the others walk the binary tree, with the same results).
-template <bool COUNT, class A, bool WIDE = false>
+// PACKED: the box tests' plane crossings by packed FMAs (slab_pair_rt), else
+// by scalar ones (slab_rt; the same bits, for kernels whose registers do not
+// leave room for the pairs).
+template <bool COUNT, class A, bool WIDE = false, bool PACKED = true>
 __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work& w) {
   if constexpr (WIDE) {
     lr_node_wide<COUNT>(a, L, stack, w);
@@ -704,9 +737,14 @@ __device__ __forceinline__ void lr_node(const A& a, LaneRay& L, int* stack, Work
   float4 n0, n1, n2, n3;
   ldg_node(a.nodes + 4 * L.cur, n0, n1, n2, n3);
   float tn0, tn1;
-  const float lim = prune_limit(L.tb);
-  const bool h0 = slab_rt(L.ray, n0.x, n0.y, n0.z, n0.w, n1.x, n1.y, tlo, lim, &tn0);
-  const bool h1 = slab_rt(L.ray, n1.z, n1.w, n2.x, n2.y, n2.z, n2.w, tlo, lim, &tn1);
+  bool h0, h1;
+  if constexpr (PACKED) {
+    slab_pair_rt(L.ray, n0, n1, n2, tlo, prune_limit(L.tb), h0, h1, tn0, tn1);
+  } else {
+    const float lim = prune_limit(L.tb);
+    h0 = slab_rt(L.ray, n0.x, n0.y, n2.x, n0.z, n0.w, n2.y, tlo, lim, &tn0);
+    h1 = slab_rt(L.ray, n1.x, n1.y, n2.z, n1.z, n1.w, n2.w, tlo, lim, &tn1);
+  }
   const int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
   if (h0 && h1) {
     const bool first0 = tn0 <= tn1;

@@ -6,6 +6,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
@@ -46,6 +47,37 @@ __device__ __forceinline__ bool inb_checked(long long i, long long n, int* err) 
 // the per-lane stacks of the lane walks (a wide node pushes up to 7 children).
 constexpr int kTraceStack = 64;
 constexpr int kLaneStack = 96;
+
+// ---- binary traversal node (64 bytes) -------------------------------------------
+// The two children's boxes (lo xyz, hi xyz) grouped by axis, so that one
+// packed FMA (fma.rn.f32x2) takes one child's x and y planes, or its two z
+// planes, at once, then the children's references (>= 0 a node slot, < 0 the
+// complement of a triangle slot):
+//   [lx0 ly0 hx0 hy0] [lx1 ly1 hx1 hy1] [lz0 hz0 lz1 hz1] [ref0 ref1 0 0]
+#ifdef __CUDACC__
+#define VLB_HD __host__ __device__
+#else
+#define VLB_HD
+#endif
+VLB_HD inline float ref_bits(int32_t r) {
+  float f;
+  std::memcpy(&f, &r, 4);
+  return f;
+}
+VLB_HD inline void pack_node(float4* q, const float* b0, const float* b1, int32_t c0, int32_t c1) {
+  q[0] = make_float4(b0[0], b0[1], b0[3], b0[4]);
+  q[1] = make_float4(b1[0], b1[1], b1[3], b1[4]);
+  q[2] = make_float4(b0[2], b0[5], b1[2], b1[5]);
+  q[3] = make_float4(ref_bits(c0), ref_bits(c1), 0.f, 0.f);
+}
+inline void unpack_node(const float4* q, float* b0, float* b1, int32_t* c0, int32_t* c1) {
+  const float x0[6] = {q[0].x, q[0].y, q[2].x, q[0].z, q[0].w, q[2].y};
+  const float x1[6] = {q[1].x, q[1].y, q[2].z, q[1].z, q[1].w, q[2].w};
+  std::memcpy(b0, x0, sizeof x0);
+  std::memcpy(b1, x1, sizeof x1);
+  std::memcpy(c0, &q[3].x, 4);
+  std::memcpy(c1, &q[3].y, 4);
+}
 
 // ---- skybox projection ------------------------------------------------------
 struct SkyboxArgs {

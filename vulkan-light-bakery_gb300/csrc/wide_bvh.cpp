@@ -44,16 +44,9 @@ float area(const float* b) {
   return dx * dy + dy * dz + dz * dx;
 }
 
-// The two children of binary node i (64-byte node: boxes then refs).
+// The two children of binary node i (the 64-byte layout of vlbk::pack_node).
 void binary_children(const float4* nodes, int32_t i, Child* c0, Child* c1) {
-  const float4 n0 = nodes[4 * size_t(i)], n1 = nodes[4 * size_t(i) + 1], n2 = nodes[4 * size_t(i) + 2],
-               n3 = nodes[4 * size_t(i) + 3];
-  const float b0[6] = {n0.x, n0.y, n0.z, n0.w, n1.x, n1.y};
-  const float b1[6] = {n1.z, n1.w, n2.x, n2.y, n2.z, n2.w};
-  std::memcpy(c0->box, b0, sizeof b0);
-  std::memcpy(c1->box, b1, sizeof b1);
-  std::memcpy(&c0->ref, &n3.x, 4);
-  std::memcpy(&c1->ref, &n3.y, 4);
+  vlbk::unpack_node(nodes + 4 * size_t(i), c0->box, c1->box, &c0->ref, &c1->ref);
 }
 
 // Quantises one axis of a wide node: scale 2^(e-127) and the bytes of each
