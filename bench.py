@@ -60,8 +60,8 @@ TRACE_NCU = {
                    "dram_bytes": 3454300000, "warp_instructions": 130316900000,
                    "l1tex_throughput_pct": 77.0, "issue_active_pct": 75.7},
     "trace_fused_lane": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
-                         "dram_bytes": 266100000, "warp_instructions": 144591000000,
-                         "l1tex_throughput_pct": 82.8, "issue_active_pct": 70.0},
+                         "dram_bytes": 86500000, "warp_instructions": 125671000000,
+                         "l1tex_throughput_pct": 71.4, "issue_active_pct": 70.3},
 }
 
 
