@@ -57,8 +57,8 @@ METRIC_FULL = "probes/s, Grays/s, p99 bake latency of the default path, <=1e-4 S
 # per launch of the headline workload, ncu's L1 and issue utilisation.
 TRACE_NCU = {
     "trace_tile": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
-                   "dram_bytes": 3454300000, "warp_instructions": 130316900000,
-                   "l1tex_throughput_pct": 77.0, "issue_active_pct": 75.7},
+                   "dram_bytes": 3415800000, "warp_instructions": 126470600000,
+                   "l1tex_throughput_pct": 79.8, "issue_active_pct": 75.4},
     "trace_fused_lane": {"capture": "profiles/trace_tile_c2.md", "scaled_from": "32^3 probes x 8",
                          "dram_bytes": 86500000, "warp_instructions": 125671000000,
                          "l1tex_throughput_pct": 71.4, "issue_active_pct": 70.3},
@@ -296,10 +296,11 @@ def accuracy_vs_fp64(ctx, scene, probes, params, pos, idx, alb, sky, sun, nsampl
 
 
 def trace_roofline(kname, k_avg_ms, stats, clk, sms, hbm_peak, peaks_measured, P, ntri, K, C, tile):
-    """Roofline of the trace kernel.  It is bound by instruction issue and L1
-    throughput together (the scene's nodes and triangles stay in L1/L2), not
-    by HBM: `bound` is the issue view, with the L1 view beside (the committed
-    ncu capture shows both near 76 %).  L1: the node and triangle bytes the lanes
+    """Roofline of the trace kernel.  It is bound by L1 throughput and
+    instruction issue together (the scene's nodes and triangles stay in
+    L1/L2), not by HBM: `bound` is the issue view, the one measured live, with
+    the L1 view beside (the committed ncu capture shows the L1 data stage at
+    80 % and issue at 75 %).  L1: the node and triangle bytes the lanes
     request (counted by an instrumented bake of the same rays) over the live
     launch time, against the nominal 128 B/clock/SM.  Issue: the capture's
     warp instructions per launch over the live launch time, against 4 issue
@@ -737,14 +738,14 @@ def batch_volumes(seed=SEED, nvol=256):
 
 
 def refbake_measure(ctx, torch, stream, steps, hbm_peak, reps=3):
-    """The reference baker's own workload on the config-1 scene: a 7^3 probe grid
+    """The reference baker's own workload on the 64-box scene: a 7^3 probe grid
     over the origin-inclusive bounds in the reference's order, one ray per pixel
     of the 3141 x 1000 equirect env map (3,141,000 rays per probe, 1.08e9 in
     all), L3 (16 coefficients), fused, plain FP32 and mixed; device-resident
     probes and output, L2 flushed before each bake."""
     import vlb
 
-    pos, idx, alb, sky, sun, _ = grid_probes(vlb, 64, (16, 16, 16))  # the config-1 scene
+    pos, idx, alb, sky, sun, _ = grid_probes(vlb, 64, (16, 16, 16))  # the 64-box (778-triangle) scene
     scene = ctx.scene(pos, idx, alb)
     probes, _ = vlb.probe_grid_ref_order(scene.bounds(include_origin=True), (7, 7, 7))
     P, W, H = probes.shape[0], 3141, 1000
@@ -753,7 +754,7 @@ def refbake_measure(ctx, torch, stream, steps, hbm_peak, reps=3):
     d_probes = torch.from_numpy(probes).cuda()
     out = torch.empty((P, 16, 3), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    res = {"workload": f"{P} probes (7^3 reference grid) x {W}x{H} equirect rays, config-1 scene, L3",
+    res = {"workload": f"{P} probes (7^3 reference grid) x {W}x{H} equirect rays, 64-box scene, L3",
            "primary_rays": P * W * H}
     for name, prec in (("fused", vlb.PREC_FUSED), ("fp32", vlb.PREC_FP32), ("mixed_bf16_hilo_tcgen05", vlb.PREC_MIXED)):
         p = vlb.bake_params(ds, 3, prec, sun, sky=skyh)

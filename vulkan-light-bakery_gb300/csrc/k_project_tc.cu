@@ -253,7 +253,7 @@ bool make_map(CUtensorMap* m, const void* ptr, uint64_t inner, uint64_t outer, u
 // chunks at the swizzled positions (chunk q of row r sits at q ^ (r & 7):
 // eight consecutive rows hit eight different bank groups, no conflicts).
 // Persistent CTAs take row tiles in turn.  A two-stage ring keeps three CTAs
-// (twelve consumer warps) on an SM: measured on the config-2 tile [786,432 x
+// (twelve consumer warps) on an SM: measured on the tile [786,432 x
 // 1024] at 92 % of the HBM copy rate (three stages, two CTAs: 74 %; one row a
 // thread: 49 %; the cp.async kernel k_project<float>: 62 %).
 constexpr int kF32Rows = 256, kF32Cols = 32;  // two rows a consumer thread: t and t + 128

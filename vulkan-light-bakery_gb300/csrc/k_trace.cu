@@ -229,7 +229,8 @@ __device__ __forceinline__ void emit_tile(const TraceArgs& a, const LaneRay& L, 
 
 template <bool COUNT, bool WIDE, bool REF>
 // Nine resident CTAs per SM (at most 56 registers): measured 1.7 % faster on
-// the config-2 bake than the unconstrained 60 registers (eight CTAs).
+// the 64^3-probe, 1024-direction bake than the unconstrained 60 registers
+// (eight CTAs).
 __global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs a) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t P = (a.nprobes + 31) / 32 * 32;
@@ -244,7 +245,8 @@ __global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs 
   // to its lanes one by one: its next rays then reuse the nodes its last ones
   // fetched.  Blocks are sized by the rays per warp, so that every warp still
   // takes about 64 blocks (the load stays balanced): up to 16 groups on the
-  // config-2 bake (9.5 % faster than one group), one group on small bakes.
+  // 64^3-probe, 1024-direction bake (9.5 % faster than one group), one group
+  // on small bakes.
   // the warp's block (next ray, end) lives in shared memory: it is touched only
   // when the warp takes rays, and the walk's registers stay free
   __shared__ uint32_t s_block[kTraceWarps][2];
@@ -286,14 +288,8 @@ __global__ void __launch_bounds__(kTraceThreads, 9) k_trace_dyn(const TraceArgs 
       if (exhausted) break;
       continue;
     }
-    // node phase (all lanes take part in the vote)
-#pragma unroll 1
-    for (int k = 0; k < kNodeSteps; ++k) {
-      lr_park(L, stack);
-      const bool at_node = L.has && L.cur >= 0;
-      if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
-      if (at_node) lr_node<COUNT, TraceArgs, WIDE>(a, L, stack, w);
-    }
+    // node phase (all lanes take part in the votes)
+    lr_node_phase<COUNT, TraceArgs, WIDE>(a, L, stack, w, kNodeSteps);
     lr_park(L, stack);
     if (!L.has) continue;
     // leaf phase
@@ -800,14 +796,9 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
         if (r0 >= r1) break;
         continue;
       }
-      // one while-while turn, as in k_trace_dyn
-#pragma unroll 1
-      for (int k = 0; k < kNodeSteps; ++k) {
-        lr_park(L, stack);
-        const bool at_node = L.has && L.cur >= 0;
-        if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
-        if (at_node) lr_node<false>(j, L, stack, w);
-      }
+      // one while-while turn, as in k_trace_dyn (the octant-specialised node
+      // phase measured 4 % slower here: short direction sets mix octants)
+      lr_node_steps<false, BakeJobDev, false, true, -1>(j, L, stack, w, kNodeSteps);
       lr_park(L, stack);
       if (!L.has) continue;
       if (L.leaf >= 0) lr_leaf<false>(j, L, w);

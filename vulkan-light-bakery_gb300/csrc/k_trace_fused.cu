@@ -262,13 +262,8 @@ __global__ void __launch_bounds__(kTraceThreads, MINB) k_trace_fused(const BakeJ
     if (__any_sync(kFull, L.has)) {
       const BakeJobDev& J = job_of<MULTI>(jobs, one, fw.q[lslot >> 8].job);
       // one while-while turn (as k_trace_dyn): node phase, then leaf phase
-#pragma unroll 1
-      for (uint32_t k = 0; k < node_steps; ++k) {
-        lr_park(L, stack);
-        const bool at_node = L.has && L.cur >= 0;
-        if (!__any_sync(kFull, at_node && L.leaf < 0)) break;
-        if (at_node) lr_node<false, BakeJobDev, false, !MULTI>(J, L, stack, w);
-      }
+      // (the octant-specialised node phase gained nothing here)
+      lr_node_steps<false, BakeJobDev, false, !MULTI, -1>(J, L, stack, w, node_steps);
       lr_park(L, stack);
       if (L.has) {
         if (L.leaf >= 0) lr_leaf<false>(J, L, w);

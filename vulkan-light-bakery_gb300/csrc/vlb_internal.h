@@ -322,7 +322,7 @@ struct BakeJobDev {
 // most 4 chunks per probe while a chunk holds at most 4096 rays (larger sets,
 // such as the 3141 x 1000 equirect set, get more chunks).  Large chunks keep
 // a warp on one probe's neighbouring directions for longer, so its rays reuse
-// the nodes it just fetched (4 chunks of 256 rays on the config-2 bake:
+// the nodes it just fetched (4 chunks of 256 rays on the 64^3-probe, 1024-direction bake:
 // 9.5 % faster than 16 of 64).  A function of S alone, so a probe's sums have
 // the same order in a single bake and in any batch.
 constexpr uint32_t kFusedSubRays = 64;
