@@ -24,3 +24,22 @@ def test_reference_arm_loads_no_product_library():
     import bench
 
     assert ref["config"] == bench.config_dict(262144, 49162)
+
+
+def test_trace_roofline_is_the_live_issue_view():
+    """The trace kernel's roofline: the committed capture's warp instructions
+    per launch over the live launch time, against 4 issue slots per SM clock;
+    the capture's DRAM bytes are the traffic."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    stats = {"bytes": 1.5e12, "node_tests_per_ray": 58.0, "node_fetches_per_ray": 58.0}
+    for kname in ("trace_tile", "trace_fused_lane"):
+        ncu = bench.TRACE_NCU[kname]
+        r = bench.trace_roofline(kname, 125.0, stats, {"sm_max_mhz": 2070.0}, 152, 6788.6, True, 262144, 49162, 9,
+                                 4, kname == "trace_tile")
+        assert r["bound"] == "issue" and r["unit"] == "warp instructions/s"
+        assert abs(r["achieved"] - ncu["warp_instructions"] / 0.125) <= 1e-9 * r["achieved"]
+        assert abs(r["frac"] - r["achieved"] / (152 * 4 * 2070e6)) <= 1e-12
+        assert 0 < r["frac"] < 1.2 and r["traffic"] == ncu["dram_bytes"]
+        assert r["l1"]["requested_bytes_per_launch"] == stats["bytes"]
