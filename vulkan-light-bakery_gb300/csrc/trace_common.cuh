@@ -722,7 +722,10 @@ __device__ __forceinline__ void lr_node_wide(const A& a, LaneRay& L, int* stack,
 // slab_pair_rt for a ray in octant OCT (bit a set: 1/d_a < 0): each axis's
 // entry and exit planes are known, so the per-axis min/max goes.  The same
 // bits as slab_pair_rt: a plane crossing fma(p, inv, -o * inv) is monotone in
-// p, so the entry plane's crossing is the minimum of the two.
+// p, so the entry plane's crossing is the minimum of the two.  (A crossing is
+// NaN only when p * inv and o * inv both overflow -- a direction component
+// below 1e-30, so inv = +-1e30, with coordinates beyond 3.4e8 -- and there
+// the two forms may differ, as the packet walk's compile-time octant may.)
 template <int OCT>
 __device__ __forceinline__ void slab_pair_oct(const RayCtx& r, const float4 q0, const float4 q1, const float4 q2,
                                               float tmin, float tmax, bool& h0, bool& h1, float& tn0, float& tn1) {
