@@ -797,7 +797,9 @@ __global__ void __launch_bounds__(kTraceThreads, 8) k_trace_batch(const BakeJobD
         continue;
       }
       // one while-while turn, as in k_trace_dyn (the octant-specialised node
-      // phase measured 4 % slower here: short direction sets mix octants)
+      // phase measured 4 % slower here, also when only jobs of 1024
+      // directions take it: its eight copies cost this kernel more than they
+      // save)
       lr_node_steps<false, BakeJobDev, false, true, -1>(j, L, stack, w, kNodeSteps);
       lr_park(L, stack);
       if (!L.has) continue;
