@@ -827,9 +827,9 @@ __device__ __forceinline__ void lr_node_steps(const A& a, LaneRay& L, int* stack
 // A turn's node phase, specialised to the warp's octant when all its rays
 // share one (the binary tree's packed walk; the others take the generic one).
 // Measured on the single-bake tile walk: 129.3 -> 125.7 ms on the bake of
-// 64^3 probes x 1024 directions in the 4096-box scene; the vote costs a few
-// instructions a turn, which the multi-job walks (short direction sets, mixed
-// octants) do not win back.
+// 64^3 probes x 1024 directions in the 4096-box scene; the multi-job walks
+// measured 4 % slower with it (also when only jobs of 1024 directions took
+// it) and keep the generic phase.
 template <bool COUNT, class A, bool WIDE = false, bool PACKED = true>
 __device__ __forceinline__ void lr_node_phase(const A& a, LaneRay& L, int* stack, Work& w, uint32_t steps) {
   if constexpr (WIDE || !PACKED) {
