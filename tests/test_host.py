@@ -128,3 +128,46 @@ def test_service_admission_plan():
     for k in range(n):  # each batch within the caps, and no batch could take the next request
         sel = b == k
         assert by[sel].sum() <= 1 << 22 and (p[sel].sum() <= 16384 or sel.sum() == 1)
+
+
+def test_node_layout_round_trip(tmp_path):
+    """The binary node layout (boxes grouped by axis for the packed box tests):
+    pack_node then unpack_node returns both boxes and both references, and the
+    packed FMA operands sit where the walk reads them -- (lo x, lo y) and
+    (hi x, hi y) of each child in one float4, the four z planes in the third."""
+    import shutil
+    import subprocess
+
+    import vlb_build
+
+    try:
+        cuda_inc = vlb_build._cuda_home() / "include"
+    except RuntimeError:
+        pytest.skip("needs nvcc's CUDA headers")
+    if not shutil.which("g++") or not (cuda_inc / "cuda_runtime.h").exists():
+        pytest.skip("needs g++ and the CUDA headers")
+    src = tmp_path / "node.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "vlb_internal.h"
+int main() {
+  const float b0[6] = {1, 2, 3, 4, 5, 6}, b1[6] = {-1, -2, -3, 7, 8, 9};
+  float4 q[4];
+  vlbk::pack_node(q, b0, b1, 5, ~7);
+  float c0[6], c1[6];
+  int32_t r0, r1;
+  vlbk::unpack_node(q, c0, c1, &r0, &r1);
+  for (int i = 0; i < 6; ++i) if (c0[i] != b0[i] || c1[i] != b1[i]) return 1;
+  if (r0 != 5 || r1 != ~7) return 2;
+  if (q[0].x != 1 || q[0].y != 2 || q[0].z != 4 || q[0].w != 5) return 3;
+  if (q[1].x != -1 || q[1].y != -2 || q[1].z != 7 || q[1].w != 8) return 4;
+  if (q[2].x != 3 || q[2].y != 6 || q[2].z != -3 || q[2].w != 9) return 5;
+  std::puts("ok");
+  return 0;
+}
+''')
+    exe = tmp_path / "node"
+    csrc = ROOT / "vulkan-light-bakery_gb300" / "csrc"
+    subprocess.run(["g++", "-std=c++17", f"-I{csrc}", f"-I{cuda_inc}", str(src), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout)
